@@ -1,0 +1,122 @@
+/*
+ * nextla_gb300.h - C ABI of the GB300 (sm_103a) implementation of NextLA.jl's
+ * recursive triangular solve / multiply.
+ *
+ * Conventions shared by every entry point:
+ *  - Matrices are column-major with an explicit leading dimension, as Julia
+ *    stores them; element (i,j) of X is X[i + j*ldx].  A transposed operand is
+ *    passed as the untransposed parent with a transpose flag, which is how a
+ *    Julia `Transpose(A)` view or a strided SubArray reaches the library.
+ *  - All pointers are device pointers owned by the caller, except where a
+ *    comment says "host".  Nothing is freed or retained by the library.
+ *  - Work is enqueued on `stream` (a cudaStream_t; NULL is the legacy default
+ *    stream) and runs asynchronously; the caller synchronises, as the
+ *    reference's callers do (test/unified_rectrxm.jl:34).
+ *  - Every call returns NLA_OK (0) or a negative status; nla_last_error()
+ *    then describes the failure for the calling thread.
+ *  - Character flags are the reference's: side 'L'/'R', uplo 'L'/'U',
+ *    trans 'N'/'T'/'C' ('C' equals 'T' for real data), func 'S' (solve,
+ *    TRSM) / 'M' (multiply, TRMM).  Unlike the reference, which silently
+ *    falls through to a default branch on an unknown character
+ *    (src/rectrxm.jl:104-124), unknown characters are rejected with
+ *    NLA_ERR_ARG.
+ */
+#ifndef NEXTLA_GB300_H
+#define NEXTLA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define NLA_API __attribute__((visibility("default")))
+#else
+#define NLA_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Element types (Float16, Float32, Float64). */
+#define NLA_F16 0
+#define NLA_F32 1
+#define NLA_F64 2
+
+/* Status codes. */
+#define NLA_OK 0
+#define NLA_ERR_ARG -1         /* bad flag, size, leading dimension or null pointer */
+#define NLA_ERR_DTYPE -2       /* element type not supported by this entry point */
+#define NLA_ERR_UNSUPPORTED -3 /* valid request this build does not implement */
+#define NLA_ERR_WORKSPACE -4   /* caller-provided workspace too small */
+#define NLA_ERR_TIMEOUT -5     /* a bounded device-side wait gave up */
+#define NLA_ERR_NOMEM -6       /* device allocation failed */
+#define NLA_ERR_CUDA_BASE -100 /* NLA_ERR_CUDA_BASE - cudaError_t for CUDA errors */
+
+/* Library version (major*10000 + minor*100 + patch). */
+NLA_API int nla_version(void);
+
+/* Description of the last failure on the calling thread ("" if none). */
+NLA_API const char* nla_last_error(void);
+
+/*
+ * unified_rectrxm!(side, uplo, trans, alpha, func, A, B)
+ * Replaces src/rectrxm.jl:43-76 (with the recursion unified_rec,
+ * src/rectrxm.jl:101-198) for one GPU.  The whole recursion runs in native
+ * host code; each base case and each off-diagonal update is one kernel launch.
+ *   func 'S': solve op(A) X = alpha B (side 'L') or X op(A) = alpha B ('R');
+ *   func 'M': B := alpha op(A) B ('L') or alpha B op(A) ('R').
+ * A is n x n (only the `uplo` triangle is read, diagonal non-unit); B is
+ * n x m for side 'L' and m x n for side 'R'; the result overwrites B.
+ * dtype is NLA_F16, NLA_F32 or NLA_F64 and applies to A and B.
+ * The recursion cut-offs are the library's tuned defaults (environment
+ * NLA_TRXM_CUTOFF_S / NLA_TRXM_CUTOFF_M override them).
+ */
+NLA_API int nla_trxm(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
+             const void* A, int64_t lda, void* B, int64_t ldb, void* stream);
+
+/*
+ * nla_trxm with explicit recursion cut-offs for solve and multiply (the
+ * reference's are 256 and 16, src/rectrxm.jl:52,63).  A cut-off <= 0 selects
+ * the default.  Solve cut-offs above 1024 are clamped to 1024.
+ */
+NLA_API int nla_trxm_ex(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
+                const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, void* stream);
+
+/*
+ * One base case of the recursion on a diagonal block.
+ * Replaces LeftLowerTRSM!/LeftUpperTRSM!/RightLowerTRSM!/RightUpperTRSM!
+ * (src/trsm.jl:128-150, kernels :5-126) for func 'S' and
+ * LeftLowerTRMM!/LeftUpperTRMM!/RightLowerTRMM!/RightUpperTRMM!
+ * (src/trmm.jl:332-389, kernels :43-312) for func 'M'.
+ * op(A) = A (transA 0) or A^T (transA 1) is the n x n triangle named by uplo
+ * (the reference passes Transpose views here); B is n x m (side 'L') or
+ * m x n (side 'R').  No alpha: the reference's base cases have none.
+ * n <= 1024 (the reference's shared buffers hold 1024 entries,
+ * src/trsm.jl:10-12).
+ */
+NLA_API int nla_diag_block(char func, char side, char uplo, int transA, int dtype, int64_t n, int64_t m, const void* A,
+                   int64_t lda, void* B, int64_t ldb, void* stream);
+
+/*
+ * The off-diagonal update: out (N x M) += alpha * op(in1) (N x R) * op(in2) (R x M).
+ * Replaces matmul! (src/matmul.jl:5-66) as launched by GEMM_ADD!
+ * (src/matmul.jl:69-74, alpha = +1) and GEMM_SUB! (src/matmul.jl:76-81,
+ * alpha = -1).  trans1/trans2 select op() = transpose (1) or identity (0),
+ * matching matmul!'s transA/transB arguments for real data.  Float16 inputs
+ * accumulate in Float32 (the reference accumulates in Float16).
+ * `out` must not overlap `in1` or `in2`.
+ */
+NLA_API int nla_gemm_update(int dtype, int trans1, int trans2, int64_t N, int64_t R, int64_t M, double alpha,
+                    const void* in1, int64_t ld1, const void* in2, int64_t ld2, void* out, int64_t ldo, void* stream);
+
+/*
+ * B .= alpha .* B (src/rectrxm.jl:64,72): each element is multiplied by alpha
+ * in Float64 and rounded back to the element type, as Julia's promotion does.
+ */
+NLA_API int nla_scale(int dtype, int64_t rows, int64_t cols, double alpha, void* B, int64_t ldb, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NEXTLA_GB300_H */

@@ -1,0 +1,85 @@
+"""ctypes binding of ``libnextla_gb300.so`` (the C ABI in include/nextla_gb300.h).
+
+The library is the only compute path: if it cannot be loaded, every entry
+point raises.  There is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnextla_gb300.so")
+
+NLA_F16, NLA_F32, NLA_F64 = 0, 1, 2
+NLA_OK = 0
+NLA_ERR_ARG = -1
+NLA_ERR_DTYPE = -2
+NLA_ERR_UNSUPPORTED = -3
+NLA_ERR_WORKSPACE = -4
+NLA_ERR_TIMEOUT = -5
+NLA_ERR_NOMEM = -6
+NLA_ERR_CUDA_BASE = -100
+
+# Every symbol declared in include/nextla_gb300.h, with its ctypes signature.
+_i32, _i64, _d, _c, _p, _sz = (ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_char, ctypes.c_void_p,
+                               ctypes.c_size_t)
+SIGNATURES = {
+    "nla_version": ([], _i32),
+    "nla_last_error": ([], ctypes.c_char_p),
+    "nla_trxm": ([_c, _c, _c, _d, _c, _i32, _i64, _i64, _p, _i64, _p, _i64, _p], _i32),
+    "nla_trxm_ex": ([_c, _c, _c, _d, _c, _i32, _i64, _i64, _p, _i64, _p, _i64, _i64, _i64, _p], _i32),
+    "nla_diag_block": ([_c, _c, _c, _i32, _i32, _i64, _i64, _p, _i64, _p, _i64, _p], _i32),
+    "nla_gemm_update": ([_i32, _i32, _i32, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _p, _i64, _p], _i32),
+    "nla_scale": ([_i32, _i64, _i64, _d, _p, _i64, _p], _i32),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class NLAError(RuntimeError):
+    """A negative status from the library, with its message."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (status %d)" % (msg or "nextla_gb300 error", code))
+        self.code = code
+
+
+class NLAArgumentError(NLAError, ValueError):
+    """Invalid arguments (the reference would have fallen through silently)."""
+
+
+def load(path: str | None = None):
+    """Load the library (built in-tree by build.py) and declare signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise ImportError("libnextla_gb300.so is not built (run nextla.jl_gb300/build.py or "
+                              "__graft_entry__.build())")
+        L = ctypes.CDLL(p)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+        return _lib
+
+
+def check(rc: int) -> None:
+    if rc == NLA_OK:
+        return
+    msg = load().nla_last_error()
+    msg = msg.decode() if msg else ""
+    if rc in (NLA_ERR_ARG, NLA_ERR_DTYPE):
+        raise NLAArgumentError(rc, msg)
+    raise NLAError(rc, msg)
+
+
+def ch(c: str):
+    return ctypes.c_char(c.encode() if isinstance(c, str) else c)

@@ -1,0 +1,276 @@
+// C ABI entry points and the native host recursion of unified_rectrxm!.
+//
+// nla_trxm mirrors src/rectrxm.jl:43-198: the trans flag becomes a transposed
+// view of A with uplo flipped (src/rectrxm.jl:56-59), alpha scales B before a
+// solve (:62-65) and after a multiply (:71-73), and the recursion splits at
+// n/2 for powers of two and at the largest power of two below n otherwise
+// (:129-133), with the forward (A11 -> GEMM -> A22) or backward ordering of
+// :153-197.  Each base case is one launch of the diagonal-block kernel and
+// each update one launch of the GEMM kernel, all on the caller's stream.
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "nla_common.cuh"
+
+namespace nla {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+void clear_error() { g_last_error.clear(); }
+int fail(int code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+int cuda_status(cudaError_t e, const char* where) {
+  set_error(std::string(where) + ": " + cudaGetErrorString(e));
+  return NLA_ERR_CUDA_BASE - (int)e;
+}
+
+int num_sms() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+
+// ---------------------------------------------------------------------------
+// Alpha scaling: B .= alpha .* B with the product formed in Float64 and
+// rounded back to the element type (src/rectrxm.jl:64,72).  When alpha is
+// exactly representable in Float32 the Float32 product of a Float32/Float16
+// element is already the correctly rounded result, so no FP64 operation is
+// issued (GB300 runs FP64 at 1/64 of the FP32 rate).
+// ---------------------------------------------------------------------------
+template <typename T, typename Tm>
+__global__ void scale_kernel(int64_t rows, int64_t cols, Tm alpha, T* B, int64_t ldb, int tB) {
+  const int64_t total = rows * cols;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i, j;
+    if (!tB) { i = idx % rows; j = idx / rows; }
+    else { j = idx % cols; i = idx / cols; }
+    T* p = B + mat_off(i, j, ldb, tB);
+    Tm v = (Tm)Elem<T>::load(p) * alpha;
+    if constexpr (sizeof(Tm) == 8) Elem<T>::store_d(p, (double)v);  // one rounding from the Float64 product
+    else Elem<T>::store(p, v);
+  }
+}
+
+int launch_scale(int dtype, int64_t rows, int64_t cols, double alpha, const Mat& B, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0 || alpha == 1.0) return NLA_OK;
+  const int64_t total = rows * cols;
+  int64_t blocks = (total + 255) / 256;
+  const int64_t cap = (int64_t)num_sms() * 8;
+  if (blocks > cap) blocks = cap;
+  const bool f32_exact = (double)(float)alpha == alpha;
+  switch (dtype) {
+    case NLA_F64:
+      scale_kernel<double, double><<<(unsigned)blocks, 256, 0, s>>>(rows, cols, alpha, (double*)B.p, B.ld, B.t);
+      break;
+    case NLA_F32:
+      if (f32_exact)
+        scale_kernel<float, float><<<(unsigned)blocks, 256, 0, s>>>(rows, cols, (float)alpha, (float*)B.p, B.ld, B.t);
+      else
+        scale_kernel<float, double><<<(unsigned)blocks, 256, 0, s>>>(rows, cols, alpha, (float*)B.p, B.ld, B.t);
+      break;
+    case NLA_F16:
+      if (f32_exact)
+        scale_kernel<__half, float><<<(unsigned)blocks, 256, 0, s>>>(rows, cols, (float)alpha, (__half*)B.p, B.ld,
+                                                                      B.t);
+      else
+        scale_kernel<__half, double><<<(unsigned)blocks, 256, 0, s>>>(rows, cols, alpha, (__half*)B.p, B.ld, B.t);
+      break;
+    default: return fail(NLA_ERR_DTYPE, "scale: unknown dtype");
+  }
+  NLA_CHECK_LAUNCH("scale_kernel");
+  return NLA_OK;
+}
+
+int launch_gemm_simt(int dtype, int64_t N, int64_t M, int64_t K, double alpha, const Mat& A, const Mat& B,
+                     const Mat& C, cudaStream_t s);
+
+int launch_gemm(int dtype, int64_t N, int64_t M, int64_t K, double alpha, const Mat& A, const Mat& B, const Mat& C,
+                cudaStream_t s) {
+  return launch_gemm_simt(dtype, N, M, K, alpha, A, B, C, s);
+}
+
+// ---------------------------------------------------------------------------
+// Argument checks.
+// ---------------------------------------------------------------------------
+static bool valid_side(char c) { return c == 'L' || c == 'R'; }
+static bool valid_uplo(char c) { return c == 'L' || c == 'U'; }
+static bool valid_trans(char c) { return c == 'N' || c == 'T' || c == 'C'; }
+static bool valid_func(char c) { return c == 'S' || c == 'M'; }
+static bool valid_dtype(int d) { return d == NLA_F16 || d == NLA_F32 || d == NLA_F64; }
+
+static int check_flags(char side, char uplo, char trans, char func, int dtype) {
+  if (!valid_side(side)) return fail(NLA_ERR_ARG, std::string("side must be 'L' or 'R', got '") + side + "'");
+  if (!valid_uplo(uplo)) return fail(NLA_ERR_ARG, std::string("uplo must be 'L' or 'U', got '") + uplo + "'");
+  if (!valid_trans(trans))
+    return fail(NLA_ERR_ARG, std::string("transpose must be 'N', 'T' or 'C', got '") + trans + "'");
+  if (!valid_func(func)) return fail(NLA_ERR_ARG, std::string("func must be 'S' or 'M', got '") + func + "'");
+  if (!valid_dtype(dtype)) return fail(NLA_ERR_DTYPE, "dtype must be NLA_F16, NLA_F32 or NLA_F64");
+  return NLA_OK;
+}
+
+static int check_matrix(const char* name, const void* p, int64_t rows, int64_t cols, int64_t ld) {
+  if (rows < 0 || cols < 0) return fail(NLA_ERR_ARG, std::string(name) + ": negative dimension");
+  const int64_t need = rows > 1 ? rows : 1;
+  if (ld < need) return fail(NLA_ERR_ARG, std::string(name) + ": leading dimension smaller than the row count");
+  if (rows > 0 && cols > 0 && p == nullptr) return fail(NLA_ERR_ARG, std::string(name) + ": null pointer");
+  return NLA_OK;
+}
+
+// src/rectrxm.jl:129-133
+int64_t split_point(int64_t n) {
+  int64_t p = 1;
+  while (p * 2 <= n) p *= 2;
+  return p == n ? n / 2 : p;
+}
+
+// ---------------------------------------------------------------------------
+// Recursion (unified_rec, src/rectrxm.jl:101-198).
+// ---------------------------------------------------------------------------
+struct Rec {
+  char func, side, uplo;
+  int dtype;
+  int64_t m;
+  int64_t threshold;
+  cudaStream_t s;
+};
+
+static int rec(const Rec& c, const Mat& A, int64_t n, const Mat& B) {
+  if (n <= c.threshold) return launch_leaf(c.func, c.side, c.uplo, c.dtype, n, c.m, A, B, c.s);
+  const int64_t mid = split_point(n), rem = n - mid;
+  const int d = c.dtype;
+  const Mat A11 = A, A22 = sub(A, mid, mid, d), A21 = sub(A, mid, 0, d), A12 = sub(A, 0, mid, d);
+  const Mat B1 = B, B2 = c.side == 'L' ? sub(B, mid, 0, d) : sub(B, 0, mid, d);
+  const bool S = c.func == 'S', L = c.side == 'L';
+  const bool forward = (L && c.uplo == 'L' && S) || (!L && c.uplo == 'U' && S) || (L && c.uplo == 'U' && !S) ||
+                       (!L && c.uplo == 'L' && !S);
+  const int64_t m = c.m;
+  if (forward) {
+    NLA_TRY(rec(c, A11, mid, B1));
+    if (L) {
+      if (S) NLA_TRY(launch_gemm(d, rem, m, mid, -1.0, A21, B1, B2, c.s));  // B2 -= A21*B1
+      else NLA_TRY(launch_gemm(d, mid, m, rem, 1.0, A12, B2, B1, c.s));     // B1 += A12*B2
+    } else {
+      if (S) NLA_TRY(launch_gemm(d, m, rem, mid, -1.0, B1, A12, B2, c.s));  // B2 -= B1*A12
+      else NLA_TRY(launch_gemm(d, m, mid, rem, 1.0, B2, A21, B1, c.s));     // B1 += B2*A21
+    }
+    return rec(c, A22, rem, B2);
+  }
+  NLA_TRY(rec(c, A22, rem, B2));
+  if (L) {
+    if (S) NLA_TRY(launch_gemm(d, mid, m, rem, -1.0, A12, B2, B1, c.s));  // B1 -= A12*B2
+    else NLA_TRY(launch_gemm(d, rem, m, mid, 1.0, A21, B1, B2, c.s));     // B2 += A21*B1
+  } else {
+    if (S) NLA_TRY(launch_gemm(d, m, mid, rem, -1.0, B2, A21, B1, c.s));  // B1 -= B2*A21
+    else NLA_TRY(launch_gemm(d, m, rem, mid, 1.0, B1, A12, B2, c.s));     // B2 += B1*A12
+  }
+  return rec(c, A11, mid, B1);
+}
+
+static int64_t env_cutoff(const char* name, int64_t dflt) {
+  const char* v = std::getenv(name);
+  if (!v || !*v) return dflt;
+  long long x = std::atoll(v);
+  return x > 0 ? (int64_t)x : dflt;
+}
+
+int64_t default_cutoff(char func, int dtype) {
+  if (func == 'S') return env_cutoff("NLA_TRXM_CUTOFF_S", 256);
+  (void)dtype;
+  return env_cutoff("NLA_TRXM_CUTOFF_M", 128);
+}
+
+int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
+              const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m,
+              cudaStream_t s) {
+  NLA_TRY(check_flags(side, uplo, trans, func, dtype));
+  if (n < 0 || m < 0) return fail(NLA_ERR_ARG, "n and m must be non-negative");
+  NLA_TRY(check_matrix("A", A, n, n, lda));
+  NLA_TRY(check_matrix("B", B, side == 'L' ? n : m, side == 'L' ? m : n, ldb));
+  if (n == 0 || m == 0) return NLA_OK;
+  Mat Am{const_cast<void*>(A), lda, 0};
+  Mat Bm{B, ldb, 0};
+  if (trans == 'T' || trans == 'C') {  // src/rectrxm.jl:56-59
+    Am.t = 1;
+    uplo = uplo == 'L' ? 'U' : 'L';
+  }
+  const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
+  Rec c{func, side, uplo, dtype, m, 0, s};
+  if (func == 'S') {
+    c.threshold = cutoff_s > 0 ? cutoff_s : default_cutoff('S', dtype);
+    if (c.threshold > 1024) c.threshold = 1024;
+    NLA_TRY(launch_scale(dtype, rows, cols, alpha, Bm, s));  // src/rectrxm.jl:64
+  } else {
+    c.threshold = cutoff_m > 0 ? cutoff_m : default_cutoff('M', dtype);
+    if (c.threshold > 1024) c.threshold = 1024;
+  }
+  NLA_TRY(rec(c, Am, n, Bm));
+  if (func == 'M') NLA_TRY(launch_scale(dtype, rows, cols, alpha, Bm, s));  // src/rectrxm.jl:72
+  return NLA_OK;
+}
+
+}  // namespace nla
+
+using namespace nla;
+
+extern "C" {
+
+int nla_version(void) { return 100; }
+
+const char* nla_last_error(void) { return g_last_error.c_str(); }
+
+int nla_trxm(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
+             const void* A, int64_t lda, void* B, int64_t ldb, void* stream) {
+  clear_error();
+  return trxm_impl(side, uplo, trans, alpha, func, dtype, n, m, A, lda, B, ldb, 0, 0, (cudaStream_t)stream);
+}
+
+int nla_trxm_ex(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
+                const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, void* stream) {
+  clear_error();
+  return trxm_impl(side, uplo, trans, alpha, func, dtype, n, m, A, lda, B, ldb, cutoff_s, cutoff_m,
+                   (cudaStream_t)stream);
+}
+
+int nla_diag_block(char func, char side, char uplo, int transA, int dtype, int64_t n, int64_t m, const void* A,
+                   int64_t lda, void* B, int64_t ldb, void* stream) {
+  clear_error();
+  NLA_TRY(check_flags(side, uplo, 'N', func, dtype));
+  if (n < 0 || m < 0) return fail(NLA_ERR_ARG, "n and m must be non-negative");
+  if (n > 1024) return fail(NLA_ERR_ARG, "diag block: n must be <= 1024");
+  NLA_TRY(check_matrix("A", A, n, n, lda));
+  NLA_TRY(check_matrix("B", B, side == 'L' ? n : m, side == 'L' ? m : n, ldb));
+  Mat Am{const_cast<void*>(A), lda, transA ? 1 : 0};
+  Mat Bm{B, ldb, 0};
+  return launch_leaf(func, side, uplo, dtype, n, m, Am, Bm, (cudaStream_t)stream);
+}
+
+int nla_gemm_update(int dtype, int trans1, int trans2, int64_t N, int64_t R, int64_t M, double alpha,
+                    const void* in1, int64_t ld1, const void* in2, int64_t ld2, void* out, int64_t ldo, void* stream) {
+  clear_error();
+  if (!valid_dtype(dtype)) return fail(NLA_ERR_DTYPE, "dtype must be NLA_F16, NLA_F32 or NLA_F64");
+  if (N < 0 || R < 0 || M < 0) return fail(NLA_ERR_ARG, "N, R and M must be non-negative");
+  NLA_TRY(check_matrix("in1", in1, trans1 ? R : N, trans1 ? N : R, ld1));
+  NLA_TRY(check_matrix("in2", in2, trans2 ? M : R, trans2 ? R : M, ld2));
+  NLA_TRY(check_matrix("out", out, N, M, ldo));
+  Mat A{const_cast<void*>(in1), ld1, trans1 ? 1 : 0};
+  Mat B{const_cast<void*>(in2), ld2, trans2 ? 1 : 0};
+  Mat C{out, ldo, 0};
+  return launch_gemm(dtype, N, M, R, alpha, A, B, C, (cudaStream_t)stream);
+}
+
+int nla_scale(int dtype, int64_t rows, int64_t cols, double alpha, void* B, int64_t ldb, void* stream) {
+  clear_error();
+  if (!valid_dtype(dtype)) return fail(NLA_ERR_DTYPE, "dtype must be NLA_F16, NLA_F32 or NLA_F64");
+  NLA_TRY(check_matrix("B", B, rows, cols, ldb));
+  Mat Bm{B, ldb, 0};
+  return launch_scale(dtype, rows, cols, alpha, Bm, (cudaStream_t)stream);
+}
+
+}  // extern "C"

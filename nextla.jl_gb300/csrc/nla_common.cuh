@@ -1,0 +1,103 @@
+// Shared definitions of the GB300 triangular solve / multiply library.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/nextla_gb300.h"
+
+namespace nla {
+
+// ---------------------------------------------------------------------------
+// Status reporting (thread-local message, negative codes).
+// ---------------------------------------------------------------------------
+void set_error(const std::string& msg);
+void clear_error();
+int fail(int code, const std::string& msg);
+int cuda_status(cudaError_t e, const char* where);
+
+#define NLA_CHECK_LAUNCH(where)                          \
+  do {                                                   \
+    cudaError_t e_ = cudaGetLastError();                 \
+    if (e_ != cudaSuccess) return ::nla::cuda_status(e_, where); \
+  } while (0)
+
+#define NLA_TRY(expr)          \
+  do {                         \
+    int rc_ = (expr);          \
+    if (rc_ != NLA_OK) return rc_; \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Matrix views.  A column-major parent with leading dimension ld; element
+// (i,j) of the view is p[i + j*ld], or p[j + i*ld] when t is set (the
+// library's form of a Julia Transpose/Adjoint wrapper of a real matrix).
+// ---------------------------------------------------------------------------
+struct Mat {
+  void* p;
+  int64_t ld;
+  int t;
+};
+
+inline size_t dtype_size(int dtype) { return dtype == NLA_F64 ? 8 : dtype == NLA_F32 ? 4 : 2; }
+
+// Element offset of (i, j) in a view.
+__host__ __device__ inline int64_t mat_off(int64_t i, int64_t j, int64_t ld, int t) {
+  return t ? j + i * ld : i + j * ld;
+}
+
+// view(X, i0+1:end, j0+1:end)
+inline Mat sub(const Mat& v, int64_t i0, int64_t j0, int dtype) {
+  Mat r = v;
+  r.p = static_cast<char*>(v.p) + mat_off(i0, j0, v.ld, v.t) * (int64_t)dtype_size(dtype);
+  return r;
+}
+
+inline Mat transposed(const Mat& v) {
+  Mat r = v;
+  r.t = !v.t;
+  return r;
+}
+
+// Element conversions between storage and compute types.
+template <typename T> struct Elem;
+template <> struct Elem<double> {
+  using compute = double;
+  __device__ static double load(const double* p) { return *p; }
+  __device__ static void store(double* p, double v) { *p = v; }
+  __device__ static void store_d(double* p, double v) { *p = v; }
+};
+template <> struct Elem<float> {
+  using compute = float;
+  __device__ static float load(const float* p) { return *p; }
+  __device__ static void store(float* p, float v) { *p = v; }
+  __device__ static void store_d(float* p, double v) { *p = (float)v; }
+};
+template <> struct Elem<__half> {
+  using compute = float;
+  __device__ static float load(const __half* p) { return __half2float(*p); }
+  __device__ static void store(__half* p, float v) { *p = __float2half_rn(v); }
+  __device__ static void store_d(__half* p, double v) { *p = __double2half(v); }
+};
+
+// ---------------------------------------------------------------------------
+// Kernel launchers (defined in the .cu files).
+// ---------------------------------------------------------------------------
+
+// out (N x M) += alpha * op(A) (N x K) * op(B) (K x M), plain dtype-preserving path.
+int launch_gemm(int dtype, int64_t N, int64_t M, int64_t K, double alpha, const Mat& A, const Mat& B, const Mat& C,
+                cudaStream_t s);
+
+// Base case on a diagonal block: func 'S' (solve) or 'M' (multiply).
+int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m, const Mat& A, const Mat& B,
+                cudaStream_t s);
+
+// B .= alpha .* B on a rows x cols view.
+int launch_scale(int dtype, int64_t rows, int64_t cols, double alpha, const Mat& B, cudaStream_t s);
+
+int num_sms();
+
+}  // namespace nla

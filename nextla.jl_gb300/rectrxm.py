@@ -1,0 +1,312 @@
+"""Host-side mirror of NextLA.jl's recursive triangular solve / multiply.
+
+The reference's entry point is the Julia function
+``unified_rectrxm!(side, uplo, transpose, alpha, func, A, B)``
+(src/rectrxm.jl:43-76) with the recursion ``unified_rec`` (src/rectrxm.jl:101-198),
+the base cases ``LeftLowerTRSM!`` ... ``RightUpperTRMM!`` (src/trsm.jl:128-150,
+src/trmm.jl:332-389) and the updates ``GEMM_ADD!`` / ``GEMM_SUB!``
+(src/matmul.jl:69-81).  This module keeps those names (``!`` becomes ``_``),
+argument orders and meanings, and drives the same recursion on CUDA tensors;
+every base case and every update is one call through the C ABI into the
+sm_103a kernels of ``libnextla_gb300.so``.
+
+Matrices are 2-D CUDA tensors holding column-major data, as a Julia ``CuArray``
+does: a column-major n x m matrix is a tensor of shape (n, m) with strides
+(1, ld).  Slicing gives the same strided views as Julia's ``view``, and ``.T``
+gives the ``Transpose`` wrapper.  Work is enqueued on torch's current stream and
+is asynchronous, like the reference's kernel launches.
+
+Differences from the reference, by design:
+  * unknown characters raise ``ValueError`` instead of falling through to a
+    default branch (src/rectrxm.jl:104-124);
+  * Float16 updates accumulate in Float32 (src/matmul.jl:50-55 accumulates in
+    Float16).
+"""
+
+from __future__ import annotations
+
+from . import _lib
+
+_DTYPE_CODES = None
+
+
+def _dtype_code(t) -> int:
+    global _DTYPE_CODES
+    if _DTYPE_CODES is None:
+        import torch
+
+        _DTYPE_CODES = {torch.float16: _lib.NLA_F16, torch.float32: _lib.NLA_F32, torch.float64: _lib.NLA_F64}
+    try:
+        return _DTYPE_CODES[t.dtype]
+    except KeyError:
+        raise ValueError("element type must be Float16, Float32 or Float64, got %s" % t.dtype) from None
+
+
+def _mat(X):
+    """(pointer, leading dimension, transposed) of a 2-D strided view."""
+    if X.dim() != 2:
+        raise ValueError("expected a matrix, got a tensor of shape %s" % (tuple(X.shape),))
+    if not X.is_cuda:
+        raise ValueError("expected a CUDA tensor (the reference's CuArray), got one on %s" % X.device)
+    r, c = X.shape
+    s0, s1 = X.stride()
+    if s0 == 1 or r <= 1:
+        ld = s1 if c > 1 else max(r, 1)
+        if ld >= max(r, 1):
+            return X.data_ptr(), ld, 0
+    if s1 == 1 or c <= 1:
+        ld = s0 if r > 1 else max(c, 1)
+        if ld >= max(c, 1):
+            return X.data_ptr(), ld, 1
+    raise ValueError("matrix views need a unit stride in one dimension (strides %s)" % ((s0, s1),))
+
+
+def _stream(X) -> int:
+    import torch
+
+    return torch.cuda.current_stream(X.device).cuda_stream
+
+
+def _check_flags(side, uplo, transpose, func):
+    if side not in ("L", "R"):
+        raise ValueError("side must be 'L' or 'R', got %r" % (side,))
+    if uplo not in ("L", "U"):
+        raise ValueError("uplo must be 'L' or 'U', got %r" % (uplo,))
+    if transpose not in ("N", "T", "C"):
+        raise ValueError("transpose must be 'N', 'T' or 'C', got %r" % (transpose,))
+    if func not in ("S", "M"):
+        raise ValueError("func must be 'S' or 'M', got %r" % (func,))
+
+
+def _check_operands(A, B, side):
+    if A.dtype != B.dtype:
+        raise ValueError("A and B must have the same element type (%s vs %s)" % (A.dtype, B.dtype))
+    if A.device != B.device:
+        raise ValueError("A and B must be on the same device")
+    n = A.shape[0]
+    if len(A.shape) != 2 or A.shape[1] != n:
+        raise ValueError("A must be square, got %s" % (tuple(A.shape),))
+    if len(B.shape) != 2 or (side == "L" and B.shape[0] != n) or (side == "R" and B.shape[1] != n):
+        raise ValueError("B of shape %s does not conform with A of size %d for side %r" % (tuple(B.shape), n, side))
+
+
+# ---------------------------------------------------------------------------
+# Base cases (src/trsm.jl:128-150, src/trmm.jl:332-389).
+# ---------------------------------------------------------------------------
+
+def _diag_block(func, side, uplo, A, B):
+    a, lda, ta = _mat(A)
+    b, ldb, tb = _mat(B)
+    if tb:
+        raise ValueError("B must be a column-major view")
+    n = A.shape[0]
+    m = B.shape[1] if side == "L" else B.shape[0]
+    L = _lib.load()
+    _lib.check(L.nla_diag_block(_lib.ch(func), _lib.ch(side), _lib.ch(uplo), ta, _dtype_code(B), n, m, a, lda, b,
+                                ldb, _stream(B)))
+    return B
+
+
+def LeftLowerTRSM_(A, B):
+    """Solve L X = B in place for a lower-triangular diagonal block (src/trsm.jl:128-132)."""
+    return _diag_block("S", "L", "L", A, B)
+
+
+def LeftUpperTRSM_(A, B):
+    """Solve U X = B in place (src/trsm.jl:134-138)."""
+    return _diag_block("S", "L", "U", A, B)
+
+
+def RightLowerTRSM_(A, B):
+    """Solve X L = B in place (src/trsm.jl:140-144)."""
+    return _diag_block("S", "R", "L", A, B)
+
+
+def RightUpperTRSM_(A, B):
+    """Solve X U = B in place (src/trsm.jl:146-150)."""
+    return _diag_block("S", "R", "U", A, B)
+
+
+def LeftLowerTRMM_(A, B):
+    """B := L B in place (src/trmm.jl:332-338)."""
+    return _diag_block("M", "L", "L", A, B)
+
+
+def LeftUpperTRMM_(A, B):
+    """B := U B in place (src/trmm.jl:350-355)."""
+    return _diag_block("M", "L", "U", A, B)
+
+
+def RightLowerTRMM_(A, B):
+    """B := B L in place (src/trmm.jl:367-372)."""
+    return _diag_block("M", "R", "L", A, B)
+
+
+def RightUpperTRMM_(A, B):
+    """B := B U in place (src/trmm.jl:384-389)."""
+    return _diag_block("M", "R", "U", A, B)
+
+
+# ---------------------------------------------------------------------------
+# Off-diagonal updates (src/matmul.jl:69-81).
+# ---------------------------------------------------------------------------
+
+def matmul_(output, input1, input2, alpha=1.0):
+    """output += alpha * input1 * input2 (the matmul! kernel, src/matmul.jl:5-66).
+    Transposed inputs are passed as transposed views (the reference passes
+    ``Transpose`` wrappers and leaves matmul!'s transA/transB at 'N')."""
+    o, ldo, to = _mat(output)
+    if to:
+        raise ValueError("output must be a column-major view")
+    a, ld1, t1 = _mat(input1)
+    b, ld2, t2 = _mat(input2)
+    N, M = output.shape
+    R = input1.shape[1]
+    if input1.shape[0] != N or input2.shape != (R, M):
+        raise ValueError("matmul_: shapes %s * %s do not conform with %s" % (tuple(input1.shape),
+                                                                             tuple(input2.shape),
+                                                                             tuple(output.shape)))
+    L = _lib.load()
+    _lib.check(L.nla_gemm_update(_dtype_code(output), t1, t2, N, R, M, float(alpha), a, ld1, b, ld2, o, ldo,
+                                 _stream(output)))
+    return output
+
+
+def GEMM_ADD_(A, B, C):
+    """C += A * B (src/matmul.jl:69-74)."""
+    return matmul_(C, A, B, 1.0)
+
+
+def GEMM_SUB_(A, B, C):
+    """A -= B * C (src/matmul.jl:76-81)."""
+    return matmul_(A, B, C, -1.0)
+
+
+def scale_(B, alpha):
+    """B .= alpha .* B (src/rectrxm.jl:64,72), Float64 product rounded to B's type."""
+    b, ldb, tb = _mat(B)
+    if tb:
+        raise ValueError("B must be a column-major view")
+    L = _lib.load()
+    _lib.check(L.nla_scale(_dtype_code(B), B.shape[0], B.shape[1], float(alpha), b, ldb, _stream(B)))
+    return B
+
+
+# ---------------------------------------------------------------------------
+# Recursion (src/rectrxm.jl:101-198) and entry point (src/rectrxm.jl:43-76).
+# ---------------------------------------------------------------------------
+
+def split_point(n: int) -> int:
+    """n/2 when log2(n) is an integer, else the largest power of two below n
+    (src/rectrxm.jl:129-133)."""
+    if n & (n - 1) == 0:
+        return n // 2
+    return 1 << (n.bit_length() - 1)
+
+
+def unified_rec(func, side, uplo, A, n, B, threshold=256):
+    """unified_rec (src/rectrxm.jl:101-198) on tensor views."""
+    if n <= threshold:
+        if func == "S":
+            if side == "L" and uplo == "L":
+                LeftLowerTRSM_(A, B)
+            elif side == "L" and uplo == "U":
+                LeftUpperTRSM_(A, B)
+            elif side == "R" and uplo == "L":
+                RightLowerTRSM_(A, B)
+            else:
+                RightUpperTRSM_(A, B)
+        else:
+            if side == "L" and uplo == "L":
+                LeftLowerTRMM_(A, B)
+            elif side == "L" and uplo == "U":
+                LeftUpperTRMM_(A, B)
+            elif side == "R" and uplo == "L":
+                RightLowerTRMM_(A, B)
+            else:
+                RightUpperTRMM_(A, B)
+        return B
+
+    mid = split_point(n)
+    A11 = A[:mid, :mid]
+    A22 = A[mid:n, mid:n]
+    A21 = A[mid:n, :mid]
+    A12 = A[:mid, mid:n]
+    if side == "L":
+        B1, B2 = B[:mid, :], B[mid:n, :]
+    else:
+        B1, B2 = B[:, :mid], B[:, mid:n]
+
+    if ((side == "L" and uplo == "L" and func == "S") or (side == "R" and uplo == "U" and func == "S")
+            or (side == "L" and uplo == "U" and func == "M") or (side == "R" and uplo == "L" and func == "M")):
+        unified_rec(func, side, uplo, A11, mid, B1, threshold)
+        if side == "L":
+            if func == "S":
+                GEMM_SUB_(B2, A21, B1)
+            else:
+                GEMM_ADD_(A12, B2, B1)
+        else:
+            if func == "S":
+                GEMM_SUB_(B2, B1, A12)
+            else:
+                GEMM_ADD_(B2, A21, B1)
+        unified_rec(func, side, uplo, A22, n - mid, B2, threshold)
+    else:
+        unified_rec(func, side, uplo, A22, n - mid, B2, threshold)
+        if side == "L":
+            if func == "S":
+                GEMM_SUB_(B1, A12, B2)
+            else:
+                GEMM_ADD_(A21, B1, B2)
+        else:
+            if func == "S":
+                GEMM_SUB_(B1, B2, A21)
+            else:
+                GEMM_ADD_(B1, A12, B2)
+        unified_rec(func, side, uplo, A11, mid, B1, threshold)
+    return B
+
+
+def unified_rectrxm_(side, uplo, transpose, alpha, func, A, B, *, native=False, thresholds=None):
+    """unified_rectrxm!(side, uplo, transpose, alpha, func, A, B) (src/rectrxm.jl:43-76).
+
+    Solves op(A) X = alpha B (func 'S', side 'L'), X op(A) = alpha B ('S', 'R'),
+    or forms B := alpha op(A) B ('M', 'L') / alpha B op(A) ('M', 'R'), in place
+    in B, and returns B.  A is n x n; only its ``uplo`` triangle is read.
+
+    By default the recursion runs here, as the reference's Julia host code
+    does, with the reference's thresholds (256 for solves, 16 for multiplies,
+    src/rectrxm.jl:52,63) unless ``thresholds=(s, m)`` is given.  With
+    ``native=True`` the whole recursion runs inside the library (nla_trxm),
+    with its own tuned cut-offs unless ``thresholds`` is given.
+    """
+    _check_flags(side, uplo, transpose, func)
+    _check_operands(A, B, side)
+    n = A.shape[0]
+    if native:
+        a, lda, ta = _mat(A)
+        b, ldb, tb = _mat(B)
+        if tb:
+            raise ValueError("B must be a column-major view")
+        tr, up = transpose, uplo
+        if ta:  # A is a transposed view of its parent: fold that into the flags
+            tr = "N" if transpose in ("T", "C") else "T"
+            up = "U" if uplo == "L" else "L"
+        m = B.shape[1] if side == "L" else B.shape[0]
+        cs, cm = thresholds if thresholds is not None else (0, 0)
+        L = _lib.load()
+        _lib.check(L.nla_trxm_ex(_lib.ch(side), _lib.ch(up), _lib.ch(tr), float(alpha), _lib.ch(func),
+                                 _dtype_code(B), n, m, a, lda, b, ldb, int(cs), int(cm), _stream(B)))
+        return B
+
+    threshold = 16 if thresholds is None else int(thresholds[1])
+    if transpose in ("T", "C"):
+        A = A.T  # Transpose(A); for real data Adjoint(A) is the same view
+        uplo = "U" if uplo == "L" else "L"
+    if func == "S":
+        threshold = 256 if thresholds is None else int(thresholds[0])
+        scale_(B, alpha)
+    unified_rec(func, side, uplo, A, n, B, threshold)
+    if func == "M":
+        scale_(B, alpha)
+    return B
