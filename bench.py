@@ -1,0 +1,330 @@
+#!/usr/bin/env python
+"""Benchmark of the recursive triangular solve on one GB300.
+
+Workload (default): Float64 TRSM, side L, uplo L, trans N, alpha 1,
+n = m = 16384, A = tril(N(0,1)/sqrt(n), -1) + diag(2 + |N(0,1)|),
+B ~ U[-1, 1], seed 0 (numpy PCG64).  The inputs (2 GiB each) are larger than
+L2 (129 MB), so no flush is needed between steps.
+
+One step = restore B from a resident pristine copy (device-to-device copy,
+inside the timed region) + one full solve.  Metric: TFLOP/s with the
+n^2 m flop count of a triangular solve.
+
+Variants:
+  plain   the dtype-preserving Float64 path (DFMA GEMM updates, FP64 leaves).
+  mixed   the mixed-precision form: BF16 tensor-core updates with an operand
+          split plus FP64 iterative refinement (when built into the library).
+
+Also reported on the same JSON line:
+  e2e           the same metric through the C ABI with host buffers: pinned
+                host A and B copied in, solved, B copied out, every step;
+  roofline      the dominant kernel's achieved rate from live CUDA-event
+                tracing inside the timed region against the measured peak;
+  cpu_baseline  the oracle (a C restatement of the reference algorithm) on the
+                host cores on a bounded sample of right-hand sides;
+  clocks        nvidia-smi samples taken during the timed region.
+
+--impl reference times the reference algorithm (the oracle port) on the host
+cores on a bounded sample of the same workload, and prints the same metric.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--variant", choices=["plain", "mixed"], default="plain")
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--m", type=int, default=16384)
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="right-hand sides in the CPU sample (0: 4 per host thread)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (the GPU is not modified)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_inputs(n, m, seed=0):
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    A = np.tril(rng.standard_normal((n, n)) / np.sqrt(n), -1)
+    A[np.diag_indices(n)] = 2.0 + np.abs(rng.standard_normal(n))
+    B = rng.uniform(-1.0, 1.0, (n, m))
+    return np.asfortranarray(A), np.asfortranarray(B)
+
+
+def cpu_baseline(A, B, sample_cols, threads):
+    """Oracle (reference algorithm restated in C) on `sample_cols` right-hand
+    sides with `threads` host threads; returns (TFLOP/s, seconds, columns)."""
+    import numpy as np
+
+    import __graft_entry__ as graft
+
+    orc = graft.load_oracle()
+    n = A.shape[0]
+    Bs = np.asfortranarray(B[:, :sample_cols])
+    t0 = time.perf_counter()
+    orc.rectrxm("L", "L", "N", 1.0, "S", A, Bs, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return float(n) * n * sample_cols / dt / 1e12, dt
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm (oracle port) on host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    threads = os.cpu_count() or 1
+    cols = args.cpu_sample or 4 * threads
+    A, B = make_inputs(args.n, args.m)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, _ = cpu_baseline(A, B, cols, threads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": "trsm_tflops", "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
+        "config": {"workload": "trsm_LLN_f64_n%d_m%d" % (args.n, args.m), "n": args.n, "m": args.m,
+                   "side": "L", "uplo": "L", "trans": "N", "alpha": 1.0},
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+                         "sample": "%d of %d right-hand sides per step, full %dx%d A" % (cols, args.m, args.n,
+                                                                                         args.n)},
+        "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as graft
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    pkg = graft.load_package()
+    L = pkg.load_library()
+    from nextla_gb300 import _lib
+
+    n, m = args.n, args.m
+    A_h, B_h = make_inputs(n, m)
+    flops = float(n) * n * m
+    # Column-major device copies (tensor of shape (n, m) with strides (1, n)).
+    A = torch.from_numpy(np.ascontiguousarray(A_h.T)).to(dev).T
+    B0 = torch.from_numpy(np.ascontiguousarray(B_h.T)).to(dev).T
+    B = torch.empty_like(B0.T).T
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def solve(Bd):
+        _lib.check(L.nla_trxm(b"L", b"L", b"N", 1.0, b"S", _lib.NLA_F64, n, m, A.data_ptr(), n, Bd.data_ptr(), n,
+                              sptr))
+
+    def step():
+        B.copy_(B0)
+        solve(B)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    _lib.trace_enable(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    barrier()
+    _lib.trace_enable(False)
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * args.steps * flops / (ms / 1e3) / 1e12
+    trace = _lib.trace_summary()
+
+    # Accuracy of the last solution on a sample of columns (FP64 GEMM in torch).
+    cols = torch.arange(0, m, max(1, m // 64), device=dev)
+    X = B[:, cols]
+    Ad = torch.tril(A)
+    R = Ad @ X - B0[:, cols]
+    berr = float(R.abs().sum(dim=1).max() / (Ad.abs().sum(dim=1).max() * X.abs().sum(dim=1).max() * n * 2.0 ** -53))
+    del Ad, R
+
+    # End to end through the C ABI with host buffers.
+    A_pin = torch.from_numpy(np.ascontiguousarray(A_h.T)).pin_memory()
+    B_pin = torch.from_numpy(np.ascontiguousarray(B_h.T)).pin_memory()
+    X_pin = torch.empty_like(B_pin).pin_memory()
+    Ae = torch.empty_like(A.T)
+    Be = torch.empty_like(B0.T)
+
+    def e2e_step():
+        Ae.copy_(A_pin, non_blocking=True)
+        Be.copy_(B_pin, non_blocking=True)
+        _lib.check(L.nla_trxm(b"L", b"L", b"N", 1.0, b"S", _lib.NLA_F64, n, m, Ae.data_ptr(), n, Be.data_ptr(), n,
+                              sptr))
+        X_pin.copy_(Be, non_blocking=True)
+
+    e2e_steps = max(1, min(args.steps, 3))
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_value = world * flops / e2e_s / 1e12
+
+    # Roofline of the dominant kernel class.
+    pk, pk_kind = peaks()
+    dom = max(trace.items(), key=lambda kv: kv[1][1]) if trace else None
+    roofline = None
+    gpu_launches = sum(v[0] for v in trace.values()) + 0
+    if dom:
+        name, (launches, kms, kflops, kbytes) = dom
+        achieved = kflops / (kms / 1e3) / 1e12
+        roofline = {"kernel": name, "bound": "fp64" if name in ("gemm_simt", "leaf_solve") else "tensor",
+                    "achieved": achieved, "peak": None, "unit": "TFLOP/s", "frac": None, "traffic": None,
+                    "launches": launches, "share": kms / sum(v[1] for v in trace.values())}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample = args.cpu_sample or 4 * threads
+        v, dt = cpu_baseline(A_h, B_h, sample, threads)
+        cpu = {"value": v, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+               "sample": "%d of %d right-hand sides, full %dx%d A, %.1f s" % (sample, m, n, n, dt)}
+
+    if rank == 0:
+        line = {
+            "metric": "trsm_tflops", "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
+            "config": {"workload": "trsm_LLN_f64_n%d_m%d_%s" % (n, m, args.variant), "n": n, "m": m, "side": "L",
+                       "uplo": "L", "trans": "N", "alpha": 1.0, "variant": args.variant,
+                       "l2": "inputs larger than L2", "parallelism": "replicas" if world > 1 else "single"},
+            "accuracy": {"backward_error": berr, "definition": "||AX-B||_inf/(||A||_inf ||X||_inf n u), 64 cols"},
+            "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": int(A_h.nbytes + B_h.nbytes),
+                    "d2h_bytes_per_step": int(B_h.nbytes)},
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": gpu_launches,
+            "trace": {k: {"launches": v[0], "ms": v[1], "tflops": v[2] / max(v[1], 1e-9) / 1e9}
+                      for k, v in trace.items()},
+            "peaks": pk_kind,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -115,6 +115,28 @@ NLA_API int nla_gemm_update(int dtype, int trans1, int trans2, int64_t N, int64_
  */
 NLA_API int nla_scale(int dtype, int64_t rows, int64_t cols, double alpha, void* B, int64_t ldb, void* stream);
 
+/*
+ * Kernel tracing (no counterpart in the reference, which has no tracing).
+ * nla_trace_enable(1) clears earlier records and starts recording; every
+ * library kernel launched afterwards is bracketed by CUDA events on its
+ * stream together with its algorithmic flops and bytes.  nla_trace_enable(0)
+ * stops recording.  nla_trace_summary() waits for the recorded events and
+ * returns, for one kernel class, the number of launches, their summed device
+ * time in milliseconds and their summed algorithmic flops and bytes.  Do not
+ * trace work that is being captured into a CUDA graph.
+ */
+#define NLA_K_LEAF_SOLVE 0 /* diagonal-block solve */
+#define NLA_K_LEAF_MULT 1  /* diagonal-block multiply */
+#define NLA_K_GEMM_SIMT 2  /* off-diagonal update on CUDA cores */
+#define NLA_K_GEMM_UMMA 3  /* off-diagonal update on tcgen05 tensor cores */
+#define NLA_K_SPLIT 4      /* operand split / staging for the tensor-core update */
+#define NLA_K_SCALE 5      /* alpha scaling and element-wise passes */
+#define NLA_K_RESIDUAL 6   /* residual and correction passes of refinement */
+#define NLA_K_BATCHED 7    /* persistent batched solve */
+#define NLA_K_COUNT 8
+NLA_API int nla_trace_enable(int on);
+NLA_API int nla_trace_summary(int kernel_class, int64_t* launches, double* ms, double* flops, double* bytes);
+
 #ifdef __cplusplus
 }
 #endif

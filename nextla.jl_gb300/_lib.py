@@ -34,7 +34,12 @@ SIGNATURES = {
     "nla_diag_block": ([_c, _c, _c, _i32, _i32, _i64, _i64, _p, _i64, _p, _i64, _p], _i32),
     "nla_gemm_update": ([_i32, _i32, _i32, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _p, _i64, _p], _i32),
     "nla_scale": ([_i32, _i64, _i64, _d, _p, _i64, _p], _i32),
+    "nla_trace_enable": ([_i32], _i32),
+    "nla_trace_summary": ([_i32, ctypes.POINTER(_i64), ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d)],
+                          _i32),
 }
+
+KERNEL_CLASSES = ["leaf_solve", "leaf_mult", "gemm_simt", "gemm_umma", "split", "scale", "residual", "batched"]
 
 _lib = None
 _lock = threading.Lock()
@@ -79,6 +84,23 @@ def check(rc: int) -> None:
     if rc in (NLA_ERR_ARG, NLA_ERR_DTYPE):
         raise NLAArgumentError(rc, msg)
     raise NLAError(rc, msg)
+
+
+def trace_enable(on: bool) -> None:
+    check(load().nla_trace_enable(1 if on else 0))
+
+
+def trace_summary() -> dict:
+    """{kernel class: (launches, device ms, algorithmic flops, bytes)} of the
+    launches recorded since trace_enable(True)."""
+    L = load()
+    out = {}
+    for k, name in enumerate(KERNEL_CLASSES):
+        n, ms, fl, by = _i64(), _d(), _d(), _d()
+        check(L.nla_trace_summary(k, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(fl), ctypes.byref(by)))
+        if n.value:
+            out[name] = (n.value, ms.value, fl.value, by.value)
+    return out
 
 
 def ch(c: str):

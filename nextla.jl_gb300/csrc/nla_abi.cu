@@ -11,6 +11,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
+#include <vector>
 
 #include "nla_common.cuh"
 
@@ -27,6 +29,56 @@ int fail(int code, const std::string& msg) {
 int cuda_status(cudaError_t e, const char* where) {
   set_error(std::string(where) + ": " + cudaGetErrorString(e));
   return NLA_ERR_CUDA_BASE - (int)e;
+}
+
+// ---------------------------------------------------------------------------
+// Tracing.
+// ---------------------------------------------------------------------------
+namespace {
+struct TraceRec {
+  int kclass;
+  cudaEvent_t e0, e1;
+  double flops, bytes;
+};
+std::mutex g_trace_mu;
+std::atomic<bool> g_trace_on{false};
+std::vector<TraceRec*> g_trace;
+std::vector<cudaEvent_t> g_event_pool;
+
+cudaEvent_t pooled_event() {
+  if (!g_event_pool.empty()) {
+    cudaEvent_t e = g_event_pool.back();
+    g_event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void clear_trace_locked() {
+  for (TraceRec* r : g_trace) {
+    g_event_pool.push_back(r->e0);
+    g_event_pool.push_back(r->e1);
+    delete r;
+  }
+  g_trace.clear();
+}
+}  // namespace
+
+void trace_begin(int kclass, cudaStream_t s, double flops, double bytes, void** handle) {
+  *handle = nullptr;
+  if (!g_trace_on.load(std::memory_order_relaxed)) return;
+  std::lock_guard<std::mutex> lk(g_trace_mu);
+  TraceRec* r = new TraceRec{kclass, pooled_event(), pooled_event(), flops, bytes};
+  cudaEventRecord(r->e0, s);
+  g_trace.push_back(r);
+  *handle = r;
+}
+
+void trace_end(void* handle, cudaStream_t s) {
+  TraceRec* r = static_cast<TraceRec*>(handle);
+  cudaEventRecord(r->e1, s);
 }
 
 int num_sms() {
@@ -65,6 +117,7 @@ int launch_scale(int dtype, int64_t rows, int64_t cols, double alpha, const Mat&
   const int64_t cap = (int64_t)num_sms() * 8;
   if (blocks > cap) blocks = cap;
   const bool f32_exact = (double)(float)alpha == alpha;
+  TraceScope trace(NLA_K_SCALE, s, (double)total, 2.0 * (double)total * (double)dtype_size(dtype));
   switch (dtype) {
     case NLA_F64:
       scale_kernel<double, double><<<(unsigned)blocks, 256, 0, s>>>(rows, cols, alpha, (double*)B.p, B.ld, B.t);
@@ -222,6 +275,39 @@ using namespace nla;
 extern "C" {
 
 int nla_version(void) { return 100; }
+
+int nla_trace_enable(int on) {
+  clear_error();
+  std::lock_guard<std::mutex> lk(g_trace_mu);
+  if (on) clear_trace_locked();
+  g_trace_on.store(on != 0);
+  return NLA_OK;
+}
+
+int nla_trace_summary(int kernel_class, int64_t* launches, double* ms, double* flops, double* bytes) {
+  clear_error();
+  if (kernel_class < 0 || kernel_class >= NLA_K_COUNT) return fail(NLA_ERR_ARG, "unknown kernel class");
+  std::lock_guard<std::mutex> lk(g_trace_mu);
+  int64_t n = 0;
+  double t = 0, f = 0, b = 0;
+  for (TraceRec* r : g_trace) {
+    if (r->kclass != kernel_class) continue;
+    cudaError_t e = cudaEventSynchronize(r->e1);
+    if (e != cudaSuccess) return cuda_status(e, "nla_trace_summary");
+    float x = 0;
+    e = cudaEventElapsedTime(&x, r->e0, r->e1);
+    if (e != cudaSuccess) return cuda_status(e, "nla_trace_summary");
+    ++n;
+    t += x;
+    f += r->flops;
+    b += r->bytes;
+  }
+  if (launches) *launches = n;
+  if (ms) *ms = t;
+  if (flops) *flops = f;
+  if (bytes) *bytes = b;
+  return NLA_OK;
+}
 
 const char* nla_last_error(void) { return g_last_error.c_str(); }
 

@@ -84,6 +84,25 @@ template <> struct Elem<__half> {
 };
 
 // ---------------------------------------------------------------------------
+// Kernel tracing: when enabled (nla_trace_enable), each traced launch is
+// bracketed by CUDA events on its stream and its algorithmic flops and bytes
+// are recorded, so callers can measure per-kernel durations live.
+// ---------------------------------------------------------------------------
+void trace_begin(int kclass, cudaStream_t s, double flops, double bytes, void** handle);
+void trace_end(void* handle, cudaStream_t s);
+
+struct TraceScope {
+  void* h = nullptr;
+  cudaStream_t s;
+  TraceScope(int kclass, cudaStream_t st, double flops, double bytes) : s(st) {
+    trace_begin(kclass, st, flops, bytes, &h);
+  }
+  ~TraceScope() {
+    if (h) trace_end(h, s);
+  }
+};
+
+// ---------------------------------------------------------------------------
 // Kernel launchers (defined in the .cu files).
 // ---------------------------------------------------------------------------
 

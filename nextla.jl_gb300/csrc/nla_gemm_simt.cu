@@ -134,6 +134,8 @@ int launch_simt(int64_t N, int64_t M, int64_t K, double alpha, const Mat& A, con
   constexpr int BM = 32 * V;
   int64_t gx = (N + BM - 1) / BM, gy = (M + BM - 1) / BM;
   if (gx > 2147483647LL || gy > 65535) return fail(NLA_ERR_UNSUPPORTED, "gemm: matrix too large for one launch");
+  TraceScope trace(NLA_K_GEMM_SIMT, s, 2.0 * (double)N * (double)M * (double)K,
+                   (double)sizeof(T) * ((double)N * K + (double)K * M + 2.0 * (double)N * M));
   gemm_simt_kernel<T, V, BK><<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(
       N, M, K, alpha, static_cast<const T*>(A.p), A.ld, A.t, static_cast<const T*>(B.p), B.ld, B.t,
       static_cast<T*>(C.p), C.ld);

@@ -232,6 +232,10 @@ int launch_leaf_t(char func, const LeafArgs& g, cudaStream_t s) {
   const size_t smem = leaf_smem<T, CW>(func, g.n);
   const int64_t grid = (g.m + CW - 1) / CW;
   if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "leaf: too many right-hand sides");
+  // n^2 m flops per solve or multiply (the benchmark's convention); bytes:
+  // the triangle once plus B read and written.
+  TraceScope trace(func == 'S' ? NLA_K_LEAF_SOLVE : NLA_K_LEAF_MULT, s, (double)g.n * g.n * (double)g.m,
+                   (double)sizeof(T) * ((double)g.n * (g.n + 1) / 2 + 2.0 * (double)g.n * g.m));
   if (func == 'S') {
     static bool configured = false;  // per instantiation; the attribute is per function
     if (!configured) {

@@ -23,21 +23,44 @@
  * src/matmul.jl:3) accumulated in the output element type, and the final
  * update promotes to Float64 because alpha is a Float64 (src/matmul.jl:64). */
 static void FN(matmul)(view out, view in1, view in2, int64_t N, int64_t R, int64_t M, double alpha) {
-  for (int64_t J = 0; J < M; ++J) {
-    for (int64_t I = 0; I < N; ++I) {
-      double outval = 0.0;
-      for (int64_t t = 0; t < R; t += 32) {
-        double tmp = 0.0;
-        int64_t kend = t + 32 < R ? t + 32 : R;
-        for (int64_t k = t; k < kend; ++k) tmp = RND(tmp + RND(*at(in1, I, k) * *at(in2, k, J)));
-        outval = RND(outval + tmp);
+  /* Columns of the output are processed in blocks of up to JB so that each
+   * operand element is reused from cache; every output element still sees
+   * exactly the reference's sequence of operations. */
+  enum { JB = 8 };
+  if (N <= 0 || M <= 0) return;
+  double* outval = (double*)malloc(sizeof(double) * (size_t)N * JB);
+  double* tmp = (double*)malloc(sizeof(double) * (size_t)N * JB);
+  if (!outval || !tmp) {
+    free(outval);
+    free(tmp);
+    return;
+  }
+  for (int64_t J0 = 0; J0 < M; J0 += JB) {
+    const int64_t nj = M - J0 < JB ? M - J0 : JB;
+    for (int64_t x = 0; x < N * nj; ++x) outval[x] = 0.0;
+    for (int64_t t = 0; t < R; t += 32) {
+      const int64_t kend = t + 32 < R ? t + 32 : R;
+      for (int64_t x = 0; x < N * nj; ++x) tmp[x] = 0.0;
+      for (int64_t k = t; k < kend; ++k) {
+        for (int64_t j = 0; j < nj; ++j) {
+          const double b = *at(in2, k, J0 + j);
+          double* tj = tmp + j * N;
+          for (int64_t I = 0; I < N; ++I) tj[I] = RND(tj[I] + RND(*at(in1, I, k) * b));
+        }
       }
-      double* o = at(out, I, J);
-      double prod = alpha * outval; /* Float64 product */
-      double sum = *o + prod;       /* Float64 sum */
-      *o = RND(sum);                /* stored back in eltype(output) */
+      for (int64_t x = 0; x < N * nj; ++x) outval[x] = RND(outval[x] + tmp[x]);
+    }
+    for (int64_t j = 0; j < nj; ++j) {
+      for (int64_t I = 0; I < N; ++I) {
+        double* o = at(out, I, J0 + j);
+        double prod = alpha * outval[j * N + I]; /* Float64 product */
+        double sum = *o + prod;                  /* Float64 sum */
+        *o = RND(sum);                           /* stored back in eltype(output) */
+      }
     }
   }
+  free(outval);
+  free(tmp);
 }
 
 /* GEMM_SUB!(X, Y, Z): X -= Y*Z, src/matmul.jl:76-81. */
