@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--m", type=int, default=16384)
     ap.add_argument("--cpu-sample", type=int, default=0,
-                    help="right-hand sides in the CPU sample (0: 4 per host thread)")
+                    help="right-hand sides in the CPU sample (0: 16 per host thread)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -157,7 +157,7 @@ def run_reference(args):
     import numpy as np
 
     threads = os.cpu_count() or 1
-    cols = args.cpu_sample or 4 * threads
+    cols = args.cpu_sample or 16 * threads
     A, B = make_inputs(args.n, args.m)
     vals = []
     for i in range(args.warmup + args.steps):
@@ -299,7 +299,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        sample = args.cpu_sample or 4 * threads
+        sample = args.cpu_sample or 16 * threads
         v, dt = cpu_baseline(A_h, B_h, sample, threads)
         cpu = {"value": v, "unit": "TFLOP/s", "cores": threads, "kind": "port",
                "sample": "%d of %d right-hand sides, full %dx%d A, %.1f s" % (sample, m, n, n, dt)}

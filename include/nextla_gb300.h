@@ -116,6 +116,51 @@ NLA_API int nla_gemm_update(int dtype, int trans1, int trans2, int64_t N, int64_
 NLA_API int nla_scale(int dtype, int64_t rows, int64_t cols, double alpha, void* B, int64_t ldb, void* stream);
 
 /*
+ * Mixed-precision form (no counterpart in the reference): the FP64 answer of
+ * unified_rectrxm! for Float64 A and B, with the off-diagonal updates on the
+ * tcgen05 tensor cores.  Each update operand is split into `split_terms`
+ * BF16 (lowp NLA_LOWP_BF16) or FP16 (NLA_LOWP_F16) slices with one
+ * power-of-two scale per row / column, slice products accumulate in FP32, and
+ * the diagonal blocks (size `cutoff`, default 128) are solved or multiplied in
+ * FP64.  Solves then run `sweeps` refinement sweeps: R = alpha*B - op(A) X in
+ * FP64, op(A) D = R with the same mixed solver, X += D.  If corr_out is not
+ * NULL it receives max|D| / max|X| of each sweep (host array of `sweeps`
+ * doubles; the call then synchronises the stream).  Multiplies (func 'M')
+ * ignore `sweeps`.  Inputs must be finite.
+ */
+#define NLA_LOWP_BF16 0
+#define NLA_LOWP_F16 1
+#define NLA_RESIDUAL_FP64 0 /* residual product on the FP64 pipe */
+typedef struct {
+  int lowp;          /* NLA_LOWP_BF16 or NLA_LOWP_F16 */
+  int split_terms;   /* 1, 2 or 3 slices per operand */
+  int sweeps;        /* refinement sweeps for solves, 0..8 */
+  int residual;      /* how the residual product is formed */
+  int64_t cutoff;    /* FP64 diagonal block size; <= 0 selects the default */
+  double* corr_out;  /* host, `sweeps` entries, or NULL */
+} nla_mixed_opts;
+NLA_API int nla_trxm_mixed(char side, char uplo, char trans, double alpha, char func, int64_t n, int64_t m,
+                           const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* opts,
+                           void* stream);
+
+/*
+ * One mixed-precision off-diagonal update (no counterpart in the reference;
+ * the mixed form of matmul!, src/matmul.jl:5-66): out (N x M, FP64) +=
+ * alpha * op(in1) (N x R) * op(in2) (R x M) from `split_terms` BF16/FP16
+ * slices per operand on the tensor cores.
+ */
+NLA_API int nla_gemm_update_mixed(int trans1, int trans2, int64_t N, int64_t R, int64_t M, double alpha,
+                                  const double* in1, int64_t ld1, const double* in2, int64_t ld2, double* out,
+                                  int64_t ldo, int lowp, int split_terms, void* stream);
+
+/*
+ * Synchronises `stream` and reports (then clears) the device-side error word
+ * that the tensor-core kernels raise when a bounded wait gives up:
+ * NLA_OK or NLA_ERR_TIMEOUT.
+ */
+NLA_API int nla_device_status(void* stream);
+
+/*
  * Kernel tracing (no counterpart in the reference, which has no tracing).
  * nla_trace_enable(1) clears earlier records and starts recording; every
  * library kernel launched afterwards is bracketed by CUDA events on its

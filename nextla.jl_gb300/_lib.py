@@ -39,6 +39,24 @@ SIGNATURES = {
                           _i32),
 }
 
+NLA_LOWP_BF16, NLA_LOWP_F16 = 0, 1
+NLA_RESIDUAL_FP64 = 0
+
+
+class MixedOpts(ctypes.Structure):
+    """nla_mixed_opts of include/nextla_gb300.h."""
+
+    _fields_ = [("lowp", ctypes.c_int), ("split_terms", ctypes.c_int), ("sweeps", ctypes.c_int),
+                ("residual", ctypes.c_int), ("cutoff", ctypes.c_int64), ("corr_out", ctypes.POINTER(ctypes.c_double))]
+
+
+SIGNATURES.update({
+    "nla_trxm_mixed": ([_c, _c, _c, _d, _c, _i64, _i64, _p, _i64, _p, _i64, ctypes.POINTER(MixedOpts), _p], _i32),
+    "nla_gemm_update_mixed": ([_i32, _i32, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _p, _i64, _i32, _i32, _p],
+                              _i32),
+    "nla_device_status": ([_p], _i32),
+})
+
 KERNEL_CLASSES = ["leaf_solve", "leaf_mult", "gemm_simt", "gemm_umma", "split", "scale", "residual", "batched"]
 
 _lib = None

@@ -144,9 +144,28 @@ int launch_scale(int dtype, int64_t rows, int64_t cols, double alpha, const Mat&
 int launch_gemm_simt(int dtype, int64_t N, int64_t M, int64_t K, double alpha, const Mat& A, const Mat& B,
                      const Mat& C, cudaStream_t s);
 
+static bool umma_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("NLA_DISABLE_UMMA");
+    return !(v && *v && *v != '0');
+  }();
+  return on;
+}
+
+// Float16 updates large enough to fill 128 x 128 tiles run on the tensor
+// cores (FP32 accumulation); everything else on CUDA cores.
 int launch_gemm(int dtype, int64_t N, int64_t M, int64_t K, double alpha, const Mat& A, const Mat& B, const Mat& C,
                 cudaStream_t s) {
+  if (dtype == NLA_F16 && umma_enabled() && N >= 128 && M >= 128 && K >= 64)
+    return launch_sliced_gemm(N, M, K, alpha, A, B, C, NLA_F16, NLA_F16, 1, false, nullptr, 0, s);
   return launch_gemm_simt(dtype, N, M, K, alpha, A, B, C, s);
+}
+
+static int launch_update(const RecPlan& c, int64_t N, int64_t M, int64_t K, double alpha, const Mat& A,
+                         const Mat& B, const Mat& C) {
+  if (c.mode == GEMM_MIXED)
+    return launch_sliced_gemm(N, M, K, alpha, A, B, C, NLA_F64, NLA_F64, c.S, c.bf16, nullptr, 0, c.s);
+  return launch_gemm(c.dtype, N, M, K, alpha, A, B, C, c.s);
 }
 
 // ---------------------------------------------------------------------------
@@ -158,7 +177,7 @@ static bool valid_trans(char c) { return c == 'N' || c == 'T' || c == 'C'; }
 static bool valid_func(char c) { return c == 'S' || c == 'M'; }
 static bool valid_dtype(int d) { return d == NLA_F16 || d == NLA_F32 || d == NLA_F64; }
 
-static int check_flags(char side, char uplo, char trans, char func, int dtype) {
+int check_flags(char side, char uplo, char trans, char func, int dtype) {
   if (!valid_side(side)) return fail(NLA_ERR_ARG, std::string("side must be 'L' or 'R', got '") + side + "'");
   if (!valid_uplo(uplo)) return fail(NLA_ERR_ARG, std::string("uplo must be 'L' or 'U', got '") + uplo + "'");
   if (!valid_trans(trans))
@@ -168,7 +187,7 @@ static int check_flags(char side, char uplo, char trans, char func, int dtype) {
   return NLA_OK;
 }
 
-static int check_matrix(const char* name, const void* p, int64_t rows, int64_t cols, int64_t ld) {
+int check_matrix(const char* name, const void* p, int64_t rows, int64_t cols, int64_t ld) {
   if (rows < 0 || cols < 0) return fail(NLA_ERR_ARG, std::string(name) + ": negative dimension");
   const int64_t need = rows > 1 ? rows : 1;
   if (ld < need) return fail(NLA_ERR_ARG, std::string(name) + ": leading dimension smaller than the row count");
@@ -186,15 +205,7 @@ int64_t split_point(int64_t n) {
 // ---------------------------------------------------------------------------
 // Recursion (unified_rec, src/rectrxm.jl:101-198).
 // ---------------------------------------------------------------------------
-struct Rec {
-  char func, side, uplo;
-  int dtype;
-  int64_t m;
-  int64_t threshold;
-  cudaStream_t s;
-};
-
-static int rec(const Rec& c, const Mat& A, int64_t n, const Mat& B) {
+int recurse(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
   if (n <= c.threshold) return launch_leaf(c.func, c.side, c.uplo, c.dtype, n, c.m, A, B, c.s);
   const int64_t mid = split_point(n), rem = n - mid;
   const int d = c.dtype;
@@ -205,25 +216,25 @@ static int rec(const Rec& c, const Mat& A, int64_t n, const Mat& B) {
                        (!L && c.uplo == 'L' && !S);
   const int64_t m = c.m;
   if (forward) {
-    NLA_TRY(rec(c, A11, mid, B1));
+    NLA_TRY(recurse(c, A11, mid, B1));
     if (L) {
-      if (S) NLA_TRY(launch_gemm(d, rem, m, mid, -1.0, A21, B1, B2, c.s));  // B2 -= A21*B1
-      else NLA_TRY(launch_gemm(d, mid, m, rem, 1.0, A12, B2, B1, c.s));     // B1 += A12*B2
+      if (S) NLA_TRY(launch_update(c, rem, m, mid, -1.0, A21, B1, B2));  // B2 -= A21*B1
+      else NLA_TRY(launch_update(c, mid, m, rem, 1.0, A12, B2, B1));     // B1 += A12*B2
     } else {
-      if (S) NLA_TRY(launch_gemm(d, m, rem, mid, -1.0, B1, A12, B2, c.s));  // B2 -= B1*A12
-      else NLA_TRY(launch_gemm(d, m, mid, rem, 1.0, B2, A21, B1, c.s));     // B1 += B2*A21
+      if (S) NLA_TRY(launch_update(c, m, rem, mid, -1.0, B1, A12, B2));  // B2 -= B1*A12
+      else NLA_TRY(launch_update(c, m, mid, rem, 1.0, B2, A21, B1));     // B1 += B2*A21
     }
-    return rec(c, A22, rem, B2);
+    return recurse(c, A22, rem, B2);
   }
-  NLA_TRY(rec(c, A22, rem, B2));
+  NLA_TRY(recurse(c, A22, rem, B2));
   if (L) {
-    if (S) NLA_TRY(launch_gemm(d, mid, m, rem, -1.0, A12, B2, B1, c.s));  // B1 -= A12*B2
-    else NLA_TRY(launch_gemm(d, rem, m, mid, 1.0, A21, B1, B2, c.s));     // B2 += A21*B1
+    if (S) NLA_TRY(launch_update(c, mid, m, rem, -1.0, A12, B2, B1));  // B1 -= A12*B2
+    else NLA_TRY(launch_update(c, rem, m, mid, 1.0, A21, B1, B2));     // B2 += A21*B1
   } else {
-    if (S) NLA_TRY(launch_gemm(d, m, mid, rem, -1.0, B2, A21, B1, c.s));  // B1 -= B2*A21
-    else NLA_TRY(launch_gemm(d, m, rem, mid, 1.0, B1, A12, B2, c.s));     // B2 += B1*A12
+    if (S) NLA_TRY(launch_update(c, m, mid, rem, -1.0, B2, A21, B1));  // B1 -= B2*A21
+    else NLA_TRY(launch_update(c, m, rem, mid, 1.0, B1, A12, B2));     // B2 += B1*A12
   }
-  return rec(c, A11, mid, B1);
+  return recurse(c, A11, mid, B1);
 }
 
 static int64_t env_cutoff(const char* name, int64_t dflt) {
@@ -254,7 +265,7 @@ int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dty
     uplo = uplo == 'L' ? 'U' : 'L';
   }
   const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
-  Rec c{func, side, uplo, dtype, m, 0, s};
+  RecPlan c{func, side, uplo, dtype, m, 0, s, GEMM_PLAIN, 1, false};
   if (func == 'S') {
     c.threshold = cutoff_s > 0 ? cutoff_s : default_cutoff('S', dtype);
     if (c.threshold > 1024) c.threshold = 1024;
@@ -263,7 +274,7 @@ int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dty
     c.threshold = cutoff_m > 0 ? cutoff_m : default_cutoff('M', dtype);
     if (c.threshold > 1024) c.threshold = 1024;
   }
-  NLA_TRY(rec(c, Am, n, Bm));
+  NLA_TRY(recurse(c, Am, n, Bm));
   if (func == 'M') NLA_TRY(launch_scale(dtype, rows, cols, alpha, Bm, s));  // src/rectrxm.jl:72
   return NLA_OK;
 }

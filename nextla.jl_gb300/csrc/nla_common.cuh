@@ -1,6 +1,7 @@
 // Shared definitions of the GB300 triangular solve / multiply library.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -116,6 +117,33 @@ int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m
 
 // B .= alpha .* B on a rows x cols view.
 int launch_scale(int dtype, int64_t rows, int64_t cols, double alpha, const Mat& B, cudaStream_t s);
+
+// Tensor-core update on staged slices (nla_umma.cu).  C (M x N) += alpha *
+// op(A) (M x K) * op(B) (K x N); in_dtype NLA_F64 (split into S BF16/FP16
+// slices) or NLA_F16 (one unscaled slice); out_dtype NLA_F64 or NLA_F16.
+int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat& A, const Mat& B, const Mat& C,
+                       int in_dtype, int out_dtype, int S, bool bf16, void* ws, size_t ws_bytes, cudaStream_t s);
+size_t sliced_workspace_bytes(int64_t M, int64_t N, int64_t K, int S);
+int workspace_get(cudaStream_t s, size_t bytes, void** out);
+int device_status(cudaStream_t s);
+
+// The recursion of unified_rec (src/rectrxm.jl:101-198) with a choice of
+// update kernel.
+enum GemmMode { GEMM_PLAIN = 0, GEMM_MIXED = 1 };
+struct RecPlan {
+  char func, side, uplo;
+  int dtype;
+  int64_t m;
+  int64_t threshold;
+  cudaStream_t s;
+  int mode;
+  int S;
+  bool bf16;
+};
+int recurse(const RecPlan& c, const Mat& A, int64_t n, const Mat& B);
+int64_t split_point(int64_t n);
+int check_flags(char side, char uplo, char trans, char func, int dtype);
+int check_matrix(const char* name, const void* p, int64_t rows, int64_t cols, int64_t ld);
 
 int num_sms();
 

@@ -1,0 +1,238 @@
+// Mixed-precision form of the recursive triangular solve / multiply: an FP64
+// answer for Float64 inputs, with the off-diagonal updates done on the tensor
+// cores from BF16 or FP16 operand slices (nla_umma.cu) and the diagonal
+// blocks in FP64 (nla_leaf.cu).  For solves, iterative refinement
+//     R = alpha*B - op(A) X   (FP64 residual)
+//     op(A) D = R             (same mixed solver)
+//     X += D
+// wins back the accuracy the split loses.
+#include <cmath>
+#include <cstdlib>
+#include <mutex>
+#include <unordered_map>
+
+#include "nla_common.cuh"
+
+namespace nla {
+namespace {
+
+// Second stream-ordered pool (per device and stream) for the refinement
+// buffers, separate from the update kernels' staging workspace.
+struct Buf {
+  void* p = nullptr;
+  size_t n = 0;
+};
+std::mutex g_buf_mu;
+std::unordered_map<uint64_t, Buf> g_bufs;
+
+int refine_buffers(cudaStream_t s, size_t bytes, void** out) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t key = ((uint64_t)(uint32_t)dev << 48) ^ (uint64_t)reinterpret_cast<uintptr_t>(s);
+  std::lock_guard<std::mutex> lk(g_buf_mu);
+  Buf& b = g_bufs[key];
+  if (b.n < bytes) {
+    if (b.p) cudaFreeAsync(b.p, s);
+    b.p = nullptr;
+    b.n = 0;
+    cudaError_t e = cudaMallocAsync(&b.p, bytes, s);
+    if (e != cudaSuccess) {
+      b.p = nullptr;
+      return cuda_status(e, "refinement buffers");
+    }
+    b.n = bytes;
+  }
+  *out = b.p;
+  return NLA_OK;
+}
+
+// dst = src on rows x cols column-major views.
+__global__ void copy_kernel(int64_t rows, int64_t cols, const double* __restrict__ src, int64_t lds,
+                            double* __restrict__ dst, int64_t ldd) {
+  const int64_t total = rows * cols;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % rows, j = idx / rows;
+    dst[i + j * ldd] = src[i + j * lds];
+  }
+}
+
+// R = B0 - R.
+__global__ void residual_kernel(int64_t rows, int64_t cols, const double* __restrict__ B0, int64_t ldb0,
+                                double* __restrict__ R, int64_t ldr) {
+  const int64_t total = rows * cols;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % rows, j = idx / rows;
+    R[i + j * ldr] = B0[i + j * ldb0] - R[i + j * ldr];
+  }
+}
+
+// X += D, and the largest |D| and |X| (as ordered bit patterns of non-negative
+// doubles) into amax[0], amax[1].
+__global__ void correct_kernel(int64_t rows, int64_t cols, const double* __restrict__ D, int64_t ldd,
+                               double* __restrict__ X, int64_t ldx, unsigned long long* amax) {
+  double md = 0.0, mx = 0.0;
+  const int64_t total = rows * cols;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % rows, j = idx / rows;
+    const double d = D[i + j * ldd];
+    const double x = X[i + j * ldx] + d;
+    X[i + j * ldx] = x;
+    md = fmax(md, fabs(d));
+    mx = fmax(mx, fabs(x));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  if ((threadIdx.x & 31) == 0 && amax) {
+    atomicMax(&amax[0], (unsigned long long)__double_as_longlong(md));
+    atomicMax(&amax[1], (unsigned long long)__double_as_longlong(mx));
+  }
+}
+
+unsigned grid_for(int64_t total) {
+  int64_t blocks = (total + 255) / 256;
+  const int64_t cap = (int64_t)num_sms() * 8;
+  return (unsigned)(blocks < cap ? (blocks > 0 ? blocks : 1) : cap);
+}
+
+int default_mixed_cutoff() {
+  const char* v = std::getenv("NLA_MIXED_CUTOFF");
+  if (v && *v) {
+    long x = std::atol(v);
+    if (x > 0) return (int)(x > 1024 ? 1024 : x);
+  }
+  return 128;
+}
+
+}  // namespace
+
+int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, int64_t n, int64_t m,
+                    const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* o,
+                    cudaStream_t s) {
+  NLA_TRY(check_flags(side, uplo, trans, func, NLA_F64));
+  if (n < 0 || m < 0) return fail(NLA_ERR_ARG, "n and m must be non-negative");
+  NLA_TRY(check_matrix("A", A, n, n, lda));
+  const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
+  NLA_TRY(check_matrix("B", B, rows, cols, ldb));
+  nla_mixed_opts opts{NLA_LOWP_BF16, 3, 2, NLA_RESIDUAL_FP64, 0, nullptr};
+  if (o) opts = *o;
+  if (opts.lowp != NLA_LOWP_BF16 && opts.lowp != NLA_LOWP_F16) return fail(NLA_ERR_ARG, "lowp must be BF16 or F16");
+  if (opts.split_terms < 1 || opts.split_terms > 3) return fail(NLA_ERR_ARG, "split_terms must be 1, 2 or 3");
+  if (opts.sweeps < 0 || opts.sweeps > 8) return fail(NLA_ERR_ARG, "sweeps must be in 0..8");
+  if (opts.residual != NLA_RESIDUAL_FP64) return fail(NLA_ERR_ARG, "unknown residual mode");
+  if (n == 0 || m == 0) return NLA_OK;
+
+  Mat Am{const_cast<double*>(A), lda, 0};
+  Mat Bm{B, ldb, 0};
+  if (trans == 'T' || trans == 'C') {  // src/rectrxm.jl:56-59
+    Am.t = 1;
+    uplo = uplo == 'L' ? 'U' : 'L';
+  }
+  RecPlan mixed{func, side, uplo, NLA_F64, m, opts.cutoff > 0 ? (opts.cutoff > 1024 ? 1024 : opts.cutoff)
+                                                               : default_mixed_cutoff(),
+                s, GEMM_MIXED, opts.split_terms, opts.lowp == NLA_LOWP_BF16};
+
+  // Size the staging workspace once for the largest update (the top split).
+  {
+    const int64_t mid = split_point(n), rem = n - mid;
+    const int64_t big = mid > rem ? mid : rem;
+    void* ws = nullptr;
+    if (n > mixed.threshold) NLA_TRY(workspace_get(s, sliced_workspace_bytes(big, m, big, opts.split_terms), &ws));
+  }
+
+  if (func == 'M') {
+    NLA_TRY(recurse(mixed, Am, n, Bm));
+    return launch_scale(NLA_F64, rows, cols, alpha, Bm, s);  // src/rectrxm.jl:72
+  }
+
+  NLA_TRY(launch_scale(NLA_F64, rows, cols, alpha, Bm, s));  // src/rectrxm.jl:64
+  if (opts.sweeps == 0) return recurse(mixed, Am, n, Bm);
+
+  // Refinement needs alpha*B (B0), a residual/correction buffer (R) and two
+  // device words for the correction norms.
+  const size_t elems = (size_t)rows * (size_t)cols;
+  void* buf = nullptr;
+  NLA_TRY(refine_buffers(s, 2 * elems * sizeof(double) + 256, &buf));
+  double* B0 = static_cast<double*>(buf);
+  double* R = B0 + elems;
+  unsigned long long* amax = reinterpret_cast<unsigned long long*>(R + elems);
+  const unsigned grid = grid_for((int64_t)elems);
+  {
+    TraceScope t(NLA_K_RESIDUAL, s, 0.0, 16.0 * (double)elems);
+    copy_kernel<<<grid, 256, 0, s>>>(rows, cols, B, ldb, B0, rows);
+    NLA_CHECK_LAUNCH("copy_kernel");
+  }
+  NLA_TRY(recurse(mixed, Am, n, Bm));  // X0
+
+  RecPlan resid{'M', side, uplo, NLA_F64, m, 128, s, GEMM_PLAIN, 1, false};
+  Mat Rm{R, rows, 0};
+  for (int k = 0; k < opts.sweeps; ++k) {
+    {
+      TraceScope t(NLA_K_RESIDUAL, s, 0.0, 16.0 * (double)elems);
+      copy_kernel<<<grid, 256, 0, s>>>(rows, cols, B, ldb, R, rows);
+      NLA_CHECK_LAUNCH("copy_kernel");
+    }
+    NLA_TRY(recurse(resid, Am, n, Rm));  // R = op(A) X (or X op(A))
+    {
+      TraceScope t(NLA_K_RESIDUAL, s, (double)elems, 24.0 * (double)elems);
+      residual_kernel<<<grid, 256, 0, s>>>(rows, cols, B0, rows, R, rows);
+      NLA_CHECK_LAUNCH("residual_kernel");
+    }
+    NLA_TRY(recurse(mixed, Am, n, Rm));  // D
+    {
+      TraceScope t(NLA_K_RESIDUAL, s, (double)elems, 24.0 * (double)elems);
+      if (opts.corr_out) cudaMemsetAsync(amax, 0, 2 * sizeof(unsigned long long), s);
+      correct_kernel<<<grid, 256, 0, s>>>(rows, cols, R, rows, B, ldb, opts.corr_out ? amax : nullptr);
+      NLA_CHECK_LAUNCH("correct_kernel");
+    }
+    if (opts.corr_out) {
+      unsigned long long h[2] = {0, 0};
+      cudaError_t e = cudaMemcpyAsync(h, amax, sizeof(h), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) return cuda_status(e, "correction norms");
+      const double md = __builtin_bit_cast(double, h[0]), mx = __builtin_bit_cast(double, h[1]);
+      opts.corr_out[k] = mx > 0 ? md / mx : md;
+    }
+  }
+  return NLA_OK;
+}
+
+}  // namespace nla
+
+using namespace nla;
+
+extern "C" {
+
+int nla_trxm_mixed(char side, char uplo, char trans, double alpha, char func, int64_t n, int64_t m,
+                   const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* opts, void* stream) {
+  clear_error();
+  return trxm_mixed_impl(side, uplo, trans, alpha, func, n, m, A, lda, B, ldb, opts, (cudaStream_t)stream);
+}
+
+int nla_gemm_update_mixed(int trans1, int trans2, int64_t N, int64_t R, int64_t M, double alpha, const double* in1,
+                          int64_t ld1, const double* in2, int64_t ld2, double* out, int64_t ldo, int lowp,
+                          int split_terms, void* stream) {
+  clear_error();
+  if (N < 0 || R < 0 || M < 0) return fail(NLA_ERR_ARG, "N, R and M must be non-negative");
+  if (lowp != NLA_LOWP_BF16 && lowp != NLA_LOWP_F16) return fail(NLA_ERR_ARG, "lowp must be BF16 or F16");
+  if (split_terms < 1 || split_terms > 3) return fail(NLA_ERR_ARG, "split_terms must be 1, 2 or 3");
+  NLA_TRY(check_matrix("in1", in1, trans1 ? R : N, trans1 ? N : R, ld1));
+  NLA_TRY(check_matrix("in2", in2, trans2 ? M : R, trans2 ? R : M, ld2));
+  NLA_TRY(check_matrix("out", out, N, M, ldo));
+  Mat A{const_cast<double*>(in1), ld1, trans1 ? 1 : 0};
+  Mat B{const_cast<double*>(in2), ld2, trans2 ? 1 : 0};
+  Mat C{out, ldo, 0};
+  return launch_sliced_gemm(N, M, R, alpha, A, B, C, NLA_F64, NLA_F64, split_terms, lowp == NLA_LOWP_BF16, nullptr,
+                            0, (cudaStream_t)stream);
+}
+
+int nla_device_status(void* stream) {
+  clear_error();
+  return device_status((cudaStream_t)stream);
+}
+
+}  // extern "C"

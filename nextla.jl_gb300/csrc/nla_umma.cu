@@ -1,0 +1,554 @@
+// Off-diagonal update on the 5th-generation tensor cores (tcgen05) of sm_103a.
+//
+//   C (M x N) += alpha * op(A) (M x K) * op(B) (K x N)
+//
+// The operands are first "staged": each is written as S slices of 16-bit
+// values (BF16 or FP16) in a K-major layout padded to the tile grid, with one
+// power-of-two exponent per row of op(A) and per column of op(B):
+//     x = 2^e * sum_p s_p * 2^(-beta p),   s_p integers, |s_p| <= 2^(beta-1)
+// (beta = 8 for BF16 slices, 11 for FP16).  The split is done with integer
+// arithmetic on the FP64 bit pattern, so it issues no FP64 instruction.
+// A Float16 operand of the plain Float16 path is staged as one unscaled slice.
+//
+// The GEMM kernel (one 128 x 128 output tile per CTA, 6 warps):
+//   warp 0      TMA producer: per 64-wide K block, one 128 x 64 box per slice
+//               of each operand (128-byte swizzle) into a multi-stage ring;
+//   warp 1      allocates TMEM, and one elected lane issues tcgen05.mma for
+//               every slice pair (p, q) kept by the split, accumulating pairs
+//               of equal weight p + q in the same FP32 TMEM accumulator;
+//   warps 2-5   epilogue: tcgen05.ld of the accumulators, combination of the
+//               weights in FP32, and the update of C (one FP64 operation per
+//               element for FP64 outputs; the power-of-two scale is applied
+//               to the exponent bits).
+// Every mbarrier wait is bounded; on expiry the kernel records an error word
+// that nla_device_status() reports, releases its TMEM and returns.
+#include <cudaTypedefs.h>
+
+#include <mutex>
+#include <unordered_map>
+
+#include "nla_common.cuh"
+#include "nla_umma.cuh"
+
+namespace nla {
+
+__device__ int g_device_error = 0;
+
+namespace {
+
+constexpr int BM = 128;
+constexpr int BN = 128;
+constexpr int BK = 64;                     // 64 16-bit elements = one 128-byte swizzle row
+constexpr int TILE_BYTES = BM * BK * 2;    // 16 KiB per slice tile (BN == BM)
+constexpr int GEMM_THREADS = 192;
+constexpr int MAX_PAIRS = 16;
+constexpr int MAX_ACC = 4;
+constexpr int SMEM_LIMIT = 232448;         // 227 KiB opt-in per CTA
+constexpr int SENTINEL_EXP = -2139062144;  // 0x80808080: "no element seen"
+constexpr int NONFINITE_EXP = 0x7fffffff;
+
+enum Epi { EPI_F64 = 0, EPI_F16 = 1 };
+
+struct GemmParams {
+  int M, N;
+  int num_kb;
+  int tiles_m, tiles_n;
+  int a_rows, b_rows;  // padded rows of one slice (row offset between stacked slices)
+  int sa, sb;          // slices of A and B loaded per stage
+  int stages;
+  int stage_bytes;
+  int npairs;
+  int8_t pair_a[MAX_PAIRS], pair_b[MAX_PAIRS], pair_acc[MAX_PAIRS], pair_first[MAX_PAIRS];
+  int nacc;
+  float acc_w[MAX_ACC];
+  uint32_t tmem_cols;
+  uint32_t idesc;
+  void* C;
+  int64_t ldc;
+  double alpha;
+  const int* ea;
+  const int* eb;
+  int exp_bias;
+};
+
+__device__ __forceinline__ double scaled_double(float v, int e) {
+  const uint32_t fb = __float_as_uint(v);
+  if ((fb << 1) == 0) return __longlong_as_double((unsigned long long)(fb >> 31) << 63);
+  const int E = (int)((fb >> 23) & 0xFF);
+  const int de = E - 127 + 1023 + e;
+  if (E == 0 || E == 255 || de <= 0 || de >= 2047) return ldexp((double)v, e);
+  const unsigned long long db = ((unsigned long long)(fb >> 31) << 63) | ((unsigned long long)de << 52) |
+                                ((unsigned long long)(fb & 0x7FFFFFu) << 29);
+  return __longlong_as_double(db);
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
+    umma_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                     const GemmParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)p.stages * p.stage_bytes);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + p.stages;
+  uint64_t* accf = bars + 2 * p.stages;
+  uint64_t* drain = accf + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  __shared__ volatile int s_abort;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  // Grouped rasterisation: 8 row tiles per group keep a wave's operands in L2.
+  const int group = 8;
+  const int per_group = group * p.tiles_n;
+  const int g = blockIdx.x / per_group;
+  const int first_m = g * group;
+  const int gsize = min(p.tiles_m - first_m, group);
+  const int local = blockIdx.x % per_group;
+  const int tm = first_m + local % gsize;
+  const int tn = local / gsize;
+  const int m0 = tm * BM, n0 = tn * BN;
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int s = 0; s < p.stages; ++s) {
+      umma::mbar_init(umma::smem_u32(&full[s]), 1);
+      umma::mbar_init(umma::smem_u32(&empty[s]), 1);
+    }
+    umma::mbar_init(umma::smem_u32(accf), 1);
+    umma::mbar_init(umma::smem_u32(drain), 1);
+    umma::fence_barrier_init();
+    umma::prefetch_tmap(&tmA);
+    umma::prefetch_tmap(&tmB);
+  }
+  if (warp == 1) umma::tmem_alloc(umma::smem_u32(tmem_slot), p.tmem_cols);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int kb = 0; kb < p.num_kb; ++kb) {
+        const int s = kb % p.stages;
+        const uint32_t round = (uint32_t)(kb / p.stages);
+        if (!umma::mbar_wait(umma::smem_u32(&empty[s]), (round & 1u) ^ 1u, &s_abort, &g_device_error, 1)) break;
+        const uint32_t fb = umma::smem_u32(&full[s]);
+        umma::mbar_arrive_expect_tx(fb, (uint32_t)p.stage_bytes);
+        uint8_t* st = smem + (size_t)s * p.stage_bytes;
+        for (int sl = 0; sl < p.sa; ++sl)
+          umma::tma_load_2d(umma::smem_u32(st + sl * TILE_BYTES), &tmA, fb, kb * BK, sl * p.a_rows + m0);
+        for (int sl = 0; sl < p.sb; ++sl)
+          umma::tma_load_2d(umma::smem_u32(st + (p.sa + sl) * TILE_BYTES), &tmB, fb, kb * BK, sl * p.b_rows + n0);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      bool ok = true;
+      for (int kb = 0; kb < p.num_kb; ++kb) {
+        const int s = kb % p.stages;
+        const uint32_t round = (uint32_t)(kb / p.stages);
+        if (!umma::mbar_wait(umma::smem_u32(&full[s]), round & 1u, &s_abort, &g_device_error, 2)) {
+          ok = false;
+          break;
+        }
+        umma::fence_after_sync();
+        const uint32_t st = umma::smem_u32(smem + (size_t)s * p.stage_bytes);
+        for (int pr = 0; pr < p.npairs; ++pr) {
+          const uint32_t a0 = st + p.pair_a[pr] * TILE_BYTES;
+          const uint32_t b0 = st + (p.sa + p.pair_b[pr]) * TILE_BYTES;
+          const uint32_t d = tmem + (uint32_t)(p.pair_acc[pr] * BN);
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk) {
+            const uint32_t acc = (kb > 0 || kk > 0 || !p.pair_first[pr]) ? 1u : 0u;
+            umma::mma_f16(d, umma::desc_kmajor_sw128(a0 + kk * 32), umma::desc_kmajor_sw128(b0 + kk * 32), p.idesc,
+                          acc);
+          }
+        }
+        umma::mma_commit(umma::smem_u32(&empty[s]));
+      }
+      if (ok) umma::mma_commit(umma::smem_u32(accf));
+      // Before TMEM is released every issued MMA must have finished.
+      umma::mma_commit(umma::smem_u32(drain));
+      umma::mbar_wait(umma::smem_u32(drain), 0, &s_abort, &g_device_error, 3, false);
+    }
+  } else {
+    // Epilogue warps 2..5 own TMEM lane quadrants (warp % 4).
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    const int i = m0 + row;
+    // tcgen05.ld is warp-collective: the lanes act on one shared verdict.
+    const bool ok = __all_sync(0xffffffffu, umma::mbar_wait(umma::smem_u32(accf), 0, &s_abort, &g_device_error, 4));
+    umma::fence_after_sync();
+    if (ok) {
+      const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16);
+      int ei = 0;
+      bool row_nan = false;
+      if (EPI == EPI_F64 && p.ea != nullptr && i < p.M) {
+        ei = p.ea[i];
+        row_nan = ei == NONFINITE_EXP;
+        ei = max(ei, -4000);
+      }
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        float v[16];
+        uint32_t r[16];
+        umma::tmem_ld16(tq + (uint32_t)c0, r);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+        for (int a = 1; a < p.nacc; ++a) {
+          umma::tmem_ld16(tq + (uint32_t)(a * BN + c0), r);
+          const float w = p.acc_w[a];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = fmaf(__uint_as_float(r[j]), w, v[j]);
+        }
+        if (i < p.M) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = n0 + c0 + j;
+            if (col >= p.N) continue;
+            if (EPI == EPI_F64) {
+              double* cp = static_cast<double*>(p.C) + i + (int64_t)col * p.ldc;
+              int ej = p.eb != nullptr ? p.eb[col] : 0;
+              if (row_nan || ej == NONFINITE_EXP) {
+                *cp = __longlong_as_double(0x7ff8000000000000ull);
+              } else {
+                const double d = scaled_double(v[j], ei + max(ej, -4000) + p.exp_bias);
+                *cp = fma(p.alpha, d, *cp);
+              }
+            } else {
+              __half* cp = static_cast<__half*>(p.C) + i + (int64_t)col * p.ldc;
+              *cp = __float2half_rn(fmaf((float)p.alpha, v[j], __half2float(*cp)));
+            }
+          }
+        }
+      }
+    }
+  }
+
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    umma::fence_after_sync();
+    umma::tmem_dealloc(tmem, p.tmem_cols);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Staging kernels.
+// ---------------------------------------------------------------------------
+
+template <typename T> __device__ __forceinline__ double to_double(T x);
+template <> __device__ __forceinline__ double to_double<double>(double x) { return x; }
+template <> __device__ __forceinline__ double to_double<__half>(__half x) { return (double)__half2float(x); }
+
+// frexp-style exponent of |x| plus one (so that x * 2^-e lies in [0.25, 0.5)
+// for the largest element), from the bit pattern.
+__device__ __forceinline__ int exp_of(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int biased = (int)((b >> 52) & 0x7FF);
+  const unsigned long long mant = b & ((1ull << 52) - 1);
+  if (biased == 0x7FF) return NONFINITE_EXP;
+  if (biased == 0) return mant == 0 ? SENTINEL_EXP : -1021;
+  return biased - 1022 + 1;
+}
+
+// Per-row maximum exponent of a rows x cols view (op(X) = X or X^T), one
+// 64 x 64 tile per CTA, reduced into e[] with atomicMax.
+template <typename T>
+__global__ void __launch_bounds__(256) row_exp_kernel(const T* __restrict__ X, int64_t ld, int t, int64_t rows,
+                                                      int64_t cols, int* __restrict__ e) {
+  __shared__ int se[64];
+  if (threadIdx.x < 64) se[threadIdx.x] = SENTINEL_EXP;
+  __syncthreads();
+  const int64_t i0 = (int64_t)blockIdx.x * 64, k0 = (int64_t)blockIdx.y * 64;
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+    int i, k;
+    if (!t) { i = idx & 63; k = idx >> 6; } else { k = idx & 63; i = idx >> 6; }
+    const int64_t gi = i0 + i, gk = k0 + k;
+    if (gi < rows && gk < cols) {
+      const int ex = exp_of(to_double(X[mat_off(gi, gk, ld, t)]));
+      if (ex != SENTINEL_EXP) atomicMax(&se[i], ex);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 64 && i0 + threadIdx.x < rows && se[threadIdx.x] != SENTINEL_EXP)
+    atomicMax(&e[i0 + threadIdx.x], se[threadIdx.x]);
+}
+
+template <typename S> __device__ __forceinline__ S from_int(int v);
+template <> __device__ __forceinline__ __nv_bfloat16 from_int<__nv_bfloat16>(int v) {
+  return __float2bfloat16_rn((float)v);
+}
+template <> __device__ __forceinline__ __half from_int<__half>(int v) { return __float2half_rn((float)v); }
+
+// Split a rows x cols view into `ns` K-major slices of type Sl (rows padded
+// to rows_pad, K padded to cols_pad, zeros in the padding).  With copy set,
+// the single slice is the element itself (a Float16 operand of the plain
+// path); otherwise slices are the integers s_p of
+//   x = 2^e[row] * sum_p s_p 2^(-beta p).
+template <typename T, typename Sl>
+__global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int64_t ld, int t, int64_t rows,
+                                                    int64_t cols, const int* __restrict__ e, Sl* __restrict__ out,
+                                                    int64_t rows_pad, int64_t cols_pad, int ns, int beta, int copy) {
+  __shared__ double tile[32][65];
+  const int64_t i0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 64;
+  for (int idx = threadIdx.x; idx < 32 * 64; idx += 256) {
+    int i, k;
+    if (!t) { i = idx & 31; k = idx >> 5; } else { k = idx & 63; i = idx >> 6; }
+    const int64_t gi = i0 + i, gk = k0 + k;
+    tile[i][k] = (gi < rows && gk < cols) ? to_double(X[mat_off(gi, gk, ld, t)]) : 0.0;
+  }
+  __syncthreads();
+  const int64_t slice_elems = rows_pad * cols_pad;
+  for (int idx = threadIdx.x; idx < 32 * 64; idx += 256) {
+    const int i = idx >> 6, k = idx & 63;
+    const int64_t gi = i0 + i, gk = k0 + k;
+    const int64_t o = gi * cols_pad + gk;
+    const double x = tile[i][k];
+    if (copy) {
+      out[o] = (Sl)(float)x;
+      continue;
+    }
+    const int ex = gi < rows ? e[gi] : SENTINEL_EXP;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int biased = (int)((b >> 52) & 0x7FF);
+    const unsigned long long mant = b & ((1ull << 52) - 1);
+    long long Y = 0;
+    if (biased != 0x7FF && ex != NONFINITE_EXP && ex != SENTINEL_EXP && (biased != 0 || mant != 0)) {
+      const unsigned long long m = biased ? (mant | (1ull << 52)) : mant;
+      const int eb = biased ? biased : 1;
+      const int sh = eb - 1013 - ex;  // Y = m * 2^sh = x * 2^(62 - ex)
+      if (sh >= 0) Y = (long long)(m << sh);
+      else if (sh > -63) Y = (long long)((m + (1ull << (-sh - 1))) >> (-sh));
+      if (b >> 63) Y = -Y;
+    }
+    for (int sl = 0; sl < ns; ++sl) {
+      const int shift = 62 - beta * (sl + 1);
+      const long long sp = (Y + (1ll << (shift - 1))) >> shift;
+      Y -= sp << shift;
+      out[(int64_t)sl * slice_elems + o] = from_int<Sl>((int)sp);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+int make_map(CUtensorMap* map, const void* base, bool bf16, uint64_t cols_pad, uint64_t total_rows) {
+  auto fn = encode_fn();
+  if (!fn) return fail(NLA_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available from the driver");
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0) return fail(NLA_ERR_ARG, "staged operand is not 16-byte aligned");
+  cuuint64_t dims[2] = {cols_pad, total_rows};
+  cuuint64_t strides[1] = {cols_pad * 2};
+  cuuint32_t box[2] = {BK, BM};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                  const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(NLA_ERR_ARG, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return NLA_OK;
+}
+
+// Stream-ordered, grow-only workspace per (device, stream).
+struct Pool {
+  void* ptr = nullptr;
+  size_t size = 0;
+};
+std::mutex g_pool_mu;
+std::unordered_map<uint64_t, Pool> g_pools;
+
+int64_t pad_to(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+template <typename F>
+void set_smem_once(F* kernel, int bytes) {
+  static std::once_flag once;
+  std::call_once(once, [&] { cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes); });
+}
+
+}  // namespace
+
+int workspace_get(cudaStream_t s, size_t bytes, void** out) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t key = ((uint64_t)(uint32_t)dev << 48) ^ (uint64_t)reinterpret_cast<uintptr_t>(s);
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  Pool& p = g_pools[key];
+  if (p.size < bytes) {
+    if (p.ptr) cudaFreeAsync(p.ptr, s);
+    p.ptr = nullptr;
+    p.size = 0;
+    size_t want = bytes + bytes / 8 + (1 << 20);
+    cudaError_t e = cudaMallocAsync(&p.ptr, want, s);
+    if (e != cudaSuccess) {
+      p.ptr = nullptr;
+      return cuda_status(e, "workspace allocation");
+    }
+    p.size = want;
+  }
+  *out = p.ptr;
+  return NLA_OK;
+}
+
+size_t sliced_workspace_bytes(int64_t M, int64_t N, int64_t K, int S) {
+  const int64_t Mp = pad_to(M, BM), Np = pad_to(N, BN), Kp = pad_to(K, BK);
+  size_t b = (size_t)S * (size_t)(Mp + Np) * (size_t)Kp * 2;
+  b = (b + 1023) & ~(size_t)1023;
+  b += (size_t)(Mp + Np) * sizeof(int) + 1024;
+  return b;
+}
+
+// One tensor-core update.  in_dtype is NLA_F64 (split into S slices of BF16
+// or FP16) or NLA_F16 (S = 1, staged as is).  out_dtype is NLA_F64 or NLA_F16.
+int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat& A, const Mat& B, const Mat& C,
+                       int in_dtype, int out_dtype, int S, bool bf16, void* ws, size_t ws_bytes, cudaStream_t s) {
+  if (M <= 0 || N <= 0) return NLA_OK;
+  if (K <= 0) return NLA_OK;
+  if (C.t) return fail(NLA_ERR_UNSUPPORTED, "tensor-core update: transposed output view");
+  const bool copy = in_dtype == NLA_F16;
+  if (copy) S = 1;
+  if (S < 1 || S > 3) return fail(NLA_ERR_ARG, "split terms must be 1, 2 or 3");
+  const int beta = bf16 ? 8 : 11;
+  const int64_t Mp = pad_to(M, BM), Np = pad_to(N, BN), Kp = pad_to(K, BK);
+  if (S * Mp > 0xFFFFFFFFLL || S * Np > 0xFFFFFFFFLL) return fail(NLA_ERR_UNSUPPORTED, "operand too large");
+  const size_t need = sliced_workspace_bytes(M, N, K, S);
+  void* base = ws;
+  if (base == nullptr) {
+    NLA_TRY(workspace_get(s, need, &base));
+  } else if (ws_bytes < need) {
+    return fail(NLA_ERR_WORKSPACE, "workspace too small for the tensor-core update");
+  }
+  uint8_t* w = static_cast<uint8_t*>(base);
+  void* As = w;
+  void* Bs = w + (size_t)S * Mp * Kp * 2;
+  size_t off = ((size_t)S * (Mp + Np) * Kp * 2 + 1023) & ~(size_t)1023;
+  int* ea = reinterpret_cast<int*>(w + off);
+  int* eb = ea + Mp;
+
+  const Mat Bt = transposed(B);  // N x K view: row j is column j of op(B)
+  {
+    TraceScope trace(NLA_K_SPLIT, s, 0.0,
+                     (double)(M * K + K * N) * (double)dtype_size(in_dtype) * (copy ? 1 : 2) +
+                         (double)S * (Mp + Np) * Kp * 2);
+    if (!copy) {
+      cudaMemsetAsync(ea, 0x80, (size_t)(Mp + Np) * sizeof(int), s);
+      dim3 ga((unsigned)((M + 63) / 64), (unsigned)((K + 63) / 64));
+      dim3 gb((unsigned)((N + 63) / 64), (unsigned)((K + 63) / 64));
+      row_exp_kernel<double><<<ga, 256, 0, s>>>((const double*)A.p, A.ld, A.t, M, K, ea);
+      row_exp_kernel<double><<<gb, 256, 0, s>>>((const double*)Bt.p, Bt.ld, Bt.t, N, K, eb);
+      NLA_CHECK_LAUNCH("row_exp_kernel");
+      dim3 sa((unsigned)(Mp / 32), (unsigned)(Kp / 64)), sb((unsigned)(Np / 32), (unsigned)(Kp / 64));
+      if (bf16) {
+        split_kernel<double, __nv_bfloat16><<<sa, 256, 0, s>>>((const double*)A.p, A.ld, A.t, M, K, ea,
+                                                               (__nv_bfloat16*)As, Mp, Kp, S, beta, 0);
+        split_kernel<double, __nv_bfloat16><<<sb, 256, 0, s>>>((const double*)Bt.p, Bt.ld, Bt.t, N, K, eb,
+                                                               (__nv_bfloat16*)Bs, Np, Kp, S, beta, 0);
+      } else {
+        split_kernel<double, __half><<<sa, 256, 0, s>>>((const double*)A.p, A.ld, A.t, M, K, ea, (__half*)As, Mp,
+                                                        Kp, S, beta, 0);
+        split_kernel<double, __half><<<sb, 256, 0, s>>>((const double*)Bt.p, Bt.ld, Bt.t, N, K, eb, (__half*)Bs,
+                                                        Np, Kp, S, beta, 0);
+      }
+    } else {
+      dim3 sa((unsigned)(Mp / 32), (unsigned)(Kp / 64)), sb((unsigned)(Np / 32), (unsigned)(Kp / 64));
+      split_kernel<__half, __half><<<sa, 256, 0, s>>>((const __half*)A.p, A.ld, A.t, M, K, nullptr, (__half*)As,
+                                                      Mp, Kp, 1, 0, 1);
+      split_kernel<__half, __half><<<sb, 256, 0, s>>>((const __half*)Bt.p, Bt.ld, Bt.t, N, K, nullptr,
+                                                      (__half*)Bs, Np, Kp, 1, 0, 1);
+    }
+    NLA_CHECK_LAUNCH("split_kernel");
+  }
+
+  const bool use_bf16 = copy ? false : bf16;
+  CUtensorMap mA, mB;
+  NLA_TRY(make_map(&mA, As, use_bf16, (uint64_t)Kp, (uint64_t)(S * Mp)));
+  NLA_TRY(make_map(&mB, Bs, use_bf16, (uint64_t)Kp, (uint64_t)(S * Np)));
+
+  GemmParams p{};
+  p.M = (int)M;
+  p.N = (int)N;
+  p.num_kb = (int)(Kp / BK);
+  p.tiles_m = (int)(Mp / BM);
+  p.tiles_n = (int)(Np / BN);
+  p.a_rows = (int)Mp;
+  p.b_rows = (int)Np;
+  p.sa = S;
+  p.sb = S;
+  p.stage_bytes = 2 * S * TILE_BYTES;
+  p.stages = (SMEM_LIMIT - 1024 - 256) / p.stage_bytes;
+  if (p.stages > 6) p.stages = 6;
+  // Slice pairs (a, b) with a + b <= S - 1 (0-based), grouped by weight.
+  p.npairs = 0;
+  p.nacc = S;
+  for (int t = 0; t < S; ++t) {
+    p.acc_w[t] = ldexpf(1.0f, -beta * t);
+    for (int a = 0; a <= t; ++a) {
+      const int b = t - a;
+      p.pair_a[p.npairs] = (int8_t)a;
+      p.pair_b[p.npairs] = (int8_t)b;
+      p.pair_acc[p.npairs] = (int8_t)t;
+      p.pair_first[p.npairs] = (int8_t)(a == 0);
+      ++p.npairs;
+    }
+  }
+  uint32_t cols = 32;
+  while (cols < (uint32_t)(p.nacc * BN)) cols <<= 1;
+  p.tmem_cols = cols;
+  p.idesc = umma::idesc_f16(BM, BN, use_bf16);
+  p.C = C.p;
+  p.ldc = C.ld;
+  p.alpha = alpha;
+  p.ea = copy ? nullptr : ea;
+  p.eb = copy ? nullptr : eb;
+  p.exp_bias = copy ? 0 : -2 * beta;
+
+  const int smem = p.stages * p.stage_bytes + 1024 + 256;
+  const int64_t grid = (int64_t)p.tiles_m * p.tiles_n;
+  if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "too many output tiles");
+  const double pair_flops = 2.0 * (double)M * (double)N * (double)K;
+  TraceScope trace(NLA_K_GEMM_UMMA, s, pair_flops * p.npairs,
+                   (double)S * (Mp + Np) * Kp * 2 + 2.0 * (double)M * N * (double)dtype_size(out_dtype));
+  if (out_dtype == NLA_F64) {
+    set_smem_once(umma_gemm_kernel<EPI_F64>, SMEM_LIMIT);
+    umma_gemm_kernel<EPI_F64><<<(unsigned)grid, GEMM_THREADS, smem, s>>>(mA, mB, p);
+  } else if (out_dtype == NLA_F16) {
+    set_smem_once(umma_gemm_kernel<EPI_F16>, SMEM_LIMIT);
+    umma_gemm_kernel<EPI_F16><<<(unsigned)grid, GEMM_THREADS, smem, s>>>(mA, mB, p);
+  } else {
+    return fail(NLA_ERR_DTYPE, "tensor-core update: unsupported output type");
+  }
+  NLA_CHECK_LAUNCH("umma_gemm_kernel");
+  return NLA_OK;
+}
+
+// Reads and clears the device error word after synchronising the stream.
+int device_status(cudaStream_t s) {
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(e, "stream synchronize");
+  int v = 0;
+  e = cudaMemcpyFromSymbol(&v, g_device_error, sizeof(int));
+  if (e != cudaSuccess) return cuda_status(e, "read device status");
+  if (v != 0) {
+    int zero = 0;
+    cudaMemcpyToSymbol(g_device_error, &zero, sizeof(int));
+    return fail(NLA_ERR_TIMEOUT, "a bounded device-side wait gave up (site " + std::to_string(v) + ")");
+  }
+  return NLA_OK;
+}
+
+}  // namespace nla

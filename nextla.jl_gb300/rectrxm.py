@@ -310,3 +310,73 @@ def unified_rectrxm_(side, uplo, transpose, alpha, func, A, B, *, native=False, 
     if func == "M":
         scale_(B, alpha)
     return B
+
+
+# ---------------------------------------------------------------------------
+# Mixed-precision form (no counterpart in the reference): FP64 answers with
+# the off-diagonal updates on the tcgen05 tensor cores.
+# ---------------------------------------------------------------------------
+
+_LOWP = {"bf16": _lib.NLA_LOWP_BF16, "f16": _lib.NLA_LOWP_F16}
+
+
+def matmul_mixed_(output, input1, input2, alpha=1.0, *, lowp="bf16", split_terms=3):
+    """output += alpha * input1 * input2 for Float64 tensors, formed on the
+    tensor cores from ``split_terms`` BF16/FP16 slices of each operand."""
+    o, ldo, to = _mat(output)
+    if to:
+        raise ValueError("output must be a column-major view")
+    a, ld1, t1 = _mat(input1)
+    b, ld2, t2 = _mat(input2)
+    N, M = output.shape
+    R = input1.shape[1]
+    if input1.shape[0] != N or tuple(input2.shape) != (R, M):
+        raise ValueError("matmul_mixed_: shapes do not conform")
+    for X in (output, input1, input2):
+        if _dtype_code(X) != _lib.NLA_F64:
+            raise ValueError("the mixed form takes Float64 operands")
+    L = _lib.load()
+    _lib.check(L.nla_gemm_update_mixed(t1, t2, N, R, M, float(alpha), a, ld1, b, ld2, o, ldo, _LOWP[lowp],
+                                       int(split_terms), _stream(output)))
+    return output
+
+
+def unified_rectrxm_mixed_(side, uplo, transpose, alpha, func, A, B, *, lowp="bf16", split_terms=3, sweeps=2,
+                           cutoff=0, corrections=False):
+    """Mixed-precision unified_rectrxm! for Float64 A and B (in place in B).
+
+    Updates run on the tensor cores from ``split_terms`` slices (``lowp`` 'bf16'
+    or 'f16'); diagonal blocks of size ``cutoff`` (0: library default) run in
+    FP64; solves add ``sweeps`` FP64-residual refinement sweeps.  With
+    ``corrections=True`` returns (B, [max|D|/max|X| per sweep])."""
+    import ctypes
+
+    _check_flags(side, uplo, transpose, func)
+    _check_operands(A, B, side)
+    if _dtype_code(B) != _lib.NLA_F64:
+        raise ValueError("the mixed form takes Float64 operands")
+    a, lda, ta = _mat(A)
+    b, ldb, tb = _mat(B)
+    if tb:
+        raise ValueError("B must be a column-major view")
+    tr, up = transpose, uplo
+    if ta:
+        tr = "N" if transpose in ("T", "C") else "T"
+        up = "U" if uplo == "L" else "L"
+    n = A.shape[0]
+    m = B.shape[1] if side == "L" else B.shape[0]
+    corr = (ctypes.c_double * max(int(sweeps), 1))()
+    opts = _lib.MixedOpts(_LOWP[lowp], int(split_terms), int(sweeps), _lib.NLA_RESIDUAL_FP64, int(cutoff),
+                          ctypes.cast(corr, ctypes.POINTER(ctypes.c_double)) if corrections else None)
+    L = _lib.load()
+    _lib.check(L.nla_trxm_mixed(_lib.ch(side), _lib.ch(up), _lib.ch(tr), float(alpha), _lib.ch(func), n, m, a, lda,
+                                b, ldb, ctypes.byref(opts), _stream(B)))
+    if corrections:
+        return B, [corr[i] for i in range(int(sweeps))] if func == "S" else []
+    return B
+
+
+def device_status(X=None):
+    """Synchronise the stream and raise if a bounded device-side wait gave up."""
+    L = _lib.load()
+    _lib.check(L.nla_device_status(_stream(X) if X is not None else None))

@@ -1,0 +1,81 @@
+"""Mixed-precision form against FP64 references.
+
+Bounds (relative Frobenius error against the FP64 oracle's answer, on
+well-conditioned seeded systems):
+  no refinement, BF16 x3 or FP16 x2 slices:   < 1e-5
+  with 2 refinement sweeps:                   < 1e-13 (plain FP64 level), and
+                                              backward error within 2x of the
+                                              plain FP64 path's (+1e-3)
+  multiply (no refinement), BF16 x3:          < 1e-5
+"""
+
+import itertools
+import os
+
+import numpy as np
+import pytest
+
+from gpu_util import to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixed(pkg, cuda, side, uplo, trans, alpha, func, A, B, **kw):
+    import torch
+
+    Ad, Bd = to_dev(A, np.float64, cuda), to_dev(B, np.float64, cuda)
+    out = pkg.unified_rectrxm_mixed_(side, uplo, trans, alpha, func, Ad, Bd, **kw)
+    pkg.device_status(Bd)
+    torch.cuda.synchronize()
+    if isinstance(out, tuple):
+        return to_host(Bd), out[1]
+    return to_host(Bd)
+
+
+@pytest.mark.parametrize("lowp,terms", [("bf16", 3), ("f16", 2)])
+def test_mixed_solve_all_forms(pkg, oracle, workloads, cuda, lowp, terms):
+    nthreads = os.cpu_count() or 1
+    for n, side, uplo, trans in itertools.product([300, 1000], "LR", "LU", "NT"):
+        A, B = workloads.problem(n, 40, side, uplo, seed=n + 1)
+        ref = oracle.rectrxm(side, uplo, trans, 0.5, "S", A, B, nthreads=nthreads)
+        X0 = _mixed(pkg, cuda, side, uplo, trans, 0.5, "S", A, B, lowp=lowp, split_terms=terms, sweeps=0, cutoff=64)
+        assert oracle.rel_err(X0, ref) < 1e-5, (n, side, uplo, trans)
+        X2 = _mixed(pkg, cuda, side, uplo, trans, 0.5, "S", A, B, lowp=lowp, split_terms=terms, sweeps=2,
+                    cutoff=64)
+        assert oracle.rel_err(X2, ref) < 1e-13, (n, side, uplo, trans)
+
+
+def test_refinement_matches_plain_backward_error(pkg, oracle, workloads, cuda):
+    import torch
+
+    n, m = 2048, 64
+    A, B = workloads.problem(n, m, "L", "L", seed=21)
+    X, corr = _mixed(pkg, cuda, "L", "L", "N", 1.0, "S", A, B, sweeps=3, corrections=True)
+    Ad, Bd = to_dev(A, np.float64, cuda), to_dev(B, np.float64, cuda)
+    pkg.unified_rectrxm_("L", "L", "N", 1.0, "S", Ad, Bd, native=True)
+    torch.cuda.synchronize()
+    Xp = to_host(Bd)
+    be_mixed = oracle.backward_error("L", "L", "N", 1.0, A, X, B)
+    be_plain = oracle.backward_error("L", "L", "N", 1.0, A, Xp, B)
+    assert be_mixed <= 2 * be_plain + 1e-3, (be_mixed, be_plain)
+    assert corr[0] < 1e-5 and corr[-1] < corr[0], corr
+
+
+@pytest.mark.parametrize("side,uplo,trans", [("R", "U", "T"), ("L", "L", "N"), ("L", "U", "T"), ("R", "L", "N")])
+def test_mixed_multiply(pkg, oracle, workloads, cuda, side, uplo, trans):
+    A, B = workloads.problem(777, 50, side, uplo, seed=3)
+    ref = oracle.rectrxm(side, uplo, trans, -2.0, "M", A, B, nthreads=os.cpu_count() or 1)
+    X = _mixed(pkg, cuda, side, uplo, trans, -2.0, "M", A, B, split_terms=3)
+    assert oracle.rel_err(X, ref) < 1e-5
+
+
+def test_mixed_rejects_bad_options(pkg, cuda):
+    import torch
+
+    A = to_dev(np.eye(4), np.float64, cuda)
+    B = to_dev(np.ones((4, 2)), np.float64, cuda)
+    with pytest.raises(ValueError):
+        pkg.unified_rectrxm_mixed_("L", "L", "N", 1.0, "S", A, B, split_terms=5)
+    with pytest.raises(ValueError):
+        pkg.unified_rectrxm_mixed_("L", "L", "N", 1.0, "S", A.float(), B.float())
+    torch.cuda.synchronize()

@@ -1,0 +1,101 @@
+"""Tensor-core (tcgen05) update kernel against torch references.
+
+Float16 plain path: the update must equal the FP32 product of the Float16
+inputs rounded once to Float16 (relative error < 2e-3, i.e. about 2 Float16
+ulps).  Mixed path: the error against an FP64 product must fall with the
+number of slices: BF16 (8-bit slices) 1/2/3 terms < 2e-2 / 1e-4 / 5e-6,
+FP16 (11-bit slices) < 2e-3 / 5e-6 / 5e-6 (FP32 accumulation bounds the last).
+"""
+
+import itertools
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _col_major(t):
+    return t.T.contiguous().T
+
+
+def _rel(x, ref):
+    import torch
+
+    return float(torch.linalg.norm((x - ref).double()) / torch.linalg.norm(ref.double()))
+
+
+def test_umma_f16_update_small(pkg, cuda):
+    import torch
+
+    g = torch.Generator(device=cuda).manual_seed(0)
+    for (N, R, M), t1, t2 in itertools.product([(128, 64, 128), (300, 200, 257), (1024, 512, 640)], [False, True],
+                                               [False, True]):
+        C = _col_major(torch.rand(N, M, device=cuda, generator=g).half())
+        A = _col_major(torch.rand(R, N, device=cuda, generator=g).half()) if t1 else \
+            _col_major(torch.rand(N, R, device=cuda, generator=g).half())
+        B = _col_major(torch.rand(M, R, device=cuda, generator=g).half()) if t2 else \
+            _col_major(torch.rand(R, M, device=cuda, generator=g).half())
+        opA = A.T if t1 else A
+        opB = B.T if t2 else B
+        ref = (C.float() - opA.float() @ opB.float()).half()
+        pkg.GEMM_SUB_(C, opA, opB)
+        pkg.device_status(C)
+        assert _rel(C, ref) < 2e-3, (N, R, M, t1, t2)
+
+
+@pytest.mark.parametrize("lowp", ["bf16", "f16"])
+def test_mixed_update_error_falls_with_terms(pkg, cuda, lowp):
+    import torch
+
+    g = torch.Generator(device=cuda).manual_seed(1)
+    bounds = {"bf16": [2e-2, 1e-4, 5e-6], "f16": [2e-3, 5e-6, 5e-6]}[lowp]
+    for (N, R, M), t1 in itertools.product([(256, 300, 130), (700, 1024, 515)], [False, True]):
+        C0 = _col_major(torch.randn(N, M, device=cuda, generator=g, dtype=torch.float64))
+        A = torch.randn(R if t1 else N, N if t1 else R, device=cuda, generator=g, dtype=torch.float64)
+        A = _col_major(A * torch.exp(2 * torch.randn(A.shape[0], 1, device=cuda, generator=g, dtype=torch.float64)))
+        B = _col_major(torch.randn(R, M, device=cuda, generator=g, dtype=torch.float64))
+        opA = A.T if t1 else A
+        prod = opA @ B
+        ref = C0 - prod
+        errs = []
+        for S in (1, 2, 3):
+            C = C0.clone().T.contiguous().T
+            pkg.matmul_mixed_(C, opA, B, -1.0, lowp=lowp, split_terms=S)
+            pkg.device_status(C)
+            # error relative to the size of the product
+            errs.append(float(torch.linalg.norm(C - ref) / torch.linalg.norm(prod)))
+        for S, (e, b) in enumerate(zip(errs, bounds), 1):
+            assert e < b, (lowp, N, R, M, t1, S, errs)
+        assert errs[1] < errs[0]
+
+
+def test_mixed_update_exact_for_short_integers(pkg, cuda):
+    """Products of values with at most 8 significant bits are exact with one
+    BF16 slice when the sum fits FP32: the result must be bit-exact."""
+    import torch
+
+    g = torch.Generator(device=cuda).manual_seed(2)
+    N, R, M = 256, 128, 256
+    A = _col_major(torch.randint(-100, 101, (N, R), device=cuda, generator=g).double())
+    B = _col_major(torch.randint(-100, 101, (R, M), device=cuda, generator=g).double())
+    C = _col_major(torch.zeros(N, M, device=cuda, dtype=torch.float64))
+    ref = A @ B
+    pkg.matmul_mixed_(C, A, B, 1.0, lowp="bf16", split_terms=2)
+    pkg.device_status(C)
+    assert torch.equal(C, ref)
+
+
+def test_mixed_update_nonfinite_rows_give_nan(pkg, cuda):
+    import torch
+
+    N, R, M = 128, 64, 128
+    A = _col_major(torch.ones(N, R, device=cuda, dtype=torch.float64))
+    A[5, 3] = float("inf")
+    B = _col_major(torch.ones(R, M, device=cuda, dtype=torch.float64))
+    C = _col_major(torch.zeros(N, M, device=cuda, dtype=torch.float64))
+    pkg.matmul_mixed_(C, A, B, 1.0)
+    pkg.device_status(C)
+    assert torch.isnan(C[5]).all()
+    assert torch.isfinite(C[:5]).all() and torch.isfinite(C[6:]).all()
+    assert float(C[0, 0]) == 64.0
