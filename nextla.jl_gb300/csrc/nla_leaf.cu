@@ -27,6 +27,8 @@
 //             writes it straight to global memory (B was fully staged first,
 //             so the in-place update has no hazard).
 // Float16 blocks are computed in Float32 and rounded once when stored.
+#include <mutex>
+
 #include "nla_common.cuh"
 
 namespace nla {
@@ -228,29 +230,32 @@ size_t leaf_smem(char func, int n) {
 }
 
 template <typename T, int CW>
+int leaf_smem_attr() {
+  static std::once_flag once;
+  static cudaError_t st = cudaSuccess;
+  std::call_once(once, [] {
+    st = cudaFuncSetAttribute(leaf_solve_kernel<T, CW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (st == cudaSuccess)
+      st = cudaFuncSetAttribute(leaf_mult_kernel<T, CW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  });
+  return st == cudaSuccess ? NLA_OK : cuda_status(st, "cudaFuncSetAttribute(leaf kernels)");
+}
+
+template <typename T, int CW>
 int launch_leaf_t(char func, const LeafArgs& g, cudaStream_t s) {
   const size_t smem = leaf_smem<T, CW>(func, g.n);
   const int64_t grid = (g.m + CW - 1) / CW;
   if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "leaf: too many right-hand sides");
+  if (smem > 200 * 1024) return fail(NLA_ERR_UNSUPPORTED, "leaf: shared memory plan too large");
+  NLA_TRY((leaf_smem_attr<T, CW>()));
   // n^2 m flops per solve or multiply (the benchmark's convention); bytes:
   // the triangle once plus B read and written.
   TraceScope trace(func == 'S' ? NLA_K_LEAF_SOLVE : NLA_K_LEAF_MULT, s, (double)g.n * g.n * (double)g.m,
                    (double)sizeof(T) * ((double)g.n * (g.n + 1) / 2 + 2.0 * (double)g.n * g.m));
-  if (func == 'S') {
-    static bool configured = false;  // per instantiation; the attribute is per function
-    if (!configured) {
-      cudaFuncSetAttribute(leaf_solve_kernel<T, CW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      configured = true;
-    }
+  if (func == 'S')
     leaf_solve_kernel<T, CW><<<(unsigned)grid, LEAF_THREADS, smem, s>>>(g);
-  } else {
-    static bool configured = false;
-    if (!configured) {
-      cudaFuncSetAttribute(leaf_mult_kernel<T, CW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      configured = true;
-    }
+  else
     leaf_mult_kernel<T, CW><<<(unsigned)grid, LEAF_THREADS, smem, s>>>(g);
-  }
   NLA_CHECK_LAUNCH(func == 'S' ? "leaf_solve_kernel" : "leaf_mult_kernel");
   return NLA_OK;
 }

@@ -43,7 +43,6 @@ constexpr int TILE_BYTES = BM * BK * 2;    // 16 KiB per slice tile (BN == BM)
 constexpr int GEMM_THREADS = 192;
 constexpr int MAX_PAIRS = 16;
 constexpr int MAX_ACC = 4;
-constexpr int SMEM_LIMIT = 232448;         // 227 KiB opt-in per CTA
 constexpr int SENTINEL_EXP = -2139062144;  // 0x80808080: "no element seen"
 constexpr int NONFINITE_EXP = 0x7fffffff;
 
@@ -375,10 +374,19 @@ std::unordered_map<uint64_t, Pool> g_pools;
 
 int64_t pad_to(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
-template <typename F>
-void set_smem_once(F* kernel, int bytes) {
+// Raise the dynamic shared-memory limit of one kernel instantiation (once per
+// process; a single GPU is used).  The limit must leave room for the kernel's
+// static shared memory, so it is set to what the launches actually use.
+constexpr int GEMM_DYN_SMEM = 200 * 1024;
+
+template <int EPI>
+int ensure_gemm_smem() {
   static std::once_flag once;
-  std::call_once(once, [&] { cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes); });
+  static cudaError_t status = cudaSuccess;
+  std::call_once(once, [] {
+    status = cudaFuncSetAttribute(umma_gemm_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_DYN_SMEM);
+  });
+  return status == cudaSuccess ? NLA_OK : cuda_status(status, "cudaFuncSetAttribute(umma_gemm_kernel)");
 }
 
 }  // namespace
@@ -490,7 +498,7 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
   p.sa = S;
   p.sb = S;
   p.stage_bytes = 2 * S * TILE_BYTES;
-  p.stages = (SMEM_LIMIT - 1024 - 256) / p.stage_bytes;
+  p.stages = (GEMM_DYN_SMEM - 1024 - 256) / p.stage_bytes;
   if (p.stages > 6) p.stages = 6;
   // Slice pairs (a, b) with a + b <= S - 1 (0-based), grouped by weight.
   p.npairs = 0;
@@ -523,11 +531,12 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
   const double pair_flops = 2.0 * (double)M * (double)N * (double)K;
   TraceScope trace(NLA_K_GEMM_UMMA, s, pair_flops * p.npairs,
                    (double)S * (Mp + Np) * Kp * 2 + 2.0 * (double)M * N * (double)dtype_size(out_dtype));
+  if (smem > GEMM_DYN_SMEM) return fail(NLA_ERR_UNSUPPORTED, "tensor-core update: shared memory plan too large");
   if (out_dtype == NLA_F64) {
-    set_smem_once(umma_gemm_kernel<EPI_F64>, SMEM_LIMIT);
+    NLA_TRY(ensure_gemm_smem<EPI_F64>());
     umma_gemm_kernel<EPI_F64><<<(unsigned)grid, GEMM_THREADS, smem, s>>>(mA, mB, p);
   } else if (out_dtype == NLA_F16) {
-    set_smem_once(umma_gemm_kernel<EPI_F16>, SMEM_LIMIT);
+    NLA_TRY(ensure_gemm_smem<EPI_F16>());
     umma_gemm_kernel<EPI_F16><<<(unsigned)grid, GEMM_THREADS, smem, s>>>(mA, mB, p);
   } else {
     return fail(NLA_ERR_DTYPE, "tensor-core update: unsupported output type");
