@@ -50,3 +50,43 @@ def reference_test_pair(n: int, m: int, side: str, uplo: str, rng) -> tuple:
 def config0():
     """Plain FP64 TRSM L/L/N: A 1024 x 1024 lower, B 1024 x 256, seed 0."""
     return problem(1024, 256, "L", "L", seed=0)
+
+
+def cond1_lower(A) -> float:
+    """1-norm condition number estimate of a lower-triangular matrix (LAPACK
+    dtrcon through scipy)."""
+    from scipy.linalg import lapack
+
+    rc, info = lapack.dtrcon(A, norm="1", uplo="L", diag="N")
+    if info != 0:
+        raise ValueError("dtrcon failed (info %d)" % info)
+    return float("inf") if rc == 0 else 1.0 / rc
+
+
+def conditioned(n: int, target: float, seed: int = 0, rtol: float = 0.25):
+    """Lower-triangular A with off-diagonals N(0,1)/sqrt(n) and diagonal
+    c * (2 + |N(0,1)|), the scale c chosen by bisection on log(c) so that the
+    dtrcon 1-norm estimate of cond(A) is within a factor 10**rtol of target.
+    Returns (A, c, cond)."""
+    rng = np.random.default_rng(seed)
+    A = np.asfortranarray(np.tril(rng.standard_normal((n, n)) / np.sqrt(max(n, 1)), -1))
+    d = 2.0 + np.abs(rng.standard_normal(n))
+    idx = np.diag_indices(n)
+
+    def cond_at(c):
+        A[idx] = c * d
+        return cond1_lower(A)
+
+    lo, hi = np.log(1e-3), np.log(1e3)  # cond decreases as c grows
+    c = 1.0
+    k = cond_at(c)
+    for _ in range(60):
+        if abs(np.log10(k) - np.log10(target)) <= rtol:
+            break
+        if k > target:
+            lo = np.log(c)
+        else:
+            hi = np.log(c)
+        c = float(np.exp(0.5 * (lo + hi)))
+        k = cond_at(c)
+    return A, c, k

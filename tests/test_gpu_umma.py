@@ -3,8 +3,8 @@
 Float16 plain path: the update must equal the FP32 product of the Float16
 inputs rounded once to Float16 (relative error < 2e-3, i.e. about 2 Float16
 ulps).  Mixed path: the error against an FP64 product must fall with the
-number of slices: BF16 (8-bit slices) 1/2/3 terms < 2e-2 / 1e-4 / 5e-6,
-FP16 (11-bit slices) < 2e-3 / 5e-6 / 5e-6 (FP32 accumulation bounds the last).
+number of slices: BF16 (8-bit slices) 1/2/3 terms < 3e-2 / 3e-4 / 1e-5,
+FP16 (11-bit slices) < 3e-3 / 1e-5 / 1e-5 (FP32 accumulation bounds the last).
 """
 
 import itertools
@@ -49,7 +49,7 @@ def test_mixed_update_error_falls_with_terms(pkg, cuda, lowp):
     import torch
 
     g = torch.Generator(device=cuda).manual_seed(1)
-    bounds = {"bf16": [2e-2, 1e-4, 5e-6], "f16": [2e-3, 5e-6, 5e-6]}[lowp]
+    bounds = {"bf16": [3e-2, 3e-4, 1e-5], "f16": [3e-3, 1e-5, 1e-5]}[lowp]
     for (N, R, M), t1 in itertools.product([(256, 300, 130), (700, 1024, 515)], [False, True]):
         C0 = _col_major(torch.randn(N, M, device=cuda, generator=g, dtype=torch.float64))
         A = torch.randn(R if t1 else N, N if t1 else R, device=cuda, generator=g, dtype=torch.float64)
