@@ -49,7 +49,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--variant", choices=["plain", "mixed"], default="plain")
+    ap.add_argument("--variant", choices=["plain", "mixed"], default="mixed")
+    ap.add_argument("--lowp", choices=["bf16", "f16"], default="bf16")
+    ap.add_argument("--terms", type=int, default=3, help="split terms (1-3, or 7 for exact updates)")
+    ap.add_argument("--sweeps", type=int, default=2)
+    ap.add_argument("--residual", choices=["split", "fp64"], default="split")
+    ap.add_argument("--cutoff", type=int, default=0)
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison step")
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--m", type=int, default=16384)
     ap.add_argument("--cpu-sample", type=int, default=0,
@@ -121,6 +127,20 @@ class ClockSampler:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+# Measured DFMA throughput of a GB300 (FP64 FMA loop on every SM).
+DFMA_PEAK_TFLOPS = 1.20
+
+
+def traffic_per_launch():
+    """DRAM bytes per launch of the dominant tensor-core kernel from the
+    committed ncu summary (profiles/umma_traffic.json), or None."""
+    path = os.path.join(ROOT, "profiles", "umma_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f).get("dram_bytes_per_launch")
 
 
 def make_inputs(n, m, seed=0):
@@ -214,9 +234,24 @@ def main():
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
 
-    def solve(Bd):
-        _lib.check(L.nla_trxm(b"L", b"L", b"N", 1.0, b"S", _lib.NLA_F64, n, m, A.data_ptr(), n, Bd.data_ptr(), n,
+    import ctypes
+
+    opts = _lib.MixedOpts({"bf16": _lib.NLA_LOWP_BF16, "f16": _lib.NLA_LOWP_F16}[args.lowp], args.terms,
+                          args.sweeps, {"split": _lib.NLA_RESIDUAL_SPLIT, "fp64": _lib.NLA_RESIDUAL_FP64}[args.residual],
+                          args.cutoff, None)
+
+    def solve_plain(Ad, Bd):
+        _lib.check(L.nla_trxm(b"L", b"L", b"N", 1.0, b"S", _lib.NLA_F64, n, m, Ad.data_ptr(), n, Bd.data_ptr(), n,
                               sptr))
+
+    def solve_mixed(Ad, Bd):
+        _lib.check(L.nla_trxm_mixed(b"L", b"L", b"N", 1.0, b"S", n, m, Ad.data_ptr(), n, Bd.data_ptr(), n,
+                                    ctypes.byref(opts), sptr))
+
+    solve_fn = solve_mixed if args.variant == "mixed" else solve_plain
+
+    def solve(Bd):
+        solve_fn(A, Bd)
 
     def step():
         B.copy_(B0)
@@ -252,13 +287,37 @@ def main():
     value = world * args.steps * flops / (ms / 1e3) / 1e12
     trace = _lib.trace_summary()
 
-    # Accuracy of the last solution on a sample of columns (FP64 GEMM in torch).
+    # Accuracy of the last solution on a sample of columns: backward error
+    # ||A X - B||_inf / (||A||_inf ||X||_inf n u), residual formed with the
+    # library's FP64-accurate split residual.
     cols = torch.arange(0, m, max(1, m // 64), device=dev)
-    X = B[:, cols]
-    Ad = torch.tril(A)
-    R = Ad @ X - B0[:, cols]
-    berr = float(R.abs().sum(dim=1).max() / (Ad.abs().sum(dim=1).max() * X.abs().sum(dim=1).max() * n * 2.0 ** -53))
-    del Ad, R
+
+    def backward_error(Xfull):
+        Xs_ = Xfull[:, cols].contiguous().T.contiguous().T
+        Bs_ = B0[:, cols].contiguous().T.contiguous().T
+        Rs_ = torch.empty_like(Xs_.T).T
+        pkg.residual_("L", "L", "N", 1.0, A, Xs_, Bs_, Rs_)
+        torch.cuda.synchronize(dev)
+        an = float(torch.tril(A).abs().sum(dim=1).max())
+        return float(Rs_.abs().sum(dim=1).max() / (an * Xs_.abs().sum(dim=1).max() * n * 2.0 ** -53))
+
+    berr = backward_error(B)
+    plain = None
+    if args.variant == "mixed" and not args.no_plain:
+        Bp = torch.empty_like(B0.T).T
+        Bp.copy_(B0)
+        solve_plain(A, Bp)  # warm-up of the plain path's kernels
+        Bp.copy_(B0)
+        barrier()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        solve_plain(A, Bp)
+        p1.record(stream)
+        barrier()
+        pms = p0.elapsed_time(p1)
+        plain = {"tflops": flops / (pms / 1e3) / 1e12, "ms": pms, "backward_error": backward_error(Bp),
+                 "steps": 1}
+        del Bp
 
     # End to end through the C ABI with host buffers.
     A_pin = torch.from_numpy(np.ascontiguousarray(A_h.T)).pin_memory()
@@ -270,8 +329,7 @@ def main():
     def e2e_step():
         Ae.copy_(A_pin, non_blocking=True)
         Be.copy_(B_pin, non_blocking=True)
-        _lib.check(L.nla_trxm(b"L", b"L", b"N", 1.0, b"S", _lib.NLA_F64, n, m, Ae.data_ptr(), n, Be.data_ptr(), n,
-                              sptr))
+        solve_fn(Ae.T, Be.T)
         X_pin.copy_(Be, non_blocking=True)
 
     e2e_steps = max(1, min(args.steps, 3))
@@ -288,13 +346,23 @@ def main():
     pk, pk_kind = peaks()
     dom = max(trace.items(), key=lambda kv: kv[1][1]) if trace else None
     roofline = None
-    gpu_launches = sum(v[0] for v in trace.values()) + 0
+    gpu_launches = sum(v[0] for v in trace.values())
     if dom:
         name, (launches, kms, kflops, kbytes) = dom
         achieved = kflops / (kms / 1e3) / 1e12
-        roofline = {"kernel": name, "bound": "fp64" if name in ("gemm_simt", "leaf_solve") else "tensor",
-                    "achieved": achieved, "peak": None, "unit": "TFLOP/s", "frac": None, "traffic": None,
-                    "launches": launches, "share": kms / sum(v[1] for v in trace.values())}
+        share = kms / sum(v[1] for v in trace.values())
+        if name == "gemm_umma":
+            peak = float(pk.get("bf16_tflops_sustained", pk.get("bf16_tflops")))
+            roofline = {"kernel": "umma_gemm/umma_exact (tcgen05 BF16 slice products)", "bound": "tensor",
+                        "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                        "traffic": traffic_per_launch(), "launches": launches, "share": share,
+                        "peak_source": "bf16_tflops_sustained of %s MEASURED_PEAKS.json" % pk_kind}
+        else:
+            # The plain FP64 path runs on the DFMA pipe; no tensor or HBM peak applies.
+            roofline = {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": DFMA_PEAK_TFLOPS,
+                        "unit": "TFLOP/s", "frac": achieved / DFMA_PEAK_TFLOPS, "traffic": None,
+                        "launches": launches, "share": share,
+                        "peak_source": "DFMA loop measured on GB300 (profiles/fp64_pipe_probe.md)"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -311,8 +379,13 @@ def main():
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
             "config": {"workload": "trsm_LLN_f64_n%d_m%d_%s" % (n, m, args.variant), "n": n, "m": m, "side": "L",
                        "uplo": "L", "trans": "N", "alpha": 1.0, "variant": args.variant,
+                       "mixed": ({"lowp": args.lowp, "split_terms": args.terms, "sweeps": args.sweeps,
+                                  "residual": args.residual, "cutoff": args.cutoff or "default"}
+                                 if args.variant == "mixed" else None),
                        "l2": "inputs larger than L2", "parallelism": "replicas" if world > 1 else "single"},
             "accuracy": {"backward_error": berr, "definition": "||AX-B||_inf/(||A||_inf ||X||_inf n u), 64 cols"},
+            "plain_fp64": plain,
+            "speedup_vs_plain_fp64": (value / plain["tflops"]) if plain else None,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": int(A_h.nbytes + B_h.nbytes),
                     "d2h_bytes_per_step": int(B_h.nbytes)},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": gpu_launches,

@@ -122,18 +122,21 @@ NLA_API int nla_scale(int dtype, int64_t rows, int64_t cols, double alpha, void*
  * BF16 (lowp NLA_LOWP_BF16) or FP16 (NLA_LOWP_F16) slices with one
  * power-of-two scale per row / column, slice products accumulate in FP32, and
  * the diagonal blocks (size `cutoff`, default 128) are solved or multiplied in
- * FP64.  Solves then run `sweeps` refinement sweeps: R = alpha*B - op(A) X in
- * FP64, op(A) D = R with the same mixed solver, X += D.  If corr_out is not
+ * FP64.  Solves then run `sweeps` refinement sweeps: R = alpha*B - op(A) X with
+ * an FP64-accurate residual product (`residual`), op(A) D = R with the same
+ * mixed solver, X += D.  If corr_out is not
  * NULL it receives max|D| / max|X| of each sweep (host array of `sweeps`
  * doubles; the call then synchronises the stream).  Multiplies (func 'M')
  * ignore `sweeps`.  Inputs must be finite.
  */
 #define NLA_LOWP_BF16 0
 #define NLA_LOWP_F16 1
-#define NLA_RESIDUAL_FP64 0 /* residual product on the FP64 pipe */
+#define NLA_RESIDUAL_FP64 0  /* residual product on the FP64 pipe (DFMA) */
+#define NLA_RESIDUAL_SPLIT 1 /* residual product from 7 BF16 slices per operand with
+                                exact FP32 chunk sums and 64-bit integer accumulation */
 typedef struct {
   int lowp;          /* NLA_LOWP_BF16 or NLA_LOWP_F16 */
-  int split_terms;   /* 1, 2 or 3 slices per operand */
+  int split_terms;   /* 1, 2 or 3 slices per operand; 7 = exact BF16 slice products (FP64-accurate updates) */
   int sweeps;        /* refinement sweeps for solves, 0..8 */
   int residual;      /* how the residual product is formed */
   int64_t cutoff;    /* FP64 diagonal block size; <= 0 selects the default */
@@ -147,11 +150,23 @@ NLA_API int nla_trxm_mixed(char side, char uplo, char trans, double alpha, char 
  * One mixed-precision off-diagonal update (no counterpart in the reference;
  * the mixed form of matmul!, src/matmul.jl:5-66): out (N x M, FP64) +=
  * alpha * op(in1) (N x R) * op(in2) (R x M) from `split_terms` BF16/FP16
- * slices per operand on the tensor cores.
+ * slices per operand on the tensor cores (1-3: FP32 accumulation; 7: BF16
+ * only, exact slice products accumulated in 64-bit integers, FP64-accurate).
  */
 NLA_API int nla_gemm_update_mixed(int trans1, int trans2, int64_t N, int64_t R, int64_t M, double alpha,
                                   const double* in1, int64_t ld1, const double* in2, int64_t ld2, double* out,
                                   int64_t ldo, int lowp, int split_terms, void* stream);
+
+/*
+ * The residual of a solve, FP64-accurate (no counterpart in the reference):
+ * R = alpha*B - op(A) X (side 'L') or alpha*B - X op(A) (side 'R'), with A
+ * n x n triangular (uplo, trans as for nla_trxm) and X, B, R of B's shape.
+ * `residual` selects NLA_RESIDUAL_SPLIT (tensor cores, exact slice products)
+ * or NLA_RESIDUAL_FP64 (FP64 pipe).  R must not overlap X or B.
+ */
+NLA_API int nla_trxm_residual(char side, char uplo, char trans, double alpha, int64_t n, int64_t m, const double* A,
+                              int64_t lda, const double* X, int64_t ldx, const double* B, int64_t ldb, double* R,
+                              int64_t ldr, int residual, void* stream);
 
 /*
  * Synchronises `stream` and reports (then clears) the device-side error word

@@ -40,7 +40,7 @@ SIGNATURES = {
 }
 
 NLA_LOWP_BF16, NLA_LOWP_F16 = 0, 1
-NLA_RESIDUAL_FP64 = 0
+NLA_RESIDUAL_FP64, NLA_RESIDUAL_SPLIT = 0, 1
 
 
 class MixedOpts(ctypes.Structure):
@@ -55,6 +55,7 @@ SIGNATURES.update({
     "nla_gemm_update_mixed": ([_i32, _i32, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _p, _i64, _i32, _i32, _p],
                               _i32),
     "nla_device_status": ([_p], _i32),
+    "nla_trxm_residual": ([_c, _c, _c, _d, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _i32, _p], _i32),
 })
 
 KERNEL_CLASSES = ["leaf_solve", "leaf_mult", "gemm_simt", "gemm_umma", "split", "scale", "residual", "batched"]

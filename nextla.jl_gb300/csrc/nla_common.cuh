@@ -124,6 +124,28 @@ int launch_scale(int dtype, int64_t rows, int64_t cols, double alpha, const Mat&
 int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat& A, const Mat& B, const Mat& C,
                        int in_dtype, int out_dtype, int S, bool bf16, void* ws, size_t ws_bytes, cudaStream_t s);
 size_t sliced_workspace_bytes(int64_t M, int64_t N, int64_t K, int S);
+
+// An operand staged for the tensor cores: S K-major 16-bit slices of a
+// rows x K view (padded to rows_pad x K_pad) and one exponent per row.
+struct Staged {
+  void* slices;
+  int* e;
+  float* nrm;  // per row: sum over k and slices of |s_p| 2^(-beta p)
+  int64_t rows, rows_pad, K, K_pad;
+  int S;
+  bool bf16;
+  bool scaled;
+  int tri;  // 0 full, 1 k <= row, 2 k >= row, 3 k < row, 4 k > row
+};
+size_t staged_bytes(int64_t rows, int64_t K, int S);
+int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bool bf16, int tri, void* buf,
+                  Staged* out, cudaStream_t s);
+// C (M x N, FP64) += alpha * A * B^T with exact slice-pair accumulation; both
+// operands staged with 7 BF16 slices.  With trans_out the product is added
+// to C^T (C is N x M).
+int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat& C, bool trans_out,
+                      cudaStream_t s);
+constexpr int EXACT_SLICES = 7;
 int workspace_get(cudaStream_t s, size_t bytes, void** out);
 int device_status(cudaStream_t s);
 

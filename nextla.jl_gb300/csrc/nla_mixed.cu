@@ -93,6 +93,19 @@ __global__ void correct_kernel(int64_t rows, int64_t cols, const double* __restr
   }
 }
 
+// R -= diag(A) X (side L) or X diag(A) (side R), in FP64.
+__global__ void diag_residual_kernel(int64_t rows, int64_t cols, const double* __restrict__ A, int64_t lda,
+                                     int left, const double* __restrict__ X, int64_t ldx, double* __restrict__ R,
+                                     int64_t ldr) {
+  const int64_t total = rows * cols;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % rows, j = idx / rows;
+    const double d = left ? A[i + i * lda] : A[j + j * lda];
+    R[i + j * ldr] = fma(-d, X[i + j * ldx], R[i + j * ldr]);
+  }
+}
+
 unsigned grid_for(int64_t total) {
   int64_t blocks = (total + 255) / 256;
   const int64_t cap = (int64_t)num_sms() * 8;
@@ -110,6 +123,33 @@ int default_mixed_cutoff() {
 
 }  // namespace
 
+// Stage the strict triangle of op(A) as the row operand of the residual
+// product: op(A) itself for side L, op(A)^T for side R.
+int stage_triangle(const Mat& Am, int64_t n, char side, char uplo, void* buf, Staged* out, cudaStream_t s) {
+  if (side == 'L') return stage_operand(Am, n, n, NLA_F64, EXACT_SLICES, true, uplo == 'L' ? 3 : 4, buf, out, s);
+  return stage_operand(transposed(Am), n, n, NLA_F64, EXACT_SLICES, true, uplo == 'L' ? 4 : 3, buf, out, s);
+}
+
+// R -= op(A) X (side L) or X op(A) (side R) with exact slice products for the
+// strict triangle (As, staged by stage_triangle) and FP64 for the diagonal.
+int split_residual(const Mat& Am, const Staged& As, char side, int64_t n, int64_t m, const Mat& Xm, const Mat& Rm,
+                   void* xbuf, Staged* Xs, unsigned grid, cudaStream_t s) {
+  const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
+  if (side == 'L') {  // op(A) (n x n) times X (n x m): B-operand rows are X's columns
+    NLA_TRY(stage_operand(transposed(Xm), m, n, NLA_F64, EXACT_SLICES, true, 0, xbuf, Xs, s));
+    NLA_TRY(launch_exact_gemm(As, *Xs, -1.0, Rm, false, s));
+  } else {  // (X op(A))^T = op(A)^T X^T: B-operand rows are X's rows; written transposed
+    NLA_TRY(stage_operand(Xm, m, n, NLA_F64, EXACT_SLICES, true, 0, xbuf, Xs, s));
+    NLA_TRY(launch_exact_gemm(As, *Xs, -1.0, Rm, true, s));
+  }
+  TraceScope t(NLA_K_RESIDUAL, s, 2.0 * (double)rows * cols, 24.0 * (double)rows * cols);
+  diag_residual_kernel<<<grid, 256, 0, s>>>(rows, cols, static_cast<const double*>(Am.p), Am.ld, side == 'L',
+                                            static_cast<const double*>(Xm.p), Xm.ld, static_cast<double*>(Rm.p),
+                                            Rm.ld);
+  NLA_CHECK_LAUNCH("diag_residual_kernel");
+  return NLA_OK;
+}
+
 int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, int64_t n, int64_t m,
                     const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* o,
                     cudaStream_t s) {
@@ -118,12 +158,16 @@ int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, i
   NLA_TRY(check_matrix("A", A, n, n, lda));
   const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
   NLA_TRY(check_matrix("B", B, rows, cols, ldb));
-  nla_mixed_opts opts{NLA_LOWP_BF16, 3, 2, NLA_RESIDUAL_FP64, 0, nullptr};
+  nla_mixed_opts opts{NLA_LOWP_BF16, 3, 2, NLA_RESIDUAL_SPLIT, 0, nullptr};
   if (o) opts = *o;
   if (opts.lowp != NLA_LOWP_BF16 && opts.lowp != NLA_LOWP_F16) return fail(NLA_ERR_ARG, "lowp must be BF16 or F16");
-  if (opts.split_terms < 1 || opts.split_terms > 3) return fail(NLA_ERR_ARG, "split_terms must be 1, 2 or 3");
+  if (!(opts.split_terms >= 1 && opts.split_terms <= 3) && opts.split_terms != EXACT_SLICES)
+    return fail(NLA_ERR_ARG, "split_terms must be 1, 2, 3 or 7");
+  if (opts.split_terms == EXACT_SLICES && opts.lowp != NLA_LOWP_BF16)
+    return fail(NLA_ERR_ARG, "exact (7-term) updates use BF16 slices");
   if (opts.sweeps < 0 || opts.sweeps > 8) return fail(NLA_ERR_ARG, "sweeps must be in 0..8");
-  if (opts.residual != NLA_RESIDUAL_FP64) return fail(NLA_ERR_ARG, "unknown residual mode");
+  if (opts.residual != NLA_RESIDUAL_FP64 && opts.residual != NLA_RESIDUAL_SPLIT)
+    return fail(NLA_ERR_ARG, "unknown residual mode");
   if (n == 0 || m == 0) return NLA_OK;
 
   Mat Am{const_cast<double*>(A), lda, 0};
@@ -152,14 +196,19 @@ int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, i
   NLA_TRY(launch_scale(NLA_F64, rows, cols, alpha, Bm, s));  // src/rectrxm.jl:64
   if (opts.sweeps == 0) return recurse(mixed, Am, n, Bm);
 
-  // Refinement needs alpha*B (B0), a residual/correction buffer (R) and two
-  // device words for the correction norms.
+  // Refinement needs alpha*B (B0), a residual/correction buffer (R), two
+  // device words for the correction norms and, for the split residual, op(A)
+  // staged once (it does not change between sweeps) and X staged per sweep.
   const size_t elems = (size_t)rows * (size_t)cols;
+  const bool split = opts.residual == NLA_RESIDUAL_SPLIT;
+  const size_t a_stage = split ? staged_bytes(n, n, EXACT_SLICES) : 0;
+  const size_t x_stage = split ? staged_bytes(m, n, EXACT_SLICES) : 0;
   void* buf = nullptr;
-  NLA_TRY(refine_buffers(s, 2 * elems * sizeof(double) + 256, &buf));
+  NLA_TRY(refine_buffers(s, 2 * elems * sizeof(double) + 2048 + a_stage + x_stage, &buf));
   double* B0 = static_cast<double*>(buf);
   double* R = B0 + elems;
   unsigned long long* amax = reinterpret_cast<unsigned long long*>(R + elems);
+  uint8_t* stage_base = reinterpret_cast<uint8_t*>(buf) + ((2 * elems * sizeof(double) + 256 + 1023) & ~(size_t)1023);
   const unsigned grid = grid_for((int64_t)elems);
   {
     TraceScope t(NLA_K_RESIDUAL, s, 0.0, 16.0 * (double)elems);
@@ -168,19 +217,34 @@ int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, i
   }
   NLA_TRY(recurse(mixed, Am, n, Bm));  // X0
 
+  // op(A) as the left operand (side L: op(A) X) or the right one (side R:
+  // X op(A), staged as op(A)^T); only its triangle is staged.
+  // The strict triangle is staged (its rows then carry no diagonal, whose
+  // size would coarsen the row scale); the diagonal term is applied in FP64.
+  Staged As{}, Xs{};
+  if (split) NLA_TRY(stage_triangle(Am, n, side, uplo, stage_base, &As, s));
   RecPlan resid{'M', side, uplo, NLA_F64, m, 128, s, GEMM_PLAIN, 1, false};
   Mat Rm{R, rows, 0};
   for (int k = 0; k < opts.sweeps; ++k) {
-    {
-      TraceScope t(NLA_K_RESIDUAL, s, 0.0, 16.0 * (double)elems);
-      copy_kernel<<<grid, 256, 0, s>>>(rows, cols, B, ldb, R, rows);
-      NLA_CHECK_LAUNCH("copy_kernel");
-    }
-    NLA_TRY(recurse(resid, Am, n, Rm));  // R = op(A) X (or X op(A))
-    {
-      TraceScope t(NLA_K_RESIDUAL, s, (double)elems, 24.0 * (double)elems);
-      residual_kernel<<<grid, 256, 0, s>>>(rows, cols, B0, rows, R, rows);
-      NLA_CHECK_LAUNCH("residual_kernel");
+    if (split) {
+      {
+        TraceScope t(NLA_K_RESIDUAL, s, 0.0, 16.0 * (double)elems);
+        copy_kernel<<<grid, 256, 0, s>>>(rows, cols, B0, rows, R, rows);
+        NLA_CHECK_LAUNCH("copy_kernel");
+      }
+      NLA_TRY(split_residual(Am, As, side, n, m, Bm, Rm, stage_base + a_stage, &Xs, grid, s));
+    } else {
+      {
+        TraceScope t(NLA_K_RESIDUAL, s, 0.0, 16.0 * (double)elems);
+        copy_kernel<<<grid, 256, 0, s>>>(rows, cols, B, ldb, R, rows);
+        NLA_CHECK_LAUNCH("copy_kernel");
+      }
+      NLA_TRY(recurse(resid, Am, n, Rm));  // R = op(A) X (or X op(A)) on the FP64 pipe
+      {
+        TraceScope t(NLA_K_RESIDUAL, s, (double)elems, 24.0 * (double)elems);
+        residual_kernel<<<grid, 256, 0, s>>>(rows, cols, B0, rows, R, rows);
+        NLA_CHECK_LAUNCH("residual_kernel");
+      }
     }
     NLA_TRY(recurse(mixed, Am, n, Rm));  // D
     {
@@ -198,6 +262,55 @@ int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, i
       opts.corr_out[k] = mx > 0 ? md / mx : md;
     }
   }
+  return NLA_OK;
+}
+
+// R = alpha*B - op(A) X (side L) or alpha*B - X op(A) (side R), FP64-accurate.
+int residual_impl(char side, char uplo, char trans, double alpha, int64_t n, int64_t m, const double* A, int64_t lda,
+                  const double* X, int64_t ldx, const double* B, int64_t ldb, double* R, int64_t ldr, int mode,
+                  cudaStream_t s) {
+  NLA_TRY(check_flags(side, uplo, trans, 'M', NLA_F64));
+  if (n < 0 || m < 0) return fail(NLA_ERR_ARG, "n and m must be non-negative");
+  const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
+  NLA_TRY(check_matrix("A", A, n, n, lda));
+  NLA_TRY(check_matrix("X", X, rows, cols, ldx));
+  NLA_TRY(check_matrix("B", B, rows, cols, ldb));
+  NLA_TRY(check_matrix("R", R, rows, cols, ldr));
+  if (mode != NLA_RESIDUAL_FP64 && mode != NLA_RESIDUAL_SPLIT) return fail(NLA_ERR_ARG, "unknown residual mode");
+  if (rows == 0 || cols == 0) return NLA_OK;
+  Mat Am{const_cast<double*>(A), lda, 0};
+  if (trans == 'T' || trans == 'C') {
+    Am.t = 1;
+    uplo = uplo == 'L' ? 'U' : 'L';
+  }
+  const Mat Xm{const_cast<double*>(X), ldx, 0}, Rm{R, ldr, 0};
+  const size_t elems = (size_t)rows * (size_t)cols;
+  const unsigned grid = grid_for((int64_t)elems);
+  if (mode == NLA_RESIDUAL_SPLIT) {
+    const size_t a_stage = staged_bytes(n, n, EXACT_SLICES), x_stage = staged_bytes(m, n, EXACT_SLICES);
+    void* buf = nullptr;
+    NLA_TRY(refine_buffers(s, a_stage + x_stage + 1024, &buf));
+    uint8_t* base = static_cast<uint8_t*>(buf);
+    copy_kernel<<<grid, 256, 0, s>>>(rows, cols, B, ldb, R, ldr);
+    NLA_CHECK_LAUNCH("copy_kernel");
+    NLA_TRY(launch_scale(NLA_F64, rows, cols, alpha, Rm, s));
+    Staged As{}, Xs{};
+    NLA_TRY(stage_triangle(Am, n, side, uplo, base, &As, s));
+    return split_residual(Am, As, side, n, m, Xm, Rm, base + a_stage, &Xs, grid, s);
+  }
+  // FP64 pipe: R = op(A) X by the plain recursion, then R = alpha*B - R.
+  void* buf = nullptr;
+  NLA_TRY(refine_buffers(s, elems * sizeof(double), &buf));
+  double* B0 = static_cast<double*>(buf);
+  copy_kernel<<<grid, 256, 0, s>>>(rows, cols, B, ldb, B0, rows);
+  copy_kernel<<<grid, 256, 0, s>>>(rows, cols, X, ldx, R, ldr);
+  NLA_CHECK_LAUNCH("copy_kernel");
+  const Mat B0m{B0, rows, 0};
+  NLA_TRY(launch_scale(NLA_F64, rows, cols, alpha, B0m, s));
+  RecPlan resid{'M', side, uplo, NLA_F64, m, 128, s, GEMM_PLAIN, 1, false};
+  NLA_TRY(recurse(resid, Am, n, Rm));
+  residual_kernel<<<grid, 256, 0, s>>>(rows, cols, B0, rows, R, ldr);
+  NLA_CHECK_LAUNCH("residual_kernel");
   return NLA_OK;
 }
 
@@ -219,7 +332,8 @@ int nla_gemm_update_mixed(int trans1, int trans2, int64_t N, int64_t R, int64_t 
   clear_error();
   if (N < 0 || R < 0 || M < 0) return fail(NLA_ERR_ARG, "N, R and M must be non-negative");
   if (lowp != NLA_LOWP_BF16 && lowp != NLA_LOWP_F16) return fail(NLA_ERR_ARG, "lowp must be BF16 or F16");
-  if (split_terms < 1 || split_terms > 3) return fail(NLA_ERR_ARG, "split_terms must be 1, 2 or 3");
+  if (!(split_terms >= 1 && split_terms <= 3) && split_terms != EXACT_SLICES)
+    return fail(NLA_ERR_ARG, "split_terms must be 1, 2, 3 or 7");
   NLA_TRY(check_matrix("in1", in1, trans1 ? R : N, trans1 ? N : R, ld1));
   NLA_TRY(check_matrix("in2", in2, trans2 ? M : R, trans2 ? R : M, ld2));
   NLA_TRY(check_matrix("out", out, N, M, ldo));
@@ -228,6 +342,14 @@ int nla_gemm_update_mixed(int trans1, int trans2, int64_t N, int64_t R, int64_t 
   Mat C{out, ldo, 0};
   return launch_sliced_gemm(N, M, R, alpha, A, B, C, NLA_F64, NLA_F64, split_terms, lowp == NLA_LOWP_BF16, nullptr,
                             0, (cudaStream_t)stream);
+}
+
+int nla_trxm_residual(char side, char uplo, char trans, double alpha, int64_t n, int64_t m, const double* A,
+                      int64_t lda, const double* X, int64_t ldx, const double* B, int64_t ldb, double* R,
+                      int64_t ldr, int residual, void* stream) {
+  clear_error();
+  return residual_impl(side, uplo, trans, alpha, n, m, A, lda, X, ldx, B, ldb, R, ldr, residual,
+                       (cudaStream_t)stream);
 }
 
 int nla_device_status(void* stream) {

@@ -234,6 +234,237 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
+// Exact-accumulation update (the FP64 residual of refinement).
+//
+// Operands are staged as S = 7 BF16 slices of integers |s| <= 128, so one
+// slice pair's products are exact and their FP32 sum over a chunk of <= 1024
+// values (|sum| <= 2^24) is exact in TMEM.  Each pair runs through the K range
+// in such chunks into one of two TMEM buffers (double-buffered); eight
+// epilogue warps drain each chunk, convert it to integers and add it, shifted
+// by the pair's weight 2^(-8(p+q)), into 64-bit fixed-point accumulators held
+// in registers.  FP64 arithmetic is used once per output element, for the
+// final C += alpha * 2^e * acc.  A tile's K range is clipped to where both
+// operands can be non-zero, so a triangular operand (staged with zeros
+// outside its triangle) costs only its triangle.
+// ---------------------------------------------------------------------------
+
+constexpr int EX_THREADS = 320;  // producer, MMA, 8 epilogue warps
+constexpr int EX_CHUNK = 16;     // k-blocks per exact chunk (1024 values)
+constexpr int EX_SLICES = 7;
+constexpr int EX_MAX_PAIRS = 28;
+constexpr int EX_STAGES = 6;
+constexpr int EX_STAGE_BYTES = 2 * TILE_BYTES;
+constexpr int EX_DYN_SMEM = EX_STAGES * EX_STAGE_BYTES + 1024 + 256;
+
+struct ExactParams {
+  int M, N, K;
+  int tiles_m, tiles_n;
+  int a_rows, b_rows;
+  int npairs;
+  int8_t pa[EX_MAX_PAIRS], pb[EX_MAX_PAIRS];
+  int tri_a, tri_b;  // staged triangle of each operand (see in_tri)
+  int trans_out;     // write the product transposed: element (i, j) to C[j + i*ldc]
+  const float* nrm_a;  // per-row slice-magnitude sums of A (headroom of the fixed point)
+  void* C;
+  int64_t ldc;
+  double alpha;
+  const int* ea;
+  const int* eb;
+};
+
+__device__ __forceinline__ void tri_k_range(int tri, int r0, int K, int& lo, int& hi) {
+  lo = 0;
+  hi = K - 1;
+  if (tri == 1 || tri == 3) hi = min(K - 1, r0 + BM - 1);
+  else if (tri == 2 || tri == 4) lo = r0;
+}
+
+__device__ __forceinline__ double scale_pow2(double d, int e) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int E = (int)((b >> 52) & 0x7FF);
+  const int ne = E + e;
+  if (E == 0 || E == 0x7FF || ne <= 0 || ne >= 2047) return ldexp(d, e);
+  return __longlong_as_double((long long)((b & ~(0x7FFull << 52)) | ((unsigned long long)ne << 52)));
+}
+
+__global__ void __launch_bounds__(EX_THREADS, 1)
+    umma_exact_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      const ExactParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + EX_STAGES * EX_STAGE_BYTES);
+  uint64_t* empty = full + EX_STAGES;
+  uint64_t* cfull = empty + EX_STAGES;
+  uint64_t* cempty = cfull + 2;
+  uint64_t* drain = cempty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  __shared__ volatile int s_abort;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int group = 8;
+  const int per_group = group * p.tiles_n;
+  const int g = blockIdx.x / per_group;
+  const int first_m = g * group;
+  const int gsize = min(p.tiles_m - first_m, group);
+  const int local = blockIdx.x % per_group;
+  const int m0 = (first_m + local % gsize) * BM, n0 = (local / gsize) * BN;
+
+  int alo, ahi, blo, bhi;
+  tri_k_range(p.tri_a, m0, p.K, alo, ahi);
+  tri_k_range(p.tri_b, n0, p.K, blo, bhi);
+  const int klo = max(alo, blo), khi = min(ahi, bhi);
+  const int kb0 = klo / BK;
+  const int kb1 = khi >= klo ? khi / BK + 1 : kb0;  // empty range when the triangles miss each other
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int s = 0; s < EX_STAGES; ++s) {
+      umma::mbar_init(umma::smem_u32(&full[s]), 1);
+      umma::mbar_init(umma::smem_u32(&empty[s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      umma::mbar_init(umma::smem_u32(&cfull[b]), 1);
+      umma::mbar_init(umma::smem_u32(&cempty[b]), 8);
+    }
+    umma::mbar_init(umma::smem_u32(drain), 1);
+    umma::fence_barrier_init();
+  }
+  if (warp == 1) umma::tmem_alloc(umma::smem_u32(tmem_slot), 256);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  bool ok = true;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int it = 0;
+      for (int pr = 0; pr < p.npairs && ok; ++pr) {
+        for (int kb = kb0; kb < kb1; ++kb, ++it) {
+          const int s = it % EX_STAGES;
+          const uint32_t round = (uint32_t)(it / EX_STAGES);
+          if (!umma::mbar_wait(umma::smem_u32(&empty[s]), (round & 1u) ^ 1u, &s_abort, &g_device_error, 11)) {
+            ok = false;
+            break;
+          }
+          const uint32_t fb = umma::smem_u32(&full[s]);
+          umma::mbar_arrive_expect_tx(fb, (uint32_t)EX_STAGE_BYTES);
+          uint8_t* st = smem + s * EX_STAGE_BYTES;
+          umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, p.pa[pr] * p.a_rows + m0);
+          umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), &tmB, fb, kb * BK, p.pb[pr] * p.b_rows + n0);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = umma::idesc_f16(BM, BN, true);
+      int it = 0, ch = 0;
+      for (int pr = 0; pr < p.npairs && ok; ++pr) {
+        for (int c0 = kb0; c0 < kb1 && ok; c0 += EX_CHUNK, ++ch) {
+          const int b = ch & 1;
+          const uint32_t use = (uint32_t)(ch >> 1);
+          if (!umma::mbar_wait(umma::smem_u32(&cempty[b]), (use & 1u) ^ 1u, &s_abort, &g_device_error, 12)) {
+            ok = false;
+            break;
+          }
+          umma::fence_after_sync();
+          const int c1 = min(c0 + EX_CHUNK, kb1);
+          for (int kb = c0; kb < c1; ++kb, ++it) {
+            const int s = it % EX_STAGES;
+            const uint32_t round = (uint32_t)(it / EX_STAGES);
+            if (!umma::mbar_wait(umma::smem_u32(&full[s]), round & 1u, &s_abort, &g_device_error, 13)) {
+              ok = false;
+              break;
+            }
+            umma::fence_after_sync();
+            const uint32_t a0 = umma::smem_u32(smem + s * EX_STAGE_BYTES);
+            const uint32_t b0 = a0 + TILE_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk)
+              umma::mma_f16(tmem + (uint32_t)(b * BN), umma::desc_kmajor_sw128(a0 + kk * 32),
+                            umma::desc_kmajor_sw128(b0 + kk * 32), idesc, (kb > c0 || kk > 0) ? 1u : 0u);
+            umma::mma_commit(umma::smem_u32(&empty[s]));
+          }
+          if (ok) umma::mma_commit(umma::smem_u32(&cfull[b]));
+        }
+      }
+      umma::mma_commit(umma::smem_u32(drain));
+      umma::mbar_wait(umma::smem_u32(drain), 0, &s_abort, &g_device_error, 14, false);
+    }
+  } else {
+    const int q = warp & 3;
+    const int h = (warp - 2) >> 2;  // column half: 0 or 1
+    const int row = q * 32 + lane;
+    const int i = m0 + row;
+    long long acc[64];
+#pragma unroll
+    for (int j = 0; j < 64; ++j) acc[j] = 0;
+    // Fixed point of this row: LSB 2^-Lb in units of 2^(ea+eb).  Every
+    // partial sum is bounded by nrm_a[i] * (1/2 + 2^-8), so Lb keeps it
+    // below 2^61 while giving short or small rows the finest resolution.
+    int Lb = 60;
+    if (i < p.M) {
+      const float bound = p.nrm_a[i] * (0.5f + 0.00390625f) * 1.001f;
+      if (bound > 0.0f) Lb = 61 - (int)ceilf(log2f(bound));
+      Lb = min(max(Lb, 0), 77);
+    }
+    int ch = 0;
+    for (int pr = 0; pr < p.npairs && ok; ++pr) {
+      const int sh = Lb - 8 * (p.pa[pr] + p.pb[pr] + 2);
+      for (int c0 = kb0; c0 < kb1; c0 += EX_CHUNK, ++ch) {
+        const int b = ch & 1;
+        const uint32_t use = (uint32_t)(ch >> 1);
+        ok = __all_sync(0xffffffffu,
+                        umma::mbar_wait(umma::smem_u32(&cfull[b]), use & 1u, &s_abort, &g_device_error, 15));
+        if (!ok) break;
+        umma::fence_after_sync();
+        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + h * 64);
+#pragma unroll
+        for (int j0 = 0; j0 < 64; j0 += 16) {
+          uint32_t r[16];
+          umma::tmem_ld16(ta + (uint32_t)j0, r);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const long long v = (long long)__float2int_rn(__uint_as_float(r[j]));
+            acc[j0 + j] += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
+          }
+        }
+        umma::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) umma::mbar_arrive(umma::smem_u32(&cempty[b]));
+      }
+    }
+    if (ok && i < p.M) {
+      int ei = p.ea[i];
+      const bool row_nan = ei == NONFINITE_EXP;
+      ei = max(ei, -4000);
+#pragma unroll
+      for (int j = 0; j < 64; ++j) {
+        const int col = n0 + h * 64 + j;
+        if (col >= p.N) continue;
+        double* cp = static_cast<double*>(p.C) +
+                     (p.trans_out ? (int64_t)col + (int64_t)i * p.ldc : (int64_t)i + (int64_t)col * p.ldc);
+        const int ej = p.eb[col];
+        if (row_nan || ej == NONFINITE_EXP) {
+          *cp = __longlong_as_double(0x7ff8000000000000ull);
+        } else {
+          const double d = scale_pow2(__ll2double_rn(acc[j]), ei + max(ej, -4000) - Lb);
+          *cp = fma(p.alpha, d, *cp);
+        }
+      }
+    }
+  }
+
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    umma::fence_after_sync();
+    umma::tmem_dealloc(tmem, 256);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Staging kernels.
 // ---------------------------------------------------------------------------
 
@@ -252,11 +483,23 @@ __device__ __forceinline__ int exp_of(double x) {
   return biased - 1022 + 1;
 }
 
+// Whether (i, k) lies in the staged part: everything (tri 0), k <= i (1),
+// k >= i (2), k < i (3) or k > i (4).
+__device__ __forceinline__ bool in_tri(int tri, int64_t i, int64_t k) {
+  switch (tri) {
+    case 1: return k <= i;
+    case 2: return k >= i;
+    case 3: return k < i;
+    case 4: return k > i;
+    default: return true;
+  }
+}
+
 // Per-row maximum exponent of a rows x cols view (op(X) = X or X^T), one
 // 64 x 64 tile per CTA, reduced into e[] with atomicMax.
 template <typename T>
 __global__ void __launch_bounds__(256) row_exp_kernel(const T* __restrict__ X, int64_t ld, int t, int64_t rows,
-                                                      int64_t cols, int* __restrict__ e) {
+                                                      int64_t cols, int tri, int* __restrict__ e) {
   __shared__ int se[64];
   if (threadIdx.x < 64) se[threadIdx.x] = SENTINEL_EXP;
   __syncthreads();
@@ -265,7 +508,7 @@ __global__ void __launch_bounds__(256) row_exp_kernel(const T* __restrict__ X, i
     int i, k;
     if (!t) { i = idx & 63; k = idx >> 6; } else { k = idx & 63; i = idx >> 6; }
     const int64_t gi = i0 + i, gk = k0 + k;
-    if (gi < rows && gk < cols) {
+    if (gi < rows && gk < cols && in_tri(tri, gi, gk)) {
       const int ex = exp_of(to_double(X[mat_off(gi, gk, ld, t)]));
       if (ex != SENTINEL_EXP) atomicMax(&se[i], ex);
     }
@@ -282,21 +525,25 @@ template <> __device__ __forceinline__ __nv_bfloat16 from_int<__nv_bfloat16>(int
 template <> __device__ __forceinline__ __half from_int<__half>(int v) { return __float2half_rn((float)v); }
 
 // Split a rows x cols view into `ns` K-major slices of type Sl (rows padded
-// to rows_pad, K padded to cols_pad, zeros in the padding).  With copy set,
-// the single slice is the element itself (a Float16 operand of the plain
-// path); otherwise slices are the integers s_p of
-//   x = 2^e[row] * sum_p s_p 2^(-beta p).
+// to rows_pad, K padded to cols_pad, zeros in the padding and outside the
+// staged triangle).  With copy set, the single slice is the element itself
+// (a Float16 operand of the plain path); otherwise slices are the integers
+// s_p of  x = 2^e[row] * sum_p s_p 2^(-beta p).
+// When nrm is not null, nrm[row] accumulates sum_k sum_p |s_p| 2^(-beta p),
+// which bounds every partial sum of slice products along that row (in units
+// of the row's scale 2^e) for a partner whose elements are below 1/2.
 template <typename T, typename Sl>
 __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int64_t ld, int t, int64_t rows,
-                                                    int64_t cols, const int* __restrict__ e, Sl* __restrict__ out,
-                                                    int64_t rows_pad, int64_t cols_pad, int ns, int beta, int copy) {
+                                                    int64_t cols, int tri, const int* __restrict__ e,
+                                                    Sl* __restrict__ out, int64_t rows_pad, int64_t cols_pad,
+                                                    int ns, int beta, int copy, float* __restrict__ nrm) {
   __shared__ double tile[32][65];
   const int64_t i0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 64;
   for (int idx = threadIdx.x; idx < 32 * 64; idx += 256) {
     int i, k;
     if (!t) { i = idx & 31; k = idx >> 5; } else { k = idx & 63; i = idx >> 6; }
     const int64_t gi = i0 + i, gk = k0 + k;
-    tile[i][k] = (gi < rows && gk < cols) ? to_double(X[mat_off(gi, gk, ld, t)]) : 0.0;
+    tile[i][k] = (gi < rows && gk < cols && in_tri(tri, gi, gk)) ? to_double(X[mat_off(gi, gk, ld, t)]) : 0.0;
   }
   __syncthreads();
   const int64_t slice_elems = rows_pad * cols_pad;
@@ -322,11 +569,18 @@ __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int
       else if (sh > -63) Y = (long long)((m + (1ull << (-sh - 1))) >> (-sh));
       if (b >> 63) Y = -Y;
     }
+    float mag = 0.0f;
     for (int sl = 0; sl < ns; ++sl) {
       const int shift = 62 - beta * (sl + 1);
       const long long sp = (Y + (1ll << (shift - 1))) >> shift;
       Y -= sp << shift;
       out[(int64_t)sl * slice_elems + o] = from_int<Sl>((int)sp);
+      mag += fabsf((float)sp) * exp2f((float)(-beta * (sl + 1)));
+    }
+    if (nrm) {
+      // 32 consecutive k of one row per warp (idx >> 6 is warp-uniform).
+      for (int off = 16; off > 0; off >>= 1) mag += __shfl_xor_sync(0xffffffffu, mag, off);
+      if ((threadIdx.x & 31) == 0 && gi < rows && mag > 0.0f) atomicAdd(&nrm[gi], mag);
     }
   }
 }
@@ -389,6 +643,15 @@ int ensure_gemm_smem() {
   return status == cudaSuccess ? NLA_OK : cuda_status(status, "cudaFuncSetAttribute(umma_gemm_kernel)");
 }
 
+int ensure_exact_smem() {
+  static std::once_flag once;
+  static cudaError_t status = cudaSuccess;
+  std::call_once(once, [] {
+    status = cudaFuncSetAttribute(umma_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, EX_DYN_SMEM);
+  });
+  return status == cudaSuccess ? NLA_OK : cuda_status(status, "cudaFuncSetAttribute(umma_exact_kernel)");
+}
+
 }  // namespace
 
 int workspace_get(cudaStream_t s, size_t bytes, void** out) {
@@ -413,24 +676,89 @@ int workspace_get(cudaStream_t s, size_t bytes, void** out) {
   return NLA_OK;
 }
 
-size_t sliced_workspace_bytes(int64_t M, int64_t N, int64_t K, int S) {
-  const int64_t Mp = pad_to(M, BM), Np = pad_to(N, BN), Kp = pad_to(K, BK);
-  size_t b = (size_t)S * (size_t)(Mp + Np) * (size_t)Kp * 2;
+size_t staged_bytes(int64_t rows, int64_t K, int S) {
+  const int64_t Rp = pad_to(rows, BM), Kp = pad_to(K, BK);
+  size_t b = (size_t)S * (size_t)Rp * (size_t)Kp * 2;
   b = (b + 1023) & ~(size_t)1023;
-  b += (size_t)(Mp + Np) * sizeof(int) + 1024;
+  b += ((size_t)Rp * sizeof(int) + 1023) & ~(size_t)1023;
+  b += ((size_t)Rp * sizeof(float) + 1023) & ~(size_t)1023;
   return b;
+}
+
+int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bool bf16, int tri, void* buf,
+                  Staged* out, cudaStream_t s) {
+  const bool copy = in_dtype == NLA_F16;
+  const int beta = bf16 ? 8 : 11;
+  if (copy) S = 1;
+  if (S < 1 || 62 - beta * S < 1) return fail(NLA_ERR_ARG, "too many slices for the slice width");
+  const int64_t Rp = pad_to(rows, BM), Kp = pad_to(K, BK);
+  uint8_t* w = static_cast<uint8_t*>(buf);
+  out->slices = w;
+  out->e = reinterpret_cast<int*>(w + (((size_t)S * Rp * Kp * 2 + 1023) & ~(size_t)1023));
+  out->nrm = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(out->e) +
+                                      (((size_t)Rp * sizeof(int) + 1023) & ~(size_t)1023));
+  out->rows = rows;
+  out->rows_pad = Rp;
+  out->K = K;
+  out->K_pad = Kp;
+  out->S = S;
+  out->bf16 = copy ? false : bf16;
+  out->tri = tri;
+  out->scaled = !copy;
+  TraceScope trace(NLA_K_SPLIT, s, 0.0,
+                   (double)rows * (double)K * (double)dtype_size(in_dtype) * (copy ? 1 : 2) + (double)S * Rp * Kp * 2);
+  const dim3 gs((unsigned)(Rp / 32), (unsigned)(Kp / 64));
+  if (copy) {
+    split_kernel<__half, __half><<<gs, 256, 0, s>>>((const __half*)X.p, X.ld, X.t, rows, K, tri, nullptr,
+                                                    (__half*)out->slices, Rp, Kp, 1, 0, 1, nullptr);
+    NLA_CHECK_LAUNCH("split_kernel");
+    return NLA_OK;
+  }
+  cudaMemsetAsync(out->e, 0x80, (size_t)Rp * sizeof(int), s);
+  cudaMemsetAsync(out->nrm, 0, (size_t)Rp * sizeof(float), s);
+  const dim3 ge((unsigned)((rows + 63) / 64), (unsigned)((K + 63) / 64));
+  row_exp_kernel<double><<<ge, 256, 0, s>>>((const double*)X.p, X.ld, X.t, rows, K, tri, out->e);
+  NLA_CHECK_LAUNCH("row_exp_kernel");
+  if (bf16)
+    split_kernel<double, __nv_bfloat16><<<gs, 256, 0, s>>>((const double*)X.p, X.ld, X.t, rows, K, tri, out->e,
+                                                           (__nv_bfloat16*)out->slices, Rp, Kp, S, beta, 0,
+                                                           out->nrm);
+  else
+    split_kernel<double, __half><<<gs, 256, 0, s>>>((const double*)X.p, X.ld, X.t, rows, K, tri, out->e,
+                                                    (__half*)out->slices, Rp, Kp, S, beta, 0, out->nrm);
+  NLA_CHECK_LAUNCH("split_kernel");
+  return NLA_OK;
+}
+
+size_t sliced_workspace_bytes(int64_t M, int64_t N, int64_t K, int S) {
+  return staged_bytes(M, K, S) + staged_bytes(N, K, S) + 1024;
 }
 
 // One tensor-core update.  in_dtype is NLA_F64 (split into S slices of BF16
 // or FP16) or NLA_F16 (S = 1, staged as is).  out_dtype is NLA_F64 or NLA_F16.
 int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat& A, const Mat& B, const Mat& C,
                        int in_dtype, int out_dtype, int S, bool bf16, void* ws, size_t ws_bytes, cudaStream_t s) {
-  if (M <= 0 || N <= 0) return NLA_OK;
-  if (K <= 0) return NLA_OK;
+  if (M <= 0 || N <= 0 || K <= 0) return NLA_OK;
   if (C.t) return fail(NLA_ERR_UNSUPPORTED, "tensor-core update: transposed output view");
   const bool copy = in_dtype == NLA_F16;
   if (copy) S = 1;
-  if (S < 1 || S > 3) return fail(NLA_ERR_ARG, "split terms must be 1, 2 or 3");
+  if (S == EXACT_SLICES && !copy) {
+    // Exact slice products (FP64-accurate update).
+    if (!bf16) return fail(NLA_ERR_ARG, "exact updates use BF16 slices");
+    if (out_dtype != NLA_F64) return fail(NLA_ERR_DTYPE, "exact updates produce Float64");
+    const size_t sa = staged_bytes(M, K, S), need = sa + staged_bytes(N, K, S) + 1024;
+    void* base = ws;
+    if (base == nullptr) {
+      NLA_TRY(workspace_get(s, need, &base));
+    } else if (ws_bytes < need) {
+      return fail(NLA_ERR_WORKSPACE, "workspace too small for the exact update");
+    }
+    Staged As, Bs;
+    NLA_TRY(stage_operand(A, M, K, NLA_F64, S, true, 0, base, &As, s));
+    NLA_TRY(stage_operand(transposed(B), N, K, NLA_F64, S, true, 0, static_cast<uint8_t*>(base) + sa, &Bs, s));
+    return launch_exact_gemm(As, Bs, alpha, C, false, s);
+  }
+  if (S < 1 || S > 3) return fail(NLA_ERR_ARG, "split terms must be 1, 2, 3 or 7");
   const int beta = bf16 ? 8 : 11;
   const int64_t Mp = pad_to(M, BM), Np = pad_to(N, BN), Kp = pad_to(K, BK);
   if (S * Mp > 0xFFFFFFFFLL || S * Np > 0xFFFFFFFFLL) return fail(NLA_ERR_UNSUPPORTED, "operand too large");
@@ -441,51 +769,16 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
   } else if (ws_bytes < need) {
     return fail(NLA_ERR_WORKSPACE, "workspace too small for the tensor-core update");
   }
-  uint8_t* w = static_cast<uint8_t*>(base);
-  void* As = w;
-  void* Bs = w + (size_t)S * Mp * Kp * 2;
-  size_t off = ((size_t)S * (Mp + Np) * Kp * 2 + 1023) & ~(size_t)1023;
-  int* ea = reinterpret_cast<int*>(w + off);
-  int* eb = ea + Mp;
+  Staged As, Bs;
+  NLA_TRY(stage_operand(A, M, K, in_dtype, S, bf16, 0, base, &As, s));
+  // N x K view: row j is column j of op(B)
+  NLA_TRY(stage_operand(transposed(B), N, K, in_dtype, S, bf16, 0, static_cast<uint8_t*>(base) + staged_bytes(M, K, S),
+                        &Bs, s));
 
-  const Mat Bt = transposed(B);  // N x K view: row j is column j of op(B)
-  {
-    TraceScope trace(NLA_K_SPLIT, s, 0.0,
-                     (double)(M * K + K * N) * (double)dtype_size(in_dtype) * (copy ? 1 : 2) +
-                         (double)S * (Mp + Np) * Kp * 2);
-    if (!copy) {
-      cudaMemsetAsync(ea, 0x80, (size_t)(Mp + Np) * sizeof(int), s);
-      dim3 ga((unsigned)((M + 63) / 64), (unsigned)((K + 63) / 64));
-      dim3 gb((unsigned)((N + 63) / 64), (unsigned)((K + 63) / 64));
-      row_exp_kernel<double><<<ga, 256, 0, s>>>((const double*)A.p, A.ld, A.t, M, K, ea);
-      row_exp_kernel<double><<<gb, 256, 0, s>>>((const double*)Bt.p, Bt.ld, Bt.t, N, K, eb);
-      NLA_CHECK_LAUNCH("row_exp_kernel");
-      dim3 sa((unsigned)(Mp / 32), (unsigned)(Kp / 64)), sb((unsigned)(Np / 32), (unsigned)(Kp / 64));
-      if (bf16) {
-        split_kernel<double, __nv_bfloat16><<<sa, 256, 0, s>>>((const double*)A.p, A.ld, A.t, M, K, ea,
-                                                               (__nv_bfloat16*)As, Mp, Kp, S, beta, 0);
-        split_kernel<double, __nv_bfloat16><<<sb, 256, 0, s>>>((const double*)Bt.p, Bt.ld, Bt.t, N, K, eb,
-                                                               (__nv_bfloat16*)Bs, Np, Kp, S, beta, 0);
-      } else {
-        split_kernel<double, __half><<<sa, 256, 0, s>>>((const double*)A.p, A.ld, A.t, M, K, ea, (__half*)As, Mp,
-                                                        Kp, S, beta, 0);
-        split_kernel<double, __half><<<sb, 256, 0, s>>>((const double*)Bt.p, Bt.ld, Bt.t, N, K, eb, (__half*)Bs,
-                                                        Np, Kp, S, beta, 0);
-      }
-    } else {
-      dim3 sa((unsigned)(Mp / 32), (unsigned)(Kp / 64)), sb((unsigned)(Np / 32), (unsigned)(Kp / 64));
-      split_kernel<__half, __half><<<sa, 256, 0, s>>>((const __half*)A.p, A.ld, A.t, M, K, nullptr, (__half*)As,
-                                                      Mp, Kp, 1, 0, 1);
-      split_kernel<__half, __half><<<sb, 256, 0, s>>>((const __half*)Bt.p, Bt.ld, Bt.t, N, K, nullptr,
-                                                      (__half*)Bs, Np, Kp, 1, 0, 1);
-    }
-    NLA_CHECK_LAUNCH("split_kernel");
-  }
-
-  const bool use_bf16 = copy ? false : bf16;
+  const bool use_bf16 = As.bf16;
   CUtensorMap mA, mB;
-  NLA_TRY(make_map(&mA, As, use_bf16, (uint64_t)Kp, (uint64_t)(S * Mp)));
-  NLA_TRY(make_map(&mB, Bs, use_bf16, (uint64_t)Kp, (uint64_t)(S * Np)));
+  NLA_TRY(make_map(&mA, As.slices, use_bf16, (uint64_t)Kp, (uint64_t)(S * Mp)));
+  NLA_TRY(make_map(&mB, Bs.slices, use_bf16, (uint64_t)Kp, (uint64_t)(S * Np)));
 
   GemmParams p{};
   p.M = (int)M;
@@ -521,8 +814,8 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
   p.C = C.p;
   p.ldc = C.ld;
   p.alpha = alpha;
-  p.ea = copy ? nullptr : ea;
-  p.eb = copy ? nullptr : eb;
+  p.ea = copy ? nullptr : As.e;
+  p.eb = copy ? nullptr : Bs.e;
   p.exp_bias = copy ? 0 : -2 * beta;
 
   const int smem = p.stages * p.stage_bytes + 1024 + 256;
@@ -542,6 +835,56 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
     return fail(NLA_ERR_DTYPE, "tensor-core update: unsupported output type");
   }
   NLA_CHECK_LAUNCH("umma_gemm_kernel");
+  return NLA_OK;
+}
+
+// C (M x N, FP64) += alpha * A * B^T from two operands staged with
+// EX_SLICES BF16 slices (A: M rows, B: N rows, same K).
+int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat& C, bool trans_out,
+                      cudaStream_t s) {
+  const int64_t M = A.rows, N = B.rows, K = A.K;
+  if (M <= 0 || N <= 0 || K <= 0) return NLA_OK;
+  if (B.K != K || A.S != EX_SLICES || B.S != EX_SLICES || !A.bf16 || !B.bf16 || !A.scaled || !B.scaled)
+    return fail(NLA_ERR_ARG, "exact update: operands not staged for it");
+  if (C.t) return fail(NLA_ERR_UNSUPPORTED, "exact update: transposed output view");
+  if (K > (1LL << 30)) return fail(NLA_ERR_UNSUPPORTED, "exact update: K too large");
+  CUtensorMap mA, mB;
+  NLA_TRY(make_map(&mA, A.slices, true, (uint64_t)A.K_pad, (uint64_t)(EX_SLICES * A.rows_pad)));
+  NLA_TRY(make_map(&mB, B.slices, true, (uint64_t)B.K_pad, (uint64_t)(EX_SLICES * B.rows_pad)));
+  ExactParams p{};
+  p.M = (int)M;
+  p.N = (int)N;
+  p.K = (int)K;
+  p.tiles_m = (int)(A.rows_pad / BM);
+  p.tiles_n = (int)(B.rows_pad / BN);
+  p.a_rows = (int)A.rows_pad;
+  p.b_rows = (int)B.rows_pad;
+  p.npairs = 0;
+  for (int t = 0; t < EX_SLICES; ++t)
+    for (int a = 0; a <= t; ++a) {
+      p.pa[p.npairs] = (int8_t)a;
+      p.pb[p.npairs] = (int8_t)(t - a);
+      ++p.npairs;
+    }
+  p.tri_a = A.tri;
+  p.tri_b = B.tri;
+  p.trans_out = trans_out ? 1 : 0;
+  p.nrm_a = A.nrm;
+  p.C = C.p;
+  p.ldc = C.ld;
+  p.alpha = alpha;
+  p.ea = A.e;
+  p.eb = B.e;
+  const int64_t grid = (int64_t)p.tiles_m * p.tiles_n;
+  if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "too many output tiles");
+  NLA_TRY(ensure_exact_smem());
+  // Executed flops of the slice pairs: 2 M N K per pair, half of that when
+  // one operand is a staged triangle (its tiles' K ranges are clipped).
+  const double tri_frac = (A.tri != 0 || B.tri != 0) ? 0.5 : 1.0;
+  TraceScope trace(NLA_K_GEMM_UMMA, s, 2.0 * (double)M * N * (double)K * p.npairs * tri_frac,
+                   (double)EX_SLICES * (A.rows_pad + B.rows_pad) * A.K_pad * 2 + 16.0 * (double)M * N);
+  umma_exact_kernel<<<(unsigned)grid, EX_THREADS, EX_DYN_SMEM, s>>>(mA, mB, p);
+  NLA_CHECK_LAUNCH("umma_exact_kernel");
   return NLA_OK;
 }
 

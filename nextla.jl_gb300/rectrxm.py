@@ -341,8 +341,32 @@ def matmul_mixed_(output, input1, input2, alpha=1.0, *, lowp="bf16", split_terms
     return output
 
 
+_RESIDUAL = {"split": _lib.NLA_RESIDUAL_SPLIT, "fp64": _lib.NLA_RESIDUAL_FP64}
+
+
+def residual_(side, uplo, transpose, alpha, A, X, B, R, *, residual="split"):
+    """R = alpha*B - op(A) X (side 'L') or alpha*B - X op(A) (side 'R') for
+    Float64 tensors, FP64-accurate (``residual`` 'split': tensor cores with
+    exact slice products; 'fp64': the FP64 pipe)."""
+    _check_flags(side, uplo, transpose, "M")
+    a, lda, ta = _mat(A)
+    if ta:
+        raise ValueError("pass A untransposed and use `transpose`")
+    x, ldx, tx = _mat(X)
+    b, ldb, tb = _mat(B)
+    r, ldr, tr = _mat(R)
+    if tx or tb or tr:
+        raise ValueError("X, B and R must be column-major views")
+    n = A.shape[0]
+    m = X.shape[1] if side == "L" else X.shape[0]
+    L = _lib.load()
+    _lib.check(L.nla_trxm_residual(_lib.ch(side), _lib.ch(uplo), _lib.ch(transpose), float(alpha), n, m, a, lda, x,
+                                   ldx, b, ldb, r, ldr, _RESIDUAL[residual], _stream(R)))
+    return R
+
+
 def unified_rectrxm_mixed_(side, uplo, transpose, alpha, func, A, B, *, lowp="bf16", split_terms=3, sweeps=2,
-                           cutoff=0, corrections=False):
+                           cutoff=0, corrections=False, residual="split"):
     """Mixed-precision unified_rectrxm! for Float64 A and B (in place in B).
 
     Updates run on the tensor cores from ``split_terms`` slices (``lowp`` 'bf16'
@@ -366,7 +390,7 @@ def unified_rectrxm_mixed_(side, uplo, transpose, alpha, func, A, B, *, lowp="bf
     n = A.shape[0]
     m = B.shape[1] if side == "L" else B.shape[0]
     corr = (ctypes.c_double * max(int(sweeps), 1))()
-    opts = _lib.MixedOpts(_LOWP[lowp], int(split_terms), int(sweeps), _lib.NLA_RESIDUAL_FP64, int(cutoff),
+    opts = _lib.MixedOpts(_LOWP[lowp], int(split_terms), int(sweeps), _RESIDUAL[residual], int(cutoff),
                           ctypes.cast(corr, ctypes.POINTER(ctypes.c_double)) if corrections else None)
     L = _lib.load()
     _lib.check(L.nla_trxm_mixed(_lib.ch(side), _lib.ch(up), _lib.ch(tr), float(alpha), _lib.ch(func), n, m, a, lda,

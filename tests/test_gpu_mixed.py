@@ -50,7 +50,7 @@ def test_refinement_matches_plain_backward_error(pkg, oracle, workloads, cuda):
 
     n, m = 2048, 64
     A, B = workloads.problem(n, m, "L", "L", seed=21)
-    X, corr = _mixed(pkg, cuda, "L", "L", "N", 1.0, "S", A, B, sweeps=3, corrections=True)
+    X, corr = _mixed(pkg, cuda, "L", "L", "N", 1.0, "S", A, B, sweeps=3, corrections=True, residual="split")
     Ad, Bd = to_dev(A, np.float64, cuda), to_dev(B, np.float64, cuda)
     pkg.unified_rectrxm_("L", "L", "N", 1.0, "S", Ad, Bd, native=True)
     torch.cuda.synchronize()
@@ -79,3 +79,21 @@ def test_mixed_rejects_bad_options(pkg, cuda):
     with pytest.raises(ValueError):
         pkg.unified_rectrxm_mixed_("L", "L", "N", 1.0, "S", A.float(), B.float())
     torch.cuda.synchronize()
+
+
+def test_exact_updates_without_refinement(pkg, oracle, workloads, cuda):
+    """split_terms = 7: FP64-accurate updates, FP64 leaves, no refinement."""
+    for side, uplo, trans in [("L", "L", "N"), ("R", "U", "T"), ("L", "U", "T"), ("R", "L", "N")]:
+        A, B = workloads.problem(1500, 60, side, uplo, seed=17)
+        ref = oracle.rectrxm(side, uplo, trans, 1.0, "S", A, B, nthreads=os.cpu_count() or 1)
+        X = _mixed(pkg, cuda, side, uplo, trans, 1.0, "S", A, B, split_terms=7, sweeps=0)
+        assert oracle.rel_err(X, ref) < 1e-13
+
+
+@pytest.mark.parametrize("residual", ["split", "fp64"])
+def test_refinement_residual_modes(pkg, oracle, workloads, cuda, residual):
+    for side, uplo, trans in [("L", "L", "N"), ("R", "U", "T"), ("R", "L", "T"), ("L", "U", "N")]:
+        A, B = workloads.problem(900, 50, side, uplo, seed=23)
+        ref = oracle.rectrxm(side, uplo, trans, 0.5, "S", A, B, nthreads=os.cpu_count() or 1)
+        X = _mixed(pkg, cuda, side, uplo, trans, 0.5, "S", A, B, split_terms=2, sweeps=3, residual=residual)
+        assert oracle.rel_err(X, ref) < 1e-14, (side, uplo, trans)
