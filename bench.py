@@ -56,6 +56,11 @@ def parse():
     ap.add_argument("--residual", choices=["split", "fp64"], default="split")
     ap.add_argument("--cutoff", type=int, default=0)
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison step")
+    ap.add_argument("--workload", choices=["single", "batched"], default="single",
+                    help="single: one n x m system; batched: 10,000 uneven systems in one persistent launch")
+    ap.add_argument("--dtype", choices=["f64", "f32"], default="f64", help="element type of the batched workload")
+    ap.add_argument("--count", type=int, default=10000, help="systems in the batched workload")
+    ap.add_argument("--tune", action="store_true", help="autotune the batched tile widths before timing")
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--m", type=int, default=16384)
     ap.add_argument("--cpu-sample", type=int, default=0,
@@ -200,10 +205,70 @@ def run_reference(args):
     return 0
 
 
+def run_batched(args):
+    """10,000 independent lower-triangular systems (side L, trans N), n_i
+    log-uniform in [16, 1024], m_i uniform in 1..128, seed 7: one persistent
+    launch replayed from a CUDA graph, against one recursion per system."""
+    import torch
+
+    import __graft_entry__ as graft
+
+    graft.load_package()
+    from nextla_gb300 import _lib, batched, tune
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    dtype = torch.float64 if args.dtype == "f64" else torch.float32
+    n, m = batched.uneven_sizes(count=args.count, seed=7)
+    A, B0, systems = batched.make_batch(n, m, dtype, dev, seed=7)
+    flops = float((n.astype(float) ** 2 * m).sum())
+    cw = tune.tune(dtype, dev)[0] if args.tune else tune.lookup(dtype, dev)
+    plan = batched.BatchPlan(dtype, "L", "N", systems, cols_per_item=cw)
+    B = B0.clone()
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(mode, steps):
+        for _ in range(args.warmup):
+            B.copy_(B0)
+            plan.solve(1.0, A, B, mode=mode)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            B.copy_(B0)
+            plan.solve(1.0, A, B, mode=mode)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / steps
+
+    _lib.trace_enable(True)
+    ms = timed("graph", args.steps)
+    _lib.trace_enable(False)
+    trace = _lib.trace_summary()
+    loop_ms = timed("loop", max(1, min(args.steps, 2)))
+    items, grid, _ = plan.info()
+    line = {
+        "metric": "batched_trsm_tflops", "value": flops / (ms / 1e3) / 1e12, "unit": "TFLOP/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded)",
+        "config": {"workload": "batched_trsm_LLN_%s_%d_uneven" % (args.dtype, args.count), "count": args.count,
+                   "n": "log-uniform [16, 1024]", "m": "uniform 1..128", "seed": 7, "flops": flops,
+                   "work_items": items, "persistent_ctas": grid, "cols_per_item": cw or "library defaults"},
+        "one_launch_per_system": {"ms": loop_ms, "tflops": flops / (loop_ms / 1e3) / 1e12},
+        "speedup_vs_one_launch_per_system": loop_ms / ms,
+        "trace": {k: {"launches": v[0], "ms": v[1]} for k, v in trace.items()},
+    }
+    print(json.dumps(line), flush=True)
+    plan.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
 
     import numpy as np
     import torch

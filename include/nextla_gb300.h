@@ -176,6 +176,42 @@ NLA_API int nla_trxm_residual(char side, char uplo, char trans, double alpha, in
 NLA_API int nla_device_status(void* stream);
 
 /*
+ * Batched solve of independent, unevenly sized systems (no counterpart in the
+ * reference, which solves one system per unified_rectrxm! call,
+ * src/rectrxm.jl:43-76).  Every system i solves op(A_i) X_i = alpha B_i
+ * (side 'L', the batch's uplo and trans) in place in B_i, with A_i n_i x n_i
+ * (n_i <= 1024) at A_pool + a_off elements and B_i n_i x m_i at
+ * B_pool + b_off elements, column-major with leading dimensions lda, ldb.
+ * A plan uploads the descriptors and a cost-sorted list of work items (one
+ * per system and block of right-hand sides); `cols_per_item` gives the block
+ * width (8, 16 or 32) for each size bucket b (16*2^b <= n < 32*2^b, the last
+ * bucket open above), or NULL for defaults.  The plan owns device memory
+ * until destroyed; one plan must not be used from two streams at once.
+ * Modes of nla_batch_solve:
+ *   NLA_BATCH_GRAPH       one persistent kernel, captured once into a CUDA
+ *                         graph (re-captured when alpha or the pools change)
+ *                         and replayed;
+ *   NLA_BATCH_PERSISTENT  the same kernel launched directly;
+ *   NLA_BATCH_LOOP        one nla_trxm recursion per system (the baseline).
+ */
+typedef struct {
+  int64_t n, m;
+  int64_t a_off, lda;
+  int64_t b_off, ldb;
+} nla_batch_desc;
+#define NLA_BATCH_BUCKETS 6
+#define NLA_BATCH_GRAPH 0
+#define NLA_BATCH_PERSISTENT 1
+#define NLA_BATCH_LOOP 2
+typedef struct nla_batch_plan_s* nla_batch_plan;
+NLA_API int nla_batch_plan_create(nla_batch_plan* plan, int dtype, char uplo, char trans, int64_t count,
+                                  const nla_batch_desc* descs, const int* cols_per_item);
+NLA_API int nla_batch_plan_info(nla_batch_plan plan, int64_t* items, int64_t* grid, double* flops);
+NLA_API int nla_batch_solve(nla_batch_plan plan, double alpha, const void* A_pool, void* B_pool, int mode,
+                            void* stream);
+NLA_API int nla_batch_plan_destroy(nla_batch_plan plan);
+
+/*
  * Kernel tracing (no counterpart in the reference, which has no tracing).
  * nla_trace_enable(1) clears earlier records and starts recording; every
  * library kernel launched afterwards is bracketed by CUDA events on its

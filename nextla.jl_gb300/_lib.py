@@ -58,6 +58,24 @@ SIGNATURES.update({
     "nla_trxm_residual": ([_c, _c, _c, _d, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _i32, _p], _i32),
 })
 
+class BatchDesc(ctypes.Structure):
+    """nla_batch_desc of include/nextla_gb300.h."""
+
+    _fields_ = [("n", ctypes.c_int64), ("m", ctypes.c_int64), ("a_off", ctypes.c_int64), ("lda", ctypes.c_int64),
+                ("b_off", ctypes.c_int64), ("ldb", ctypes.c_int64)]
+
+
+NLA_BATCH_BUCKETS = 6
+NLA_BATCH_GRAPH, NLA_BATCH_PERSISTENT, NLA_BATCH_LOOP = 0, 1, 2
+
+SIGNATURES.update({
+    "nla_batch_plan_create": ([ctypes.POINTER(_p), _i32, _c, _c, _i64, ctypes.POINTER(BatchDesc),
+                               ctypes.POINTER(_i32)], _i32),
+    "nla_batch_plan_info": ([_p, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_d)], _i32),
+    "nla_batch_solve": ([_p, _d, _p, _p, _i32, _p], _i32),
+    "nla_batch_plan_destroy": ([_p], _i32),
+})
+
 KERNEL_CLASSES = ["leaf_solve", "leaf_mult", "gemm_simt", "gemm_umma", "split", "scale", "residual", "batched"]
 
 _lib = None
