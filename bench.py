@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--dtype", choices=["f64", "f32"], default="f64", help="element type of the batched workload")
     ap.add_argument("--count", type=int, default=10000, help="systems in the batched workload")
     ap.add_argument("--tune", action="store_true", help="autotune the batched tile widths before timing")
+    ap.add_argument("--error-table", action="store_true",
+                    help="mixed-precision error and speed versus cond(A) (JSON line per configuration)")
+    ap.add_argument("--conds", default="1e2,1e4,1e6,1e8")
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--m", type=int, default=16384)
     ap.add_argument("--cpu-sample", type=int, default=0,
@@ -263,12 +266,87 @@ def run_batched(args):
     return 0
 
 
+def run_error_table(args):
+    """Float64 TRSM L/L/N at n x m with A graded to cond(A) in --conds (LAPACK
+    dtrcon 1-norm estimate): for each cond, the plain FP64 solve (the FP64
+    oracle of this table) and every mixed configuration (BF16 / FP16 slices,
+    1-3 terms and 7 exact BF16 terms, 0-3 refinement sweeps).  One JSON line
+    each: time, TFLOP/s, normwise relative error against the FP64 solution
+    and backward error (double-double residual on 64 sampled columns)."""
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as graft
+
+    pkg = graft.load_package()
+    from nextla_gb300 import workloads
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    n, m = args.n, args.m
+    flops = float(n) * n * m
+    rng = np.random.default_rng(1)
+    B_h = np.asfortranarray(rng.uniform(-1.0, 1.0, (n, m)))
+    B0 = torch.from_numpy(np.ascontiguousarray(B_h.T)).to(dev).T
+    cols = torch.arange(0, m, max(1, m // 64), device=dev)
+
+    def berr(A, X):
+        Xs = X[:, cols].contiguous().T.contiguous().T
+        Bs = B0[:, cols].contiguous().T.contiguous().T
+        Rs = torch.empty_like(Xs.T).T
+        pkg.residual_("L", "L", "N", 1.0, A, Xs, Bs, Rs, residual="dd")
+        torch.cuda.synchronize(dev)
+        an = float(torch.tril(A).abs().sum(dim=1).max())
+        return float(Rs.abs().sum(dim=1).max() / (an * Xs.abs().sum(dim=1).max() * n * 2.0 ** -53))
+
+    def timed(fn, A):
+        X = torch.empty_like(B0.T).T
+        X.copy_(B0)
+        fn(A, X)  # warm-up (also sizes the workspace pools)
+        X.copy_(B0)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn(A, X)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        pkg.device_status(X)
+        return X, e0.elapsed_time(e1)
+
+    for target in [float(c) for c in args.conds.split(",")]:
+        A_h, c, cond = workloads.conditioned(n, target, seed=0)
+        A = torch.from_numpy(np.ascontiguousarray(A_h.T)).to(dev).T
+        del A_h
+        Xref, pms = timed(lambda A_, X_: pkg.unified_rectrxm_("L", "L", "N", 1.0, "S", A_, X_, native=True), A)
+        ref_norm = float(torch.linalg.norm(Xref))
+        base = {"n": n, "m": m, "cond_target": target, "cond1_dtrcon": cond, "diag_scale": c}
+        print(json.dumps(dict(base, variant="plain_fp64", ms=pms, tflops=flops / pms / 1e9, rel_err=0.0,
+                              backward_error=berr(A, Xref))), flush=True)
+        configs = [("bf16", t, sw) for t in (1, 2, 3) for sw in (0, 1, 2, 3)]
+        configs += [("f16", t, sw) for t in (1, 2, 3) for sw in (0, 1, 2, 3)]
+        configs += [("bf16", 7, sw) for sw in (0, 1)]
+        for lowp, terms, sweeps in configs:
+            fn = (lambda A_, X_, lowp=lowp, terms=terms, sweeps=sweeps:
+                  pkg.unified_rectrxm_mixed_("L", "L", "N", 1.0, "S", A_, X_, lowp=lowp, split_terms=terms,
+                                             sweeps=sweeps))
+            X, ms = timed(fn, A)
+            rel = float(torch.linalg.norm(X - Xref)) / ref_norm
+            print(json.dumps(dict(base, variant="mixed", lowp=lowp, split_terms=terms, sweeps=sweeps, ms=ms,
+                                  tflops=flops / ms / 1e9, rel_err=rel, backward_error=berr(A, X),
+                                  finite=bool(torch.isfinite(X).all()))), flush=True)
+            del X
+        del A, Xref
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.error_table:
+        return run_error_table(args)
 
     import numpy as np
     import torch
@@ -353,15 +431,15 @@ def main():
     trace = _lib.trace_summary()
 
     # Accuracy of the last solution on a sample of columns: backward error
-    # ||A X - B||_inf / (||A||_inf ||X||_inf n u), residual formed with the
-    # library's FP64-accurate split residual.
+    # ||A X - B||_inf / (||A||_inf ||X||_inf n u), residual accumulated in
+    # double-double (the library's NLA_RESIDUAL_DD mode).
     cols = torch.arange(0, m, max(1, m // 64), device=dev)
 
     def backward_error(Xfull):
         Xs_ = Xfull[:, cols].contiguous().T.contiguous().T
         Bs_ = B0[:, cols].contiguous().T.contiguous().T
         Rs_ = torch.empty_like(Xs_.T).T
-        pkg.residual_("L", "L", "N", 1.0, A, Xs_, Bs_, Rs_)
+        pkg.residual_("L", "L", "N", 1.0, A, Xs_, Bs_, Rs_, residual="dd")
         torch.cuda.synchronize(dev)
         an = float(torch.tril(A).abs().sum(dim=1).max())
         return float(Rs_.abs().sum(dim=1).max() / (an * Xs_.abs().sum(dim=1).max() * n * 2.0 ** -53))

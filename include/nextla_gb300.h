@@ -134,6 +134,8 @@ NLA_API int nla_scale(int dtype, int64_t rows, int64_t cols, double alpha, void*
 #define NLA_RESIDUAL_FP64 0  /* residual product on the FP64 pipe (DFMA) */
 #define NLA_RESIDUAL_SPLIT 1 /* residual product from 7 BF16 slices per operand with
                                 exact FP32 chunk sums and 64-bit integer accumulation */
+#define NLA_RESIDUAL_DD 2    /* nla_trxm_residual only: double-double accumulation on
+                                the FP64 pipe, rounded once (for measuring errors) */
 typedef struct {
   int lowp;          /* NLA_LOWP_BF16 or NLA_LOWP_F16 */
   int split_terms;   /* 1, 2 or 3 slices per operand; 7 = exact BF16 slice products (FP64-accurate updates) */
@@ -161,8 +163,9 @@ NLA_API int nla_gemm_update_mixed(int trans1, int trans2, int64_t N, int64_t R, 
  * The residual of a solve, FP64-accurate (no counterpart in the reference):
  * R = alpha*B - op(A) X (side 'L') or alpha*B - X op(A) (side 'R'), with A
  * n x n triangular (uplo, trans as for nla_trxm) and X, B, R of B's shape.
- * `residual` selects NLA_RESIDUAL_SPLIT (tensor cores, exact slice products)
- * or NLA_RESIDUAL_FP64 (FP64 pipe).  R must not overlap X or B.
+ * `residual` selects NLA_RESIDUAL_SPLIT (tensor cores, exact slice products),
+ * NLA_RESIDUAL_FP64 (FP64 pipe) or NLA_RESIDUAL_DD (double-double, rounded
+ * once: the reference value for backward errors).  R must not overlap X or B.
  */
 NLA_API int nla_trxm_residual(char side, char uplo, char trans, double alpha, int64_t n, int64_t m, const double* A,
                               int64_t lda, const double* X, int64_t ldx, const double* B, int64_t ldb, double* R,

@@ -40,7 +40,7 @@ SIGNATURES = {
 }
 
 NLA_LOWP_BF16, NLA_LOWP_F16 = 0, 1
-NLA_RESIDUAL_FP64, NLA_RESIDUAL_SPLIT = 0, 1
+NLA_RESIDUAL_FP64, NLA_RESIDUAL_SPLIT, NLA_RESIDUAL_DD = 0, 1, 2
 
 
 class MixedOpts(ctypes.Structure):

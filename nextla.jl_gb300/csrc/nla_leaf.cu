@@ -42,32 +42,31 @@ __global__ void __launch_bounds__(LEAF_THREADS) leaf_mult_kernel(LeafArgs g) {
   load_block<T, Tc, CW>(g, X, c0, ncols);
   __syncthreads();
 
+  constexpr int CT = CW / 4;
+  const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;
   for (int r0 = 0; r0 < n; r0 += LEAF_THREADS) {
     const int rows = min(LEAF_THREADS, n - r0);
     const int kmax = min(n, r0 + rows);  // k <= r
-    const int t = threadIdx.x;
-    const int r = r0 + t;
-    Tc acc[CW];
+    Tc acc[4][CT];
 #pragma unroll
-    for (int c = 0; c < CW; ++c) acc[c] = Tc(0);
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int c = 0; c < CT; ++c) acc[i][c] = Tc(0);
     for (int k0 = 0; k0 < kmax; k0 += PANEL) {
       const int kw = min(PANEL, kmax - k0);
       stage_slab<LEAF_THREADS, T>(g, slab, r0, rows, k0, kw, [](int i, int j) { return j <= i; });
       __syncthreads();
-      if (t < rows) {
-        for (int kk = 0; kk < kw; ++kk) {
-          const Tc a = slab[t * SLAB_PAD + kk];
-          const Tc* xr = X + (k0 + kk) * CW;
-#pragma unroll
-          for (int c = 0; c < CW; ++c) acc[c] = fma(a, xr[c], acc[c]);
-        }
-      }
+      tile_product<Tc, CW>(slab, X + (size_t)k0 * CW, kw, acc);
       __syncthreads();
     }
-    if (t < rows) {
 #pragma unroll
-      for (int c = 0; c < CW; ++c)
-        if (c < ncols) Elem<T>::store(Bp + b_off<T>(g, r, c0 + c), acc[c]);
+    for (int i = 0; i < 4; ++i) {
+      const int r = tr + 32 * i;
+      if (r < rows) {
+#pragma unroll
+        for (int c = 0; c < CT; ++c)
+          if (tc * CT + c < ncols) Elem<T>::store(Bp + b_off<T>(g, r0 + r, c0 + tc * CT + c), acc[i][c]);
+      }
     }
   }
 }

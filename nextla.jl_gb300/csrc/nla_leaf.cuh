@@ -94,6 +94,53 @@ __device__ __forceinline__ void store_block(const LeafArgs& g, const Tc* X, int6
   }
 }
 
+// acc[i][c] += sum_kk slab[tr + 32 i][kk] * Xp[kk, tc * CW/4 + c] for
+// kk < pw: LEAF_THREADS threads as 32 row lanes (tr) x 4 column groups (tc,
+// one warp each, so the X reads are warp-wide broadcasts).  Each k step reads
+// 4 slab values and CW/4 values of X for 4 * CW/4 fused multiply-adds.
+template <typename Tc, int CW>
+__device__ __forceinline__ void tile_product(const Tc* __restrict__ slab, const Tc* __restrict__ Xp, int pw,
+                                             Tc (&acc)[4][CW / 4]) {
+  constexpr int CT = CW / 4;
+  const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;
+  for (int kk = 0; kk < pw; ++kk) {
+    Tc a[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = slab[(tr + 32 * i) * SLAB_PAD + kk];
+    Tc xv[CT];
+    const Tc* xr = Xp + kk * CW + tc * CT;
+#pragma unroll
+    for (int c = 0; c < CT; ++c) xv[c] = xr[c];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int c = 0; c < CT; ++c) acc[i][c] = fma(a[i], xv[c], acc[i][c]);
+  }
+}
+
+// Xo[r, :] -= sum_kk slab[r][kk] * Xp[kk, :] for r < rows, kk < pw.
+template <typename Tc, int CW>
+__device__ __forceinline__ void trailing_update(const Tc* __restrict__ slab, const Tc* __restrict__ Xp,
+                                                Tc* __restrict__ Xo, int rows, int pw) {
+  constexpr int CT = CW / 4;
+  const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;
+  Tc acc[4][CT];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int c = 0; c < CT; ++c) acc[i][c] = Tc(0);
+  tile_product<Tc, CW>(slab, Xp, pw, acc);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = tr + 32 * i;
+    if (r < rows) {
+      Tc* xo = Xo + r * CW + tc * CT;
+#pragma unroll
+      for (int c = 0; c < CT; ++c) xo[c] -= acc[i][c];
+    }
+  }
+}
+
 // Canonical lower-left solve: X := L^{-1} (alpha X) for the CW columns
 // starting at c0 (ncols of them valid), run by one CTA of LEAF_THREADS.
 // smem holds leaf_solve_smem_elems(n, CW) compute-type elements.
@@ -139,26 +186,16 @@ __device__ __forceinline__ void solve_block(const LeafArgs& g, int64_t c0, int n
     }
     __syncthreads();
 
-    // Rows below the panel: X[r, :] -= A[r, panel] * X[panel, :].
+    // Rows below the panel: X[r, :] -= A[r, panel] * X[panel, :], as a
+    // register-tiled product: thread (tr, tc) owns rows r0 + tr + 32 i
+    // (i < 4) and the CW/4 columns of column group tc (its warp), so each
+    // k step reads 4 slab values and one broadcast vector of X for 4 * CW/4
+    // fused multiply-adds.
     for (int r0 = p0 + pw; r0 < n; r0 += LEAF_THREADS) {
       const int rows = min(LEAF_THREADS, n - r0);
       stage_slab<LEAF_THREADS, T>(g, slab, r0, rows, p0, pw, [](int, int) { return true; });
       __syncthreads();
-      const int t = threadIdx.x;
-      if (t < rows) {
-        Tc acc[CW];
-#pragma unroll
-        for (int c = 0; c < CW; ++c) acc[c] = Tc(0);
-        for (int kk = 0; kk < pw; ++kk) {
-          const Tc a = slab[t * SLAB_PAD + kk];
-          const Tc* xr = X + (p0 + kk) * CW;
-#pragma unroll
-          for (int c = 0; c < CW; ++c) acc[c] = fma(a, xr[c], acc[c]);
-        }
-        Tc* xo = X + (r0 + t) * CW;
-#pragma unroll
-        for (int c = 0; c < CW; ++c) xo[c] -= acc[c];
-      }
+      trailing_update<Tc, CW>(slab, X + (size_t)p0 * CW, X + (size_t)r0 * CW, rows, pw);
       __syncthreads();
     }
   }

@@ -106,6 +106,54 @@ __global__ void diag_residual_kernel(int64_t rows, int64_t cols, const double* _
   }
 }
 
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+  s = a + b;
+  const double bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+
+// R = alpha*B - op(A) X (left) or alpha*B - X op(A) (right), accumulated in
+// double-double (exact products by fma, error-free sums) and rounded once;
+// op(A) is the `lower` (after the transpose flip) triangle of A or A^T.
+__global__ void dd_residual_kernel(int64_t rows, int64_t cols, int64_t n, const double* __restrict__ A, int64_t lda,
+                                   int tA, int lower, int left, const double* __restrict__ X, int64_t ldx,
+                                   const double* __restrict__ B, int64_t ldb, double alpha, double* __restrict__ R,
+                                   int64_t ldr) {
+  const int64_t total = rows * cols;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % rows, j = idx / rows;
+    double hi = 0.0, lo = 0.0;
+    // left:  sum over k of op(A)(i,k) X(k,j), k in the triangle of row i
+    // right: sum over k of X(i,k) op(A)(k,j), k in the triangle of column j
+    const int64_t piv = left ? i : j;
+    int64_t k0, k1;
+    if (left) { k0 = lower ? 0 : piv; k1 = lower ? piv + 1 : n; }
+    else { k0 = lower ? piv : 0; k1 = lower ? n : piv + 1; }
+    for (int64_t k = k0; k < k1; ++k) {
+      double a, x;
+      if (left) {
+        a = tA ? A[k + i * lda] : A[i + k * lda];
+        x = X[k + j * ldx];
+      } else {
+        a = tA ? A[j + k * lda] : A[k + j * lda];
+        x = X[i + k * ldx];
+      }
+      const double p = a * x;
+      const double pe = fma(a, x, -p);
+      double e;
+      two_sum(hi, p, hi, e);
+      lo += e + pe;
+    }
+    const double b = B[i + j * ldb];
+    const double q = alpha * b;
+    const double qe = fma(alpha, b, -q);
+    double r, e2;
+    two_sum(q, -hi, r, e2);
+    R[i + j * ldr] = r + ((e2 + qe) - lo);
+  }
+}
+
 unsigned grid_for(int64_t total) {
   int64_t blocks = (total + 255) / 256;
   const int64_t cap = (int64_t)num_sms() * 8;
@@ -276,7 +324,8 @@ int residual_impl(char side, char uplo, char trans, double alpha, int64_t n, int
   NLA_TRY(check_matrix("X", X, rows, cols, ldx));
   NLA_TRY(check_matrix("B", B, rows, cols, ldb));
   NLA_TRY(check_matrix("R", R, rows, cols, ldr));
-  if (mode != NLA_RESIDUAL_FP64 && mode != NLA_RESIDUAL_SPLIT) return fail(NLA_ERR_ARG, "unknown residual mode");
+  if (mode != NLA_RESIDUAL_FP64 && mode != NLA_RESIDUAL_SPLIT && mode != NLA_RESIDUAL_DD)
+    return fail(NLA_ERR_ARG, "unknown residual mode");
   if (rows == 0 || cols == 0) return NLA_OK;
   Mat Am{const_cast<double*>(A), lda, 0};
   if (trans == 'T' || trans == 'C') {
@@ -286,6 +335,13 @@ int residual_impl(char side, char uplo, char trans, double alpha, int64_t n, int
   const Mat Xm{const_cast<double*>(X), ldx, 0}, Rm{R, ldr, 0};
   const size_t elems = (size_t)rows * (size_t)cols;
   const unsigned grid = grid_for((int64_t)elems);
+  if (mode == NLA_RESIDUAL_DD) {
+    TraceScope t(NLA_K_RESIDUAL, s, 2.0 * (double)n * (double)elems / 2.0, 8.0 * (double)elems * 4.0);
+    dd_residual_kernel<<<grid_for((int64_t)elems), 256, 0, s>>>(rows, cols, n, A, lda, Am.t, uplo == 'L',
+                                                                side == 'L', X, ldx, B, ldb, alpha, R, ldr);
+    NLA_CHECK_LAUNCH("dd_residual_kernel");
+    return NLA_OK;
+  }
   if (mode == NLA_RESIDUAL_SPLIT) {
     const size_t a_stage = staged_bytes(n, n, EXACT_SLICES), x_stage = staged_bytes(m, n, EXACT_SLICES);
     void* buf = nullptr;

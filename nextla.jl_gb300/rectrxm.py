@@ -341,13 +341,14 @@ def matmul_mixed_(output, input1, input2, alpha=1.0, *, lowp="bf16", split_terms
     return output
 
 
-_RESIDUAL = {"split": _lib.NLA_RESIDUAL_SPLIT, "fp64": _lib.NLA_RESIDUAL_FP64}
+_RESIDUAL = {"split": _lib.NLA_RESIDUAL_SPLIT, "fp64": _lib.NLA_RESIDUAL_FP64, "dd": _lib.NLA_RESIDUAL_DD}
 
 
 def residual_(side, uplo, transpose, alpha, A, X, B, R, *, residual="split"):
     """R = alpha*B - op(A) X (side 'L') or alpha*B - X op(A) (side 'R') for
     Float64 tensors, FP64-accurate (``residual`` 'split': tensor cores with
-    exact slice products; 'fp64': the FP64 pipe)."""
+    exact slice products; 'fp64': the FP64 pipe; 'dd': double-double on the
+    FP64 pipe, rounded once, for measuring backward errors)."""
     _check_flags(side, uplo, transpose, "M")
     a, lda, ta = _mat(A)
     if ta:

@@ -48,18 +48,26 @@ def test_residual_exact_on_integers(pkg, cuda, side):
         np.testing.assert_array_equal(R, ref)
 
 
-def test_residual_against_rationals(pkg, workloads, cuda):
-    """Full 53-bit data: entry error <= 2^-48 * (|op(A)| |X|) + ulp(R)."""
+@pytest.mark.parametrize("mode", ["split", "dd"])
+def test_residual_against_rationals(pkg, workloads, cuda, mode):
+    """Full 53-bit data: entry error <= 2^-48 * (|op(A)| |X|) + ulp(R); the
+    double-double mode with a nearly cancelling right-hand side is checked
+    to 4 ulps of the exact residual itself."""
     n, m = 256, 3
-    A, X = workloads.problem(n, m, "L", "L", seed=12)
+    A, _ = workloads.problem(n, m, "L", "L", seed=12)
     X = np.random.default_rng(5).standard_normal((n, m))
-    B = np.random.default_rng(6).standard_normal((n, m))
-    R = _residual(pkg, cuda, "L", "L", "N", 1.0, A, X, B)
     L = np.tril(A)
+    B = np.random.default_rng(6).standard_normal((n, m))
+    if mode == "dd":
+        B = L @ X + 1e-12 * B  # the residual is ~1e-12 of the terms
+    R = _residual(pkg, cuda, "L", "L", "N", 1.0, A, X, B, mode=mode)
     for j in range(m):
         for i in range(n):
             exact = Fraction(B[i, j]) - sum((Fraction(L[i, k]) * Fraction(X[k, j]) for k in range(i + 1)), Fraction(0))
-            bound = 2.0 ** -48 * float(np.abs(L[i, : i + 1]) @ np.abs(X[: i + 1, j])) + np.spacing(abs(float(exact)))
+            if mode == "dd":
+                bound = 4 * np.spacing(abs(float(exact)))
+            else:
+                bound = 2.0 ** -48 * float(np.abs(L[i, : i + 1]) @ np.abs(X[: i + 1, j])) + np.spacing(abs(float(exact)))
             assert abs(float(Fraction(R[i, j]) - exact)) <= bound, (i, j)
 
 
@@ -76,6 +84,6 @@ def test_residual_all_forms_vs_fp64(pkg, workloads, cuda, side, uplo, trans):
     prod = opA @ X if side == "L" else X @ opA
     ref = -0.5 * B - prod
     scale = np.abs(opA) @ np.abs(X) if side == "L" else np.abs(X) @ np.abs(opA)
-    for mode in ("split", "fp64"):
+    for mode in ("split", "fp64", "dd"):
         R = _residual(pkg, cuda, side, uplo, trans, -0.5, A, X, B, mode=mode)
         assert np.max(np.abs(R - ref) / scale) < 1e-13, mode
