@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--error-table", action="store_true",
                     help="mixed-precision error and speed versus cond(A) (JSON line per configuration)")
     ap.add_argument("--conds", default="1e2,1e4,1e6,1e8")
+    ap.add_argument("--kernel-case", choices=["exact", "fast", "leaf", "dfma"], default=None,
+                    help="run single launches of one kernel on a moderate case (for ncu captures)")
+    ap.add_argument("--case-size", type=int, default=4096)
+    ap.add_argument("--case-reps", type=int, default=2)
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--m", type=int, default=16384)
     ap.add_argument("--cpu-sample", type=int, default=0,
@@ -135,10 +139,6 @@ class ClockSampler:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                 "samples": len(sm)}
-
-
-# Measured DFMA throughput of a GB300 (FP64 FMA loop on every SM).
-DFMA_PEAK_TFLOPS = 1.20
 
 
 def traffic_per_launch():
@@ -339,10 +339,60 @@ def run_error_table(args):
     return 0
 
 
+def run_kernel_case(args):
+    """Single launches of one kernel on an s x s case (s = --case-size),
+    sized so that operands exceed L2 but the device holds a few GB at most:
+      exact  one exact slice-product update, C (s x s) -= A (s x s) B (s x s),
+             7 BF16 slices per operand;
+      fast   the same with 3 BF16 slices (FP32 accumulation);
+      leaf   one FP64 diagonal-block solve of order 128 with 8 s right-hand
+             sides;
+      dfma   one FP64 update on CUDA cores, s x s x s."""
+    import torch
+
+    import __graft_entry__ as graft
+
+    pkg = graft.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    g = torch.Generator(device=dev).manual_seed(0)
+    s = args.case_size
+
+    def cm(r, c):
+        return torch.randn(c, r, generator=g, device=dev, dtype=torch.float64).T
+
+    times = []
+    for _ in range(args.case_reps):
+        if args.kernel_case in ("exact", "fast"):
+            A, B, C = cm(s, s), cm(s, s), cm(s, s)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            pkg.matmul_mixed_(C, A, B, -1.0, split_terms=7 if args.kernel_case == "exact" else 3)
+        elif args.kernel_case == "leaf":
+            n = 128
+            A = cm(n, n).tril_() + 4 * torch.eye(n, device=dev, dtype=torch.float64)
+            A = A.T.contiguous().T
+            B = cm(n, 8 * s)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            pkg.LeftLowerTRSM_(A, B)
+        else:
+            A, B, C = cm(s, s), cm(s, s), cm(s, s)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            pkg.GEMM_SUB_(C, A, B)
+        pkg.device_status()
+        times.append((time.perf_counter() - t0) * 1e3)
+    print(json.dumps({"kernel_case": args.kernel_case, "size": s, "host_ms": times}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.kernel_case:
+        return run_kernel_case(args)
     if args.workload == "batched":
         return run_batched(args)
     if args.error_table:
@@ -487,6 +537,7 @@ def main():
 
     # Roofline of the dominant kernel class.
     pk, pk_kind = peaks()
+    pipes = _lib.measure_pipes(sptr)
     dom = max(trace.items(), key=lambda kv: kv[1][1]) if trace else None
     roofline = None
     gpu_launches = sum(v[0] for v in trace.values())
@@ -502,10 +553,11 @@ def main():
                         "peak_source": "bf16_tflops_sustained of %s MEASURED_PEAKS.json" % pk_kind}
         else:
             # The plain FP64 path runs on the DFMA pipe; no tensor or HBM peak applies.
-            roofline = {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": DFMA_PEAK_TFLOPS,
-                        "unit": "TFLOP/s", "frac": achieved / DFMA_PEAK_TFLOPS, "traffic": None,
+            dfma = pipes["dfma"]
+            roofline = {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": dfma,
+                        "unit": "TFLOP/s", "frac": achieved / dfma, "traffic": None,
                         "launches": launches, "share": share,
-                        "peak_source": "DFMA loop measured on GB300 (profiles/fp64_pipe_probe.md)"}
+                        "peak_source": "DFMA probe measured live (nla_measure_pipes)"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -534,6 +586,7 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": gpu_launches,
             "trace": {k: {"launches": v[0], "ms": v[1], "tflops": v[2] / max(v[1], 1e-9) / 1e9}
                       for k, v in trace.items()},
+            "pipes_tflops": pipes,
             "peaks": pk_kind,
         }
         print(json.dumps(line), flush=True)

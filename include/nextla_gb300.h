@@ -215,6 +215,14 @@ NLA_API int nla_batch_solve(nla_batch_plan plan, double alpha, const void* A_poo
 NLA_API int nla_batch_plan_destroy(nla_batch_plan plan);
 
 /*
+ * Measured throughput (TFLOP/s) of the pipes the plain paths use on the
+ * current GPU (no counterpart in the reference): FP64 FMA on CUDA cores,
+ * FP64 mma.sync m8n8k4, FP32 FMA.  Any output pointer may be NULL.  Runs a
+ * few milliseconds of probe kernels on `stream` and synchronises it.
+ */
+NLA_API int nla_measure_pipes(double* dfma_tflops, double* dmma_tflops, double* ffma_tflops, void* stream);
+
+/*
  * Kernel tracing (no counterpart in the reference, which has no tracing).
  * nla_trace_enable(1) clears earlier records and starts recording; every
  * library kernel launched afterwards is bracketed by CUDA events on its

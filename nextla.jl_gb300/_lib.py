@@ -76,6 +76,16 @@ SIGNATURES.update({
     "nla_batch_plan_destroy": ([_p], _i32),
 })
 
+SIGNATURES["nla_measure_pipes"] = ([ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d), _p], _i32)
+
+
+def measure_pipes(stream=None) -> dict:
+    """{'dfma', 'dmma', 'ffma'}: measured TFLOP/s of those pipes on this GPU."""
+    a, b, c = _d(), _d(), _d()
+    check(load().nla_measure_pipes(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), stream))
+    return {"dfma": a.value, "dmma": b.value, "ffma": c.value}
+
+
 KERNEL_CLASSES = ["leaf_solve", "leaf_mult", "gemm_simt", "gemm_umma", "split", "scale", "residual", "batched"]
 
 _lib = None

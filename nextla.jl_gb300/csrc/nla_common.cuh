@@ -140,11 +140,22 @@ struct Staged {
 size_t staged_bytes(int64_t rows, int64_t K, int S);
 int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bool bf16, int tri, void* buf,
                   Staged* out, cudaStream_t s);
+// The diagonal term and final rounding of a residual computed by the exact
+// update: C := C - P - d_i * X(pos), with d_i = d[i * dstride] (i the row of
+// the staged A operand) and X at the position of C's element.
+struct ResidualTerm {
+  const double* x;
+  int64_t ldx;
+  const double* d;
+  int64_t dstride;
+};
+
 // C (M x N, FP64) += alpha * A * B^T with exact slice-pair accumulation; both
 // operands staged with 7 BF16 slices.  With trans_out the product is added
-// to C^T (C is N x M).
+// to C^T (C is N x M).  With res, the epilogue instead forms a residual
+// (alpha is then -1 implicitly), rounding once.
 int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat& C, bool trans_out,
-                      cudaStream_t s);
+                      cudaStream_t s, const ResidualTerm* res = nullptr);
 constexpr int EXACT_SLICES = 7;
 int workspace_get(cudaStream_t s, size_t bytes, void** out);
 int device_status(cudaStream_t s);

@@ -26,6 +26,15 @@ __global__ void __launch_bounds__(LEAF_THREADS) leaf_solve_kernel(LeafArgs g) {
   solve_block<T, CW>(g, c0, ncols, smem_raw, typename Elem<T>::compute(1));
 }
 
+// Wide blocks of right-hand sides, one per thread in the panel solves.
+template <typename T, int CW>
+__global__ void __launch_bounds__(LEAF_THREADS) leaf_solve_wide_kernel(LeafArgs g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t c0 = (int64_t)blockIdx.x * CW;
+  const int ncols = (int)(g.m - c0 < CW ? g.m - c0 : CW);
+  solve_block_wide<T, CW>(g, c0, ncols, smem_raw, typename Elem<T>::compute(1));
+}
+
 // Canonical lower-left multiply: X := L X for CW columns.
 template <typename T, int CW>
 __global__ void __launch_bounds__(LEAF_THREADS) leaf_mult_kernel(LeafArgs g) {
@@ -110,6 +119,48 @@ int launch_leaf_t(char func, const LeafArgs& g, cudaStream_t s) {
   return NLA_OK;
 }
 
+template <typename T, int CW>
+int launch_leaf_wide(const LeafArgs& g, cudaStream_t s) {
+  using Tc = typename Elem<T>::compute;
+  const size_t smem = leaf_solve_smem_elems(g.n, CW) * sizeof(Tc);
+  const int64_t grid = (g.m + CW - 1) / CW;
+  if (smem > 200 * 1024) return fail(NLA_ERR_UNSUPPORTED, "leaf: shared memory plan too large");
+  static std::once_flag once;
+  static cudaError_t st = cudaSuccess;
+  std::call_once(once, [] {
+    st = cudaFuncSetAttribute(leaf_solve_wide_kernel<T, CW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              200 * 1024);
+  });
+  if (st != cudaSuccess) return cuda_status(st, "cudaFuncSetAttribute(leaf_solve_wide_kernel)");
+  TraceScope trace(NLA_K_LEAF_SOLVE, s, (double)g.n * g.n * (double)g.m,
+                   (double)sizeof(T) * ((double)g.n * (g.n + 1) / 2 + 2.0 * (double)g.n * g.m));
+  leaf_solve_wide_kernel<T, CW><<<(unsigned)grid, LEAF_THREADS, smem, s>>>(g);
+  NLA_CHECK_LAUNCH("leaf_solve_wide_kernel");
+  return NLA_OK;
+}
+
+// Wide solve blocks: the widest of 128/64/32 right-hand sides whose block
+// fits 128 KiB of shared memory and still gives two CTAs per SM; 0 when the
+// row-parallel kernel is the better choice (few right-hand sides).
+int wide_cols(int64_t n, int64_t m, size_t elem) {
+  if (m < 32) return 0;
+  const int64_t want = 2 * (int64_t)num_sms();
+  for (int cw : {128, 64, 32}) {
+    if ((size_t)n * cw * elem > 128 * 1024) continue;
+    if ((m + cw - 1) / cw >= want || cw == 32) return cw;
+  }
+  return 0;
+}
+
+template <typename T>
+int launch_solve_wide(const LeafArgs& g, int cw, cudaStream_t s) {
+  switch (cw) {
+    case 128: return launch_leaf_wide<T, 128>(g, s);
+    case 64: return launch_leaf_wide<T, 64>(g, s);
+    default: return launch_leaf_wide<T, 32>(g, s);
+  }
+}
+
 }  // namespace
 
 int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m, const Mat& A, const Mat& B,
@@ -132,6 +183,17 @@ int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m
     uplo = uplo == 'L' ? 'U' : 'L';
   }
   g.rev = uplo == 'U';
+  if (func == 'S') {
+    const int cw = wide_cols(n, m, dtype == NLA_F64 ? 8 : 4);
+    if (cw) {
+      switch (dtype) {
+        case NLA_F64: return launch_solve_wide<double>(g, cw, s);
+        case NLA_F32: return launch_solve_wide<float>(g, cw, s);
+        case NLA_F16: return launch_solve_wide<__half>(g, cw, s);
+        default: break;
+      }
+    }
+  }
   switch (dtype) {
     case NLA_F64:
       return n <= 512 ? launch_leaf_t<double, 16>(func, g, s) : launch_leaf_t<double, 8>(func, g, s);

@@ -203,6 +203,98 @@ __device__ __forceinline__ void solve_block(const LeafArgs& g, int64_t c0, int n
   store_block<T, Tc, CW>(g, X, c0, ncols);
 }
 
+// Xo[r, :] -= sum_kk slab[r][kk] * Xp[kk, :] for r < rows, kk < pw, for wide
+// column blocks: LEAF_THREADS threads as RG row groups x (LEAF_THREADS / RG)
+// column groups, each thread a 4-row x CT-column register tile (rows strided
+// by RG so that slab reads are conflict-free).  rows <= 4 * RG.
+template <typename Tc, int CW, int RG>
+__device__ __forceinline__ void trailing_update_wide(const Tc* __restrict__ slab, const Tc* __restrict__ Xp,
+                                                     Tc* __restrict__ Xo, int rows, int pw) {
+  constexpr int CG = LEAF_THREADS / RG;
+  constexpr int CT = CW / CG;
+  const int tr = threadIdx.x % RG, tc = threadIdx.x / RG;
+  Tc acc[4][CT];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int c = 0; c < CT; ++c) acc[i][c] = Tc(0);
+  for (int kk = 0; kk < pw; ++kk) {
+    Tc a[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = slab[(tr + RG * i) * SLAB_PAD + kk];
+    const Tc* xr = Xp + kk * CW + tc * CT;
+#pragma unroll
+    for (int c = 0; c < CT; ++c) {
+      const Tc xv = xr[c];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i][c] = fma(a[i], xv, acc[i][c]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = tr + RG * i;
+    if (r < rows) {
+      Tc* xo = Xo + r * CW + tc * CT;
+#pragma unroll
+      for (int c = 0; c < CT; ++c) xo[c] -= acc[i][c];
+    }
+  }
+}
+
+// Canonical lower-left solve for wide column blocks (CW in {16, 32, 64, 128}):
+// the same panels as solve_block, but each panel's 32 x 32 triangle is solved
+// with one right-hand side per thread (threads < CW), as a fully unrolled
+// dot product against the panel's already-solved values in registers, so
+// every lane does useful work and no value has to cross lanes.
+template <typename T, int CW>
+__device__ __forceinline__ void solve_block_wide(const LeafArgs& g, int64_t c0, int ncols, unsigned char* smem_raw,
+                                                 typename Elem<T>::compute alpha) {
+  using Tc = typename Elem<T>::compute;
+  constexpr int RG = CW >= 128 ? 16 : 32;  // row groups of the trailing update
+  constexpr int CHUNK = 4 * RG;            // rows per trailing-update pass
+  Tc* X = reinterpret_cast<Tc*>(smem_raw);            // n x CW
+  Tc* inv_d = X + (size_t)g.n * CW;                   // n
+  Tc* slab = inv_d + g.n;                             // 128 x 33
+  Tc* diag = slab + LEAF_THREADS * SLAB_PAD;          // 32 x 33
+  const int n = g.n;
+  const T* A = static_cast<const T*>(g.A);
+
+  load_block<T, Tc, CW>(g, X, c0, ncols, alpha);
+  for (int i = threadIdx.x; i < n; i += LEAF_THREADS) inv_d[i] = Tc(1) / Elem<T>::load(A + a_off<T>(g, i, i));
+  __syncthreads();
+
+  const int t = threadIdx.x;
+  for (int p0 = 0; p0 < n; p0 += PANEL) {
+    const int pw = min(PANEL, n - p0);
+    stage_slab<PANEL, T>(g, diag, p0, pw, p0, pw, [](int i, int j) { return j < i; });
+    __syncthreads();
+    if (t < CW) {
+      Tc x[PANEL];
+#pragma unroll
+      for (int r = 0; r < PANEL; ++r) {
+        if (r < pw) {
+          Tc y = X[(p0 + r) * CW + t];
+#pragma unroll
+          for (int j = 0; j < r; ++j) y = fma(-diag[r * SLAB_PAD + j], x[j], y);
+          y *= inv_d[p0 + r];
+          x[r] = y;
+          X[(p0 + r) * CW + t] = y;
+        }
+      }
+    }
+    __syncthreads();
+    for (int r0 = p0 + pw; r0 < n; r0 += CHUNK) {
+      const int rows = min(CHUNK, n - r0);
+      stage_slab<CHUNK, T>(g, slab, r0, rows, p0, pw, [](int, int) { return true; });
+      __syncthreads();
+      trailing_update_wide<Tc, CW, RG>(slab, X + (size_t)p0 * CW, X + (size_t)r0 * CW, rows, pw);
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  store_block<T, Tc, CW>(g, X, c0, ncols);
+}
+
 __host__ __device__ constexpr size_t leaf_solve_smem_elems(int n, int CW) {
   return (size_t)n * CW + (size_t)n + (size_t)LEAF_THREADS * SLAB_PAD + (size_t)PANEL * SLAB_PAD;
 }

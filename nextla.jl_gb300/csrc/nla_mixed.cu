@@ -93,19 +93,6 @@ __global__ void correct_kernel(int64_t rows, int64_t cols, const double* __restr
   }
 }
 
-// R -= diag(A) X (side L) or X diag(A) (side R), in FP64.
-__global__ void diag_residual_kernel(int64_t rows, int64_t cols, const double* __restrict__ A, int64_t lda,
-                                     int left, const double* __restrict__ X, int64_t ldx, double* __restrict__ R,
-                                     int64_t ldr) {
-  const int64_t total = rows * cols;
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = idx % rows, j = idx / rows;
-    const double d = left ? A[i + i * lda] : A[j + j * lda];
-    R[i + j * ldr] = fma(-d, X[i + j * ldx], R[i + j * ldr]);
-  }
-}
-
 __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
   s = a + b;
   const double bp = s - a;
@@ -178,24 +165,21 @@ int stage_triangle(const Mat& Am, int64_t n, char side, char uplo, void* buf, St
   return stage_operand(transposed(Am), n, n, NLA_F64, EXACT_SLICES, true, uplo == 'L' ? 4 : 3, buf, out, s);
 }
 
-// R -= op(A) X (side L) or X op(A) (side R) with exact slice products for the
-// strict triangle (As, staged by stage_triangle) and FP64 for the diagonal.
+// R -= op(A) X (side L) or X op(A) (side R): exact slice products for the
+// strict triangle (As, staged by stage_triangle); the diagonal term and the
+// subtraction are folded into the exact kernel's epilogue (one rounding).
 int split_residual(const Mat& Am, const Staged& As, char side, int64_t n, int64_t m, const Mat& Xm, const Mat& Rm,
-                   void* xbuf, Staged* Xs, unsigned grid, cudaStream_t s) {
-  const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
+                   void* xbuf, Staged* Xs, cudaStream_t s) {
+  // The epilogue subtracts the exact strict-triangle product and the FP64
+  // diagonal term from R (= alpha*B on entry) and rounds once.
+  const ResidualTerm term{static_cast<const double*>(Xm.p), Xm.ld, static_cast<const double*>(Am.p), Am.ld + 1};
   if (side == 'L') {  // op(A) (n x n) times X (n x m): B-operand rows are X's columns
     NLA_TRY(stage_operand(transposed(Xm), m, n, NLA_F64, EXACT_SLICES, true, 0, xbuf, Xs, s));
-    NLA_TRY(launch_exact_gemm(As, *Xs, -1.0, Rm, false, s));
-  } else {  // (X op(A))^T = op(A)^T X^T: B-operand rows are X's rows; written transposed
-    NLA_TRY(stage_operand(Xm, m, n, NLA_F64, EXACT_SLICES, true, 0, xbuf, Xs, s));
-    NLA_TRY(launch_exact_gemm(As, *Xs, -1.0, Rm, true, s));
+    return launch_exact_gemm(As, *Xs, -1.0, Rm, false, s, &term);
   }
-  TraceScope t(NLA_K_RESIDUAL, s, 2.0 * (double)rows * cols, 24.0 * (double)rows * cols);
-  diag_residual_kernel<<<grid, 256, 0, s>>>(rows, cols, static_cast<const double*>(Am.p), Am.ld, side == 'L',
-                                            static_cast<const double*>(Xm.p), Xm.ld, static_cast<double*>(Rm.p),
-                                            Rm.ld);
-  NLA_CHECK_LAUNCH("diag_residual_kernel");
-  return NLA_OK;
+  // (X op(A))^T = op(A)^T X^T: B-operand rows are X's rows; written transposed
+  NLA_TRY(stage_operand(Xm, m, n, NLA_F64, EXACT_SLICES, true, 0, xbuf, Xs, s));
+  return launch_exact_gemm(As, *Xs, -1.0, Rm, true, s, &term);
 }
 
 int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, int64_t n, int64_t m,
@@ -280,7 +264,7 @@ int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, i
         copy_kernel<<<grid, 256, 0, s>>>(rows, cols, B0, rows, R, rows);
         NLA_CHECK_LAUNCH("copy_kernel");
       }
-      NLA_TRY(split_residual(Am, As, side, n, m, Bm, Rm, stage_base + a_stage, &Xs, grid, s));
+      NLA_TRY(split_residual(Am, As, side, n, m, Bm, Rm, stage_base + a_stage, &Xs, s));
     } else {
       {
         TraceScope t(NLA_K_RESIDUAL, s, 0.0, 16.0 * (double)elems);
@@ -352,7 +336,7 @@ int residual_impl(char side, char uplo, char trans, double alpha, int64_t n, int
     NLA_TRY(launch_scale(NLA_F64, rows, cols, alpha, Rm, s));
     Staged As{}, Xs{};
     NLA_TRY(stage_triangle(Am, n, side, uplo, base, &As, s));
-    return split_residual(Am, As, side, n, m, Xm, Rm, base + a_stage, &Xs, grid, s);
+    return split_residual(Am, As, side, n, m, Xm, Rm, base + a_stage, &Xs, s);
   }
   // FP64 pipe: R = op(A) X by the plain recursion, then R = alpha*B - R.
   void* buf = nullptr;

@@ -265,6 +265,12 @@ struct ExactParams {
   int tri_a, tri_b;  // staged triangle of each operand (see in_tri)
   int trans_out;     // write the product transposed: element (i, j) to C[j + i*ldc]
   const float* nrm_a;  // per-row slice-magnitude sums of A (headroom of the fixed point)
+  // Residual epilogue (when res_x is set): C := C - P - d_i * X(pos), with
+  // d_i = res_d[i * res_dstride] and X at the position of C's element.
+  const double* res_x;
+  int64_t res_ldx;
+  const double* res_d;
+  int64_t res_dstride;
   void* C;
   int64_t ldc;
   double alpha;
@@ -285,6 +291,12 @@ __device__ __forceinline__ double scale_pow2(double d, int e) {
   const int ne = E + e;
   if (E == 0 || E == 0x7FF || ne <= 0 || ne >= 2047) return ldexp(d, e);
   return __longlong_as_double((long long)((b & ~(0x7FFull << 52)) | ((unsigned long long)ne << 52)));
+}
+
+__device__ __forceinline__ void two_sum_dev(double a, double b, double& s, double& e) {
+  s = a + b;
+  const double bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
 }
 
 __global__ void __launch_bounds__(EX_THREADS, 1)
@@ -447,9 +459,25 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
         const int ej = p.eb[col];
         if (row_nan || ej == NONFINITE_EXP) {
           *cp = __longlong_as_double(0x7ff8000000000000ull);
-        } else {
+        } else if (p.res_x == nullptr) {
           const double d = scale_pow2(__ll2double_rn(acc[j]), ei + max(ej, -4000) - Lb);
           *cp = fma(p.alpha, d, *cp);
+        } else {
+          // Residual epilogue: C := C - P - d_i x with P exact in acc, formed
+          // with error-free transformations and rounded once.
+          const int e = ei + max(ej, -4000) - Lb;
+          const double hi_u = __ll2double_rn(acc[j]);
+          const double lo_u = __ll2double_rn(acc[j] - (long long)hi_u);
+          const double s_hi = scale_pow2(hi_u, e), s_lo = scale_pow2(lo_u, e);
+          const double dg = p.res_d[(int64_t)i * p.res_dstride];
+          const double xv = p.res_x[p.trans_out ? (int64_t)col + (int64_t)i * p.res_ldx
+                                                : (int64_t)i + (int64_t)col * p.res_ldx];
+          const double pr = dg * xv;
+          const double pe = fma(dg, xv, -pr);
+          double t1, e1, t2, e2;
+          two_sum_dev(*cp, -s_hi, t1, e1);
+          two_sum_dev(t1, -pr, t2, e2);
+          *cp = t2 + (((e1 + e2) - pe) - s_lo);
         }
       }
     }
@@ -841,7 +869,7 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
 // C (M x N, FP64) += alpha * A * B^T from two operands staged with
 // EX_SLICES BF16 slices (A: M rows, B: N rows, same K).
 int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat& C, bool trans_out,
-                      cudaStream_t s) {
+                      cudaStream_t s, const ResidualTerm* res) {
   const int64_t M = A.rows, N = B.rows, K = A.K;
   if (M <= 0 || N <= 0 || K <= 0) return NLA_OK;
   if (B.K != K || A.S != EX_SLICES || B.S != EX_SLICES || !A.bf16 || !B.bf16 || !A.scaled || !B.scaled)
@@ -870,6 +898,12 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
   p.tri_b = B.tri;
   p.trans_out = trans_out ? 1 : 0;
   p.nrm_a = A.nrm;
+  if (res) {
+    p.res_x = res->x;
+    p.res_ldx = res->ldx;
+    p.res_d = res->d;
+    p.res_dstride = res->dstride;
+  }
   p.C = C.p;
   p.ldc = C.ld;
   p.alpha = alpha;
