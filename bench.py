@@ -64,6 +64,11 @@ def parse():
     ap.add_argument("--error-table", action="store_true",
                     help="mixed-precision error and speed versus cond(A) (JSON line per configuration)")
     ap.add_argument("--conds", default="1e2,1e4,1e6,1e8")
+    ap.add_argument("--config3", action="store_true",
+                    help="mixed TRMM R/U/T n=12288 (3-term BF16) and Float16 TRSM n=8192 m=4096, vs FP64")
+    ap.add_argument("--sweep-plain", action="store_true",
+                    help="plain F32/F64 TRSM and TRMM over the 8 side/uplo/trans forms, alpha 0.5 (config 1)")
+    ap.add_argument("--sizes", default="4096,8192,16384")
     ap.add_argument("--kernel-case", choices=["exact", "fast", "leaf", "dfma"], default=None,
                     help="run single launches of one kernel on a moderate case (for ncu captures)")
     ap.add_argument("--case-size", type=int, default=4096)
@@ -339,6 +344,147 @@ def run_error_table(args):
     return 0
 
 
+def run_sweep_plain(args):
+    """Dtype-preserving TRSM and TRMM in Float32 and Float64 over all 8
+    side/uplo/trans forms (trans N, T), alpha = 0.5, B n x n uniform[-1, 1],
+    A built as in config 0 (seeded): one JSON line per case with the
+    device time, n^3 flop rate and the relative error of 64 sampled columns
+    against an FP64 (double-double residual for solves) check."""
+    import itertools
+
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as graft
+
+    pkg = graft.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    for n in [int(x) for x in args.sizes.split(",")]:
+        rng = np.random.default_rng(n)
+        Z = rng.standard_normal((n, n)) / np.sqrt(n)
+        d = 2.0 + np.abs(rng.standard_normal(n))
+        B_h = rng.uniform(-1.0, 1.0, (n, n))
+        B64 = torch.from_numpy(np.ascontiguousarray(B_h.T)).to(dev).T
+        for uplo in "LU":
+            T = np.tril(Z, -1) if uplo == "L" else np.triu(Z, 1)
+            T[np.diag_indices(n)] = d
+            A64 = torch.from_numpy(np.ascontiguousarray(T.T)).to(dev).T
+            del T
+            for dtype, side, trans, func in itertools.product([torch.float32, torch.float64], "LR", "NT", "SM"):
+                A = A64.to(dtype).T.contiguous().T
+                B0 = B64.to(dtype).T.contiguous().T
+                X = torch.empty_like(B0.T).T
+                X.copy_(B0)
+                pkg.unified_rectrxm_(side, uplo, trans, 0.5, func, A, X, native=True)  # warm-up
+                X.copy_(B0)
+                torch.cuda.synchronize(dev)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                pkg.unified_rectrxm_(side, uplo, trans, 0.5, func, A, X, native=True)
+                e1.record()
+                torch.cuda.synchronize(dev)
+                ms = e0.elapsed_time(e1)
+                # accuracy on sampled columns (rows for side R) in FP64
+                idx = torch.arange(0, n, max(1, n // 64), device=dev)
+                opA = (torch.tril(A64) if uplo == "L" else torch.triu(A64))
+                opA = opA.T if trans == "T" else opA
+                if side == "L":
+                    Xs, Bs = X[:, idx].double(), B64[:, idx]
+                    lhs = opA @ Xs if func == "S" else Xs
+                    rhs = 0.5 * Bs if func == "S" else 0.5 * (opA @ Bs)
+                else:
+                    Xs, Bs = X[idx, :].double(), B64[idx, :]
+                    lhs = Xs @ opA if func == "S" else Xs
+                    rhs = 0.5 * Bs if func == "S" else 0.5 * (Bs @ opA)
+                rel = float(torch.linalg.norm(lhs - rhs) / torch.linalg.norm(rhs))
+                print(json.dumps({"n": n, "dtype": str(dtype).split(".")[-1], "func": func, "side": side,
+                                  "uplo": uplo, "trans": trans, "ms": ms,
+                                  "tflops": float(n) ** 3 / (ms / 1e3) / 1e12, "rel_check": rel}), flush=True)
+                del A, B0, X
+            del A64
+        del B64
+    return 0
+
+
+def run_config3(args):
+    """(1) TRMM side R, uplo U, trans T, n = 12288, B 12288 x 12288 Float64,
+    updates from 3-term BF16 splits (FP64 diagonal blocks), against the plain
+    FP64 TRMM of the same inputs; (2) TRSM L/L/N with Float16 A and B,
+    n = 8192, m = 4096 (A: diagonal 2+|N(0,1)|, off-diagonals N(0,1)/sqrt(n)),
+    Float16 updates on tensor cores with FP32 accumulation, against an FP64
+    solve of the same (Float16-rounded) inputs."""
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as graft
+
+    pkg = graft.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1)
+
+    n = 12288
+    rng = np.random.default_rng(3)
+    T = np.triu(rng.standard_normal((n, n)) / np.sqrt(n), 1)
+    T[np.diag_indices(n)] = 2.0 + np.abs(rng.standard_normal(n))
+    A = torch.from_numpy(np.ascontiguousarray(T.T)).to(dev).T
+    del T
+    B0 = torch.from_numpy(np.ascontiguousarray(rng.uniform(-1, 1, (n, n)).T)).to(dev).T
+    ref = torch.empty_like(B0.T).T
+
+    def plain():
+        ref.copy_(B0)
+        pkg.unified_rectrxm_("R", "U", "T", 1.0, "M", A, ref, native=True)
+
+    pms = timed(plain)
+    X = torch.empty_like(B0.T).T
+
+    def mixed():
+        X.copy_(B0)
+        pkg.unified_rectrxm_mixed_("R", "U", "T", 1.0, "M", A, X, lowp="bf16", split_terms=3)
+
+    ms = timed(mixed)
+    rel = float(torch.linalg.norm(X - ref) / torch.linalg.norm(ref))
+    flops = float(n) ** 3
+    print(json.dumps({"case": "trmm_RUT_f64_mixed_bf16x3_n12288", "ms": ms, "tflops": flops / ms / 1e9,
+                      "plain_fp64_ms": pms, "plain_fp64_tflops": flops / pms / 1e9, "rel_err_vs_fp64": rel}),
+          flush=True)
+    del A, B0, ref, X
+
+    n, m = 8192, 4096
+    rng = np.random.default_rng(4)
+    T = np.tril(rng.standard_normal((n, n)) / np.sqrt(n), -1)
+    T[np.diag_indices(n)] = 2.0 + np.abs(rng.standard_normal(n))
+    A16 = torch.from_numpy(np.ascontiguousarray(T.T)).to(dev).T.half().T.contiguous().T
+    del T
+    B16 = torch.from_numpy(np.ascontiguousarray(rng.uniform(-1, 1, (n, m)).T)).to(dev).T.half().T.contiguous().T
+    X16 = torch.empty_like(B16.T).T
+
+    def f16():
+        X16.copy_(B16)
+        pkg.unified_rectrxm_("L", "L", "N", 1.0, "S", A16, X16, native=True)
+
+    ms = timed(f16)
+    A64 = A16.double().T.contiguous().T
+    X64 = B16.double().T.contiguous().T
+    pkg.unified_rectrxm_("L", "L", "N", 1.0, "S", A64, X64, native=True)
+    torch.cuda.synchronize(dev)
+    rel = float(torch.linalg.norm(X16.double() - X64) / torch.linalg.norm(X64))
+    print(json.dumps({"case": "trsm_LLN_f16_n8192_m4096", "ms": ms, "tflops": float(n) * n * m / ms / 1e9,
+                      "rel_err_vs_fp64": rel, "unit_roundoff_f16": 2.0 ** -11}), flush=True)
+    return 0
+
+
 def run_kernel_case(args):
     """Single launches of one kernel on an s x s case (s = --case-size),
     sized so that operands exceed L2 but the device holds a few GB at most:
@@ -393,6 +539,10 @@ def main():
         return run_reference(args)
     if args.kernel_case:
         return run_kernel_case(args)
+    if args.sweep_plain:
+        return run_sweep_plain(args)
+    if args.config3:
+        return run_config3(args)
     if args.workload == "batched":
         return run_batched(args)
     if args.error_table:
