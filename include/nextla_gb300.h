@@ -172,6 +172,27 @@ NLA_API int nla_trxm_residual(char side, char uplo, char trans, double alpha, in
                               int64_t ldr, int residual, void* stream);
 
 /*
+ * nla_gemm_update_mixed without any device allocation.  No counterpart in the
+ * reference (which allocates nothing itself but has no mixed form).
+ * Some callers cannot let a library call cudaMalloc: a host framework that
+ * owns all device memory through its own allocator, a process held to a fixed
+ * device-memory budget, or a latency-critical loop that cannot absorb an
+ * allocation.  This entry point stages its operands in a static device array
+ * of NLA_NOALLOC_SCRATCH_BYTES that the library defines (held by every GPU
+ * that loads the library until the process exits) instead of the pooled
+ * workspace.  Updates whose staging would exceed that size fail with
+ * NLA_ERR_WORKSPACE: with 3 slices, for example, about (N + M) * R <= 11e6
+ * once N, M are rounded up to 128 and R to 64.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (concurrent streams or unordered host threads) race.
+ */
+#define NLA_NOALLOC_SCRATCH_BYTES (64ll << 20)
+NLA_API int nla_gemm_update_mixed_noalloc(int trans1, int trans2, int64_t N, int64_t R, int64_t M, double alpha,
+                                          const double* in1, int64_t ld1, const double* in2, int64_t ld2,
+                                          double* out, int64_t ldo, int lowp, int split_terms, void* stream);
+
+/*
  * Synchronises `stream` and reports (then clears) the device-side error word
  * that the tensor-core kernels raise when a bounded wait gives up:
  * NLA_OK or NLA_ERR_TIMEOUT.

@@ -56,7 +56,10 @@ SIGNATURES.update({
                               _i32),
     "nla_device_status": ([_p], _i32),
     "nla_trxm_residual": ([_c, _c, _c, _d, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _i32, _p], _i32),
+    "nla_gemm_update_mixed_noalloc": ([_i32, _i32, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _p, _i64, _i32, _i32,
+                                       _p], _i32),
 })
+NLA_NOALLOC_SCRATCH_BYTES = 64 << 20
 
 class BatchDesc(ctypes.Structure):
     """nla_batch_desc of include/nextla_gb300.h."""
