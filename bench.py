@@ -76,7 +76,7 @@ def parse():
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--m", type=int, default=16384)
     ap.add_argument("--cpu-sample", type=int, default=0,
-                    help="right-hand sides in the CPU sample (0: 16 per host thread)")
+                    help="right-hand sides in the CPU sample (0: 128 per host thread)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -190,7 +190,7 @@ def run_reference(args):
     import numpy as np
 
     threads = os.cpu_count() or 1
-    cols = args.cpu_sample or 16 * threads
+    cols = args.cpu_sample or 128 * threads
     A, B = make_inputs(args.n, args.m)
     vals = []
     for i in range(args.warmup + args.steps):
@@ -642,9 +642,11 @@ def main():
         pkg.residual_("L", "L", "N", 1.0, A, Xs_, Bs_, Rs_, residual="dd")
         torch.cuda.synchronize(dev)
         an = float(torch.tril(A).abs().sum(dim=1).max())
-        return float(Rs_.abs().sum(dim=1).max() / (an * Xs_.abs().sum(dim=1).max() * n * 2.0 ** -53))
+        rn = float(Rs_.abs().sum(dim=1).max())
+        xn = float(Xs_.abs().sum(dim=1).max())
+        return rn / (an * xn * n * 2.0 ** -53), {"r_inf": rn, "a_inf": an, "x_inf": xn}
 
-    berr = backward_error(B)
+    berr, berr_parts = backward_error(B)
     plain = None
     if args.variant == "mixed" and not args.no_plain:
         Bp = torch.empty_like(B0.T).T
@@ -658,7 +660,8 @@ def main():
         p1.record(stream)
         barrier()
         pms = p0.elapsed_time(p1)
-        plain = {"tflops": flops / (pms / 1e3) / 1e12, "ms": pms, "backward_error": backward_error(Bp),
+        pb, pparts = backward_error(Bp)
+        plain = {"tflops": flops / (pms / 1e3) / 1e12, "ms": pms, "backward_error": pb, "norms": pparts,
                  "steps": 1}
         del Bp
 
@@ -712,7 +715,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        sample = args.cpu_sample or 16 * threads
+        sample = args.cpu_sample or 128 * threads
         v, dt = cpu_baseline(A_h, B_h, sample, threads)
         cpu = {"value": v, "unit": "TFLOP/s", "cores": threads, "kind": "port",
                "sample": "%d of %d right-hand sides, full %dx%d A, %.1f s" % (sample, m, n, n, dt)}
@@ -728,7 +731,9 @@ def main():
                                   "residual": args.residual, "cutoff": args.cutoff or "default"}
                                  if args.variant == "mixed" else None),
                        "l2": "inputs larger than L2", "parallelism": "replicas" if world > 1 else "single"},
-            "accuracy": {"backward_error": berr, "definition": "||AX-B||_inf/(||A||_inf ||X||_inf n u), 64 cols"},
+            "accuracy": {"backward_error": berr, "norms": berr_parts,
+                         "definition": "||AX-B||_inf/(||A||_inf ||X||_inf n u), 64 sampled columns, "
+                                       "residual in double-double"},
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (value / plain["tflops"]) if plain else None,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": int(A_h.nbytes + B_h.nbytes),

@@ -238,8 +238,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 //
 // Operands are staged as S = 7 BF16 slices of integers |s| <= 128, so one
 // slice pair's products are exact and their FP32 sum over a chunk of <= 1024
-// values (|sum| <= 2^24) is exact in TMEM.  Each pair runs through the K range
-// in such chunks into one of two TMEM buffers (double-buffered); eight
+// values (|sum| <= 2^24) is exact in TMEM.  K is walked in 1024-value chunks
+// (outer loop, so all CTAs of a wave share a small working set in L2) and,
+// inside each chunk, every slice pair accumulates into one of two TMEM
+// buffers (double-buffered); eight
 // epilogue warps drain each chunk, convert it to integers and add it, shifted
 // by the pair's weight 2^(-8(p+q)), into 64-bit fixed-point accumulators held
 // in registers.  FP64 arithmetic is used once per output element, for the
@@ -351,19 +353,23 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   if (warp == 0) {
     if (lane == 0) {
       int it = 0;
-      for (int pr = 0; pr < p.npairs && ok; ++pr) {
-        for (int kb = kb0; kb < kb1; ++kb, ++it) {
-          const int s = it % EX_STAGES;
-          const uint32_t round = (uint32_t)(it / EX_STAGES);
-          if (!umma::mbar_wait(umma::smem_u32(&empty[s]), (round & 1u) ^ 1u, &s_abort, &g_device_error, 11)) {
-            ok = false;
-            break;
+      for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
+        const int c0 = max(kb0, cc * EX_CHUNK), c1 = min(kb1, (cc + 1) * EX_CHUNK);
+        if (c0 >= c1) continue;  // empty K range (the operands' triangles miss each other)
+        for (int pr = 0; pr < p.npairs && ok; ++pr) {
+          for (int kb = c0; kb < c1; ++kb, ++it) {
+            const int s = it % EX_STAGES;
+            const uint32_t round = (uint32_t)(it / EX_STAGES);
+            if (!umma::mbar_wait(umma::smem_u32(&empty[s]), (round & 1u) ^ 1u, &s_abort, &g_device_error, 11)) {
+              ok = false;
+              break;
+            }
+            const uint32_t fb = umma::smem_u32(&full[s]);
+            umma::mbar_arrive_expect_tx(fb, (uint32_t)EX_STAGE_BYTES);
+            uint8_t* st = smem + s * EX_STAGE_BYTES;
+            umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, p.pa[pr] * p.a_rows + m0);
+            umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), &tmB, fb, kb * BK, p.pb[pr] * p.b_rows + n0);
           }
-          const uint32_t fb = umma::smem_u32(&full[s]);
-          umma::mbar_arrive_expect_tx(fb, (uint32_t)EX_STAGE_BYTES);
-          uint8_t* st = smem + s * EX_STAGE_BYTES;
-          umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, p.pa[pr] * p.a_rows + m0);
-          umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), &tmB, fb, kb * BK, p.pb[pr] * p.b_rows + n0);
         }
       }
     }
@@ -371,8 +377,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     if (lane == 0) {
       const uint32_t idesc = umma::idesc_f16(BM, BN, true);
       int it = 0, ch = 0;
-      for (int pr = 0; pr < p.npairs && ok; ++pr) {
-        for (int c0 = kb0; c0 < kb1 && ok; c0 += EX_CHUNK, ++ch) {
+      for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
+        const int c0 = max(kb0, cc * EX_CHUNK), c1 = min(kb1, (cc + 1) * EX_CHUNK);
+        if (c0 >= c1) continue;
+        for (int pr = 0; pr < p.npairs && ok; ++pr, ++ch) {
           const int b = ch & 1;
           const uint32_t use = (uint32_t)(ch >> 1);
           if (!umma::mbar_wait(umma::smem_u32(&cempty[b]), (use & 1u) ^ 1u, &s_abort, &g_device_error, 12)) {
@@ -380,7 +388,6 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
             break;
           }
           umma::fence_after_sync();
-          const int c1 = min(c0 + EX_CHUNK, kb1);
           for (int kb = c0; kb < c1; ++kb, ++it) {
             const int s = it % EX_STAGES;
             const uint32_t round = (uint32_t)(it / EX_STAGES);
@@ -421,9 +428,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
       Lb = min(max(Lb, 0), 77);
     }
     int ch = 0;
-    for (int pr = 0; pr < p.npairs && ok; ++pr) {
-      const int sh = Lb - 8 * (p.pa[pr] + p.pb[pr] + 2);
-      for (int c0 = kb0; c0 < kb1; c0 += EX_CHUNK, ++ch) {
+    for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
+      if (max(kb0, cc * EX_CHUNK) >= min(kb1, (cc + 1) * EX_CHUNK)) continue;
+      for (int pr = 0; pr < p.npairs && ok; ++pr, ++ch) {
+        const int sh = Lb - 8 * (p.pa[pr] + p.pb[pr] + 2);
         const int b = ch & 1;
         const uint32_t use = (uint32_t)(ch >> 1);
         ok = __all_sync(0xffffffffu,
