@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(LEAF_THREADS) leaf_mult_kernel(LeafArgs g) {
       const int kw = min(PANEL, kmax - k0);
       stage_slab<LEAF_THREADS, T>(g, slab, r0, rows, k0, kw, [](int i, int j) { return j <= i; });
       __syncthreads();
-      tile_product<Tc, CW>(slab, X + (size_t)k0 * CW, kw, acc);
+      tile_product<Tc, CW>(slab, X + (size_t)k0 * CW, kw, rows, acc);
       __syncthreads();
     }
 #pragma unroll
@@ -159,6 +159,13 @@ int launch_solve_wide(const LeafArgs& g, int cw, cudaStream_t s) {
     case 64: return launch_leaf_wide<T, 64>(g, s);
     default: return launch_leaf_wide<T, 32>(g, s);
   }
+}
+
+// Float64 register tiles wider than 32 columns do not fit the register file
+// without spilling, so Float64 uses 32-column blocks.
+template <>
+int launch_solve_wide<double>(const LeafArgs& g, int, cudaStream_t s) {
+  return launch_leaf_wide<double, 32>(g, s);
 }
 
 }  // namespace

@@ -98,23 +98,26 @@ __device__ __forceinline__ void store_block(const LeafArgs& g, const Tc* X, int6
 // kk < pw: LEAF_THREADS threads as 32 row lanes (tr) x 4 column groups (tc,
 // one warp each, so the X reads are warp-wide broadcasts).  Each k step reads
 // 4 slab values and CW/4 values of X for 4 * CW/4 fused multiply-adds.
+// Row slots i with 32 i >= rows hold no row of the chunk and are skipped (the
+// test is uniform across a warp).
 template <typename Tc, int CW>
 __device__ __forceinline__ void tile_product(const Tc* __restrict__ slab, const Tc* __restrict__ Xp, int pw,
-                                             Tc (&acc)[4][CW / 4]) {
+                                             int rows, Tc (&acc)[4][CW / 4]) {
   constexpr int CT = CW / 4;
   const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;
   for (int kk = 0; kk < pw; ++kk) {
-    Tc a[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) a[i] = slab[(tr + 32 * i) * SLAB_PAD + kk];
     Tc xv[CT];
     const Tc* xr = Xp + kk * CW + tc * CT;
 #pragma unroll
     for (int c = 0; c < CT; ++c) xv[c] = xr[c];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 4; ++i) {
+      if (32 * i < rows) {
+        const Tc a = slab[(tr + 32 * i) * SLAB_PAD + kk];
 #pragma unroll
-      for (int c = 0; c < CT; ++c) acc[i][c] = fma(a[i], xv[c], acc[i][c]);
+        for (int c = 0; c < CT; ++c) acc[i][c] = fma(a, xv[c], acc[i][c]);
+      }
+    }
   }
 }
 
@@ -129,7 +132,7 @@ __device__ __forceinline__ void trailing_update(const Tc* __restrict__ slab, con
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int c = 0; c < CT; ++c) acc[i][c] = Tc(0);
-  tile_product<Tc, CW>(slab, Xp, pw, acc);
+  tile_product<Tc, CW>(slab, Xp, pw, rows, acc);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int r = tr + 32 * i;
@@ -218,16 +221,20 @@ __device__ __forceinline__ void trailing_update_wide(const Tc* __restrict__ slab
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int c = 0; c < CT; ++c) acc[i][c] = Tc(0);
+  // Row slots with RG * i >= rows hold no row of the chunk and are skipped
+  // (uniform across a warp when rows is a multiple of RG).
+  const int slots = (rows + RG - 1) / RG;
   for (int kk = 0; kk < pw; ++kk) {
     Tc a[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) a[i] = slab[(tr + RG * i) * SLAB_PAD + kk];
+    for (int i = 0; i < 4; ++i) a[i] = i < slots ? slab[(tr + RG * i) * SLAB_PAD + kk] : Tc(0);
     const Tc* xr = Xp + kk * CW + tc * CT;
 #pragma unroll
     for (int c = 0; c < CT; ++c) {
       const Tc xv = xr[c];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) acc[i][c] = fma(a[i], xv, acc[i][c]);
+      for (int i = 0; i < 4; ++i)
+        if (i < slots) acc[i][c] = fma(a[i], xv, acc[i][c]);
     }
   }
 #pragma unroll
