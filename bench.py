@@ -12,8 +12,13 @@ n^2 m flop count of a triangular solve.
 
 Variants:
   plain   the dtype-preserving Float64 path (DFMA GEMM updates, FP64 leaves).
-  mixed   the mixed-precision form: BF16 tensor-core updates with an operand
-          split plus FP64 iterative refinement (when built into the library).
+  mixed   the mixed-precision form (default): every GEMM update on the BF16
+          tensor cores.  With --terms 7 (default) each FP64 operand is split
+          into 7 BF16 slices and the 28 significant slice pairs accumulate
+          exactly (FP32 chunks drained into int64), so the updates are as
+          accurate as FP64 and no refinement sweep is needed (--sweeps 0).
+          --terms 1-3 with --sweeps >= 1 is the cheaper split plus
+          FP64-residual iterative refinement.
 
 Also reported on the same JSON line:
   e2e           the same metric through the C ABI with host buffers: pinned
@@ -51,8 +56,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--variant", choices=["plain", "mixed"], default="mixed")
     ap.add_argument("--lowp", choices=["bf16", "f16"], default="bf16")
-    ap.add_argument("--terms", type=int, default=3, help="split terms (1-3, or 7 for exact updates)")
-    ap.add_argument("--sweeps", type=int, default=2)
+    ap.add_argument("--terms", type=int, default=7, help="split terms (1-3, or 7 for exact updates)")
+    ap.add_argument("--sweeps", type=int, default=0)
     ap.add_argument("--residual", choices=["split", "fp64"], default="split")
     ap.add_argument("--cutoff", type=int, default=0)
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison step")

@@ -25,6 +25,7 @@
 #include <cudaTypedefs.h>
 
 #include <mutex>
+#include <type_traits>
 #include <unordered_map>
 
 #include "nla_common.cuh"
@@ -560,19 +561,47 @@ template <> __device__ __forceinline__ __nv_bfloat16 from_int<__nv_bfloat16>(int
 }
 template <> __device__ __forceinline__ __half from_int<__half>(int v) { return __float2half_rn((float)v); }
 
-// Split a rows x cols view into `ns` K-major slices of type Sl (rows padded
-// to rows_pad, K padded to cols_pad, zeros in the padding and outside the
-// staged triangle).  With copy set, the single slice is the element itself
-// (a Float16 operand of the plain path); otherwise slices are the integers
-// s_p of  x = 2^e[row] * sum_p s_p 2^(-beta p).
+// Two adjacent slice values packed for one 32-bit store.
+template <typename S> __device__ __forceinline__ uint32_t pack2(S a, S b) {
+  return (uint32_t)__builtin_bit_cast(uint16_t, a) | ((uint32_t)__builtin_bit_cast(uint16_t, b) << 16);
+}
+
+// x * 2^(62 - ex) rounded to an integer (0 for zeros, non-finite values and
+// rows without a finite element), from the FP64 bit pattern.
+__device__ __forceinline__ long long fixed_of(double x, int ex) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int biased = (int)((b >> 52) & 0x7FF);
+  const unsigned long long mant = b & ((1ull << 52) - 1);
+  long long Y = 0;
+  if (biased != 0x7FF && ex != NONFINITE_EXP && ex != SENTINEL_EXP && (biased != 0 || mant != 0)) {
+    const unsigned long long m = biased ? (mant | (1ull << 52)) : mant;
+    const int eb = biased ? biased : 1;
+    const int sh = eb - 1013 - ex;  // Y = m * 2^sh = x * 2^(62 - ex)
+    if (sh >= 0) Y = (long long)(m << sh);
+    else if (sh > -63) Y = (long long)((m + (1ull << (-sh - 1))) >> (-sh));
+    if (b >> 63) Y = -Y;
+  }
+  return Y;
+}
+
+// Split a rows x cols view into NS K-major slices of type Sl (rows padded to
+// rows_pad, K padded to cols_pad, zeros in the padding and outside the staged
+// triangle).  The slices are the integers s_p of
+//   x = 2^e[row] * sum_p s_p 2^(-beta p),  beta = 8 (BF16) or 11 (FP16),
+// peeled from the top of the 63-bit fixed-point value with round-to-nearest
+// so that |s_p| <= 2^(beta-1).  NS = 0 stages the element itself (a Float16
+// operand of the plain path).  The slice count and width are compile-time
+// constants, so every shift is an immediate; each thread produces two
+// adjacent K values and writes them with one 32-bit store per slice.
 // When nrm is not null, nrm[row] accumulates sum_k sum_p |s_p| 2^(-beta p),
 // which bounds every partial sum of slice products along that row (in units
 // of the row's scale 2^e) for a partner whose elements are below 1/2.
-template <typename T, typename Sl>
+template <typename T, typename Sl, int NS>
 __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int64_t ld, int t, int64_t rows,
                                                     int64_t cols, int tri, const int* __restrict__ e,
                                                     Sl* __restrict__ out, int64_t rows_pad, int64_t cols_pad,
-                                                    int ns, int beta, int copy, float* __restrict__ nrm) {
+                                                    float* __restrict__ nrm) {
+  constexpr int BETA = std::is_same<Sl, __nv_bfloat16>::value ? 8 : 11;
   __shared__ double tile[32][65];
   const int64_t i0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 64;
   for (int idx = threadIdx.x; idx < 32 * 64; idx += 256) {
@@ -583,40 +612,33 @@ __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int
   }
   __syncthreads();
   const int64_t slice_elems = rows_pad * cols_pad;
-  for (int idx = threadIdx.x; idx < 32 * 64; idx += 256) {
-    const int i = idx >> 6, k = idx & 63;
+  // One row per warp and pass (idx >> 5 is warp-uniform), two K values per lane.
+  for (int idx = threadIdx.x; idx < 32 * 32; idx += 256) {
+    const int i = idx >> 5, k = (idx & 31) * 2;
     const int64_t gi = i0 + i, gk = k0 + k;
-    const int64_t o = gi * cols_pad + gk;
-    const double x = tile[i][k];
-    if (copy) {
-      out[o] = (Sl)(float)x;
+    uint32_t* o = reinterpret_cast<uint32_t*>(out + gi * cols_pad + gk);
+    if constexpr (NS == 0) {
+      *o = pack2<Sl>((Sl)(float)tile[i][k], (Sl)(float)tile[i][k + 1]);
       continue;
-    }
-    const int ex = gi < rows ? e[gi] : SENTINEL_EXP;
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const int biased = (int)((b >> 52) & 0x7FF);
-    const unsigned long long mant = b & ((1ull << 52) - 1);
-    long long Y = 0;
-    if (biased != 0x7FF && ex != NONFINITE_EXP && ex != SENTINEL_EXP && (biased != 0 || mant != 0)) {
-      const unsigned long long m = biased ? (mant | (1ull << 52)) : mant;
-      const int eb = biased ? biased : 1;
-      const int sh = eb - 1013 - ex;  // Y = m * 2^sh = x * 2^(62 - ex)
-      if (sh >= 0) Y = (long long)(m << sh);
-      else if (sh > -63) Y = (long long)((m + (1ull << (-sh - 1))) >> (-sh));
-      if (b >> 63) Y = -Y;
-    }
-    float mag = 0.0f;
-    for (int sl = 0; sl < ns; ++sl) {
-      const int shift = 62 - beta * (sl + 1);
-      const long long sp = (Y + (1ll << (shift - 1))) >> shift;
-      Y -= sp << shift;
-      out[(int64_t)sl * slice_elems + o] = from_int<Sl>((int)sp);
-      mag += fabsf((float)sp) * exp2f((float)(-beta * (sl + 1)));
-    }
-    if (nrm) {
-      // 32 consecutive k of one row per warp (idx >> 6 is warp-uniform).
-      for (int off = 16; off > 0; off >>= 1) mag += __shfl_xor_sync(0xffffffffu, mag, off);
-      if ((threadIdx.x & 31) == 0 && gi < rows && mag > 0.0f) atomicAdd(&nrm[gi], mag);
+    } else {
+      const int ex = gi < rows ? e[gi] : SENTINEL_EXP;
+      long long y0 = fixed_of(tile[i][k], ex), y1 = fixed_of(tile[i][k + 1], ex);
+      float mag = 0.0f;
+#pragma unroll
+      for (int sl = 0; sl < NS; ++sl) {
+        const int shift = 62 - BETA * (sl + 1);
+        const long long s0 = (y0 + (1ll << (shift - 1))) >> shift;
+        const long long s1 = (y1 + (1ll << (shift - 1))) >> shift;
+        y0 -= s0 << shift;
+        y1 -= s1 << shift;
+        o[sl * (slice_elems / 2)] = pack2<Sl>(from_int<Sl>((int)s0), from_int<Sl>((int)s1));
+        // 2^(-beta (sl + 1)) built from its exponent bits (exact).
+        mag += (fabsf((float)s0) + fabsf((float)s1)) * __int_as_float((127 - BETA * (sl + 1)) << 23);
+      }
+      if (nrm) {
+        for (int off = 16; off > 0; off >>= 1) mag += __shfl_xor_sync(0xffffffffu, mag, off);
+        if ((threadIdx.x & 31) == 0 && gi < rows && mag > 0.0f) atomicAdd(&nrm[gi], mag);
+      }
     }
   }
 }
@@ -745,8 +767,8 @@ int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bo
                    (double)rows * (double)K * (double)dtype_size(in_dtype) * (copy ? 1 : 2) + (double)S * Rp * Kp * 2);
   const dim3 gs((unsigned)(Rp / 32), (unsigned)(Kp / 64));
   if (copy) {
-    split_kernel<__half, __half><<<gs, 256, 0, s>>>((const __half*)X.p, X.ld, X.t, rows, K, tri, nullptr,
-                                                    (__half*)out->slices, Rp, Kp, 1, 0, 1, nullptr);
+    split_kernel<__half, __half, 0><<<gs, 256, 0, s>>>((const __half*)X.p, X.ld, X.t, rows, K, tri, nullptr,
+                                                       (__half*)out->slices, Rp, Kp, nullptr);
     NLA_CHECK_LAUNCH("split_kernel");
     return NLA_OK;
   }
@@ -755,13 +777,25 @@ int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bo
   const dim3 ge((unsigned)((rows + 63) / 64), (unsigned)((K + 63) / 64));
   row_exp_kernel<double><<<ge, 256, 0, s>>>((const double*)X.p, X.ld, X.t, rows, K, tri, out->e);
   NLA_CHECK_LAUNCH("row_exp_kernel");
-  if (bf16)
-    split_kernel<double, __nv_bfloat16><<<gs, 256, 0, s>>>((const double*)X.p, X.ld, X.t, rows, K, tri, out->e,
-                                                           (__nv_bfloat16*)out->slices, Rp, Kp, S, beta, 0,
-                                                           out->nrm);
-  else
-    split_kernel<double, __half><<<gs, 256, 0, s>>>((const double*)X.p, X.ld, X.t, rows, K, tri, out->e,
-                                                    (__half*)out->slices, Rp, Kp, S, beta, 0, out->nrm);
+  const double* xp = static_cast<const double*>(X.p);
+  if (bf16) {
+    auto* o = static_cast<__nv_bfloat16*>(out->slices);
+    switch (S) {
+      case 1: split_kernel<double, __nv_bfloat16, 1><<<gs, 256, 0, s>>>(xp, X.ld, X.t, rows, K, tri, out->e, o, Rp, Kp, out->nrm); break;
+      case 2: split_kernel<double, __nv_bfloat16, 2><<<gs, 256, 0, s>>>(xp, X.ld, X.t, rows, K, tri, out->e, o, Rp, Kp, out->nrm); break;
+      case 3: split_kernel<double, __nv_bfloat16, 3><<<gs, 256, 0, s>>>(xp, X.ld, X.t, rows, K, tri, out->e, o, Rp, Kp, out->nrm); break;
+      case EXACT_SLICES: split_kernel<double, __nv_bfloat16, EXACT_SLICES><<<gs, 256, 0, s>>>(xp, X.ld, X.t, rows, K, tri, out->e, o, Rp, Kp, out->nrm); break;
+      default: return fail(NLA_ERR_ARG, "BF16 slices: 1, 2, 3 or 7 terms");
+    }
+  } else {
+    auto* o = static_cast<__half*>(out->slices);
+    switch (S) {
+      case 1: split_kernel<double, __half, 1><<<gs, 256, 0, s>>>(xp, X.ld, X.t, rows, K, tri, out->e, o, Rp, Kp, out->nrm); break;
+      case 2: split_kernel<double, __half, 2><<<gs, 256, 0, s>>>(xp, X.ld, X.t, rows, K, tri, out->e, o, Rp, Kp, out->nrm); break;
+      case 3: split_kernel<double, __half, 3><<<gs, 256, 0, s>>>(xp, X.ld, X.t, rows, K, tri, out->e, o, Rp, Kp, out->nrm); break;
+      default: return fail(NLA_ERR_ARG, "FP16 slices: 1, 2 or 3 terms");
+    }
+  }
   NLA_CHECK_LAUNCH("split_kernel");
   return NLA_OK;
 }
