@@ -152,13 +152,17 @@ class ClockSampler:
 
 
 def traffic_per_launch():
-    """DRAM bytes per launch of the dominant tensor-core kernel from the
-    committed ncu summary (profiles/umma_traffic.json), or None."""
-    path = os.path.join(ROOT, "profiles", "umma_traffic.json")
+    """DRAM bytes (read + write) per launch of the dominant tensor-core kernel,
+    from the committed ncu summary of the same workload
+    (profiles/umma_exact_kernel_n16384_dram.md), or None."""
+    path = os.path.join(ROOT, "profiles", "umma_exact_kernel_n16384_dram.md")
     if not os.path.exists(path):
         return None
     with open(path) as f:
-        return json.load(f).get("dram_bytes_per_launch")
+        for line in f:
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    return None
 
 
 def make_inputs(n, m, seed=0):
@@ -703,11 +707,15 @@ def main():
         name, (launches, kms, kflops, kbytes) = dom
         achieved = kflops / (kms / 1e3) / 1e12
         share = kms / sum(v[1] for v in trace.values())
+        # The committed DRAM capture covers the exact 7-slice updates of the
+        # 16384 x 16384 solve only.
+        exact_headline = (args.variant == "mixed" and args.terms == 7 and args.n == 16384 and args.m == 16384)
         if name == "gemm_umma":
             peak = float(pk.get("bf16_tflops_sustained", pk.get("bf16_tflops")))
             roofline = {"kernel": "umma_gemm/umma_exact (tcgen05 BF16 slice products)", "bound": "tensor",
                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                        "traffic": traffic_per_launch(), "launches": launches, "share": share,
+                        "traffic": traffic_per_launch() if exact_headline else None,
+                        "launches": launches, "share": share,
                         "peak_source": "bf16_tflops_sustained of %s MEASURED_PEAKS.json" % pk_kind}
         else:
             # The plain FP64 path runs on the DFMA pipe; no tensor or HBM peak applies.

@@ -95,29 +95,41 @@ __device__ __forceinline__ void store_block(const LeafArgs& g, const Tc* X, int6
 }
 
 // acc[i][c] += sum_kk slab[tr + 32 i][kk] * Xp[kk, tc * CW/4 + c] for
-// kk < pw: LEAF_THREADS threads as 32 row lanes (tr) x 4 column groups (tc,
-// one warp each, so the X reads are warp-wide broadcasts).  Each k step reads
-// 4 slab values and CW/4 values of X for 4 * CW/4 fused multiply-adds.
-// Row slots i with 32 i >= rows hold no row of the chunk and are skipped (the
-// test is uniform across a warp).
-template <typename Tc, int CW>
-__device__ __forceinline__ void tile_product(const Tc* __restrict__ slab, const Tc* __restrict__ Xp, int pw,
-                                             int rows, Tc (&acc)[4][CW / 4]) {
+// kk < pw and row slots i < SLOTS: LEAF_THREADS threads as 32 row lanes (tr)
+// x 4 column groups (tc, one warp each, so the X reads are warp-wide
+// broadcasts).  Each k step reads SLOTS slab values and CW/4 values of X for
+// SLOTS * CW/4 fused multiply-adds.
+template <typename Tc, int CW, int SLOTS>
+__device__ __forceinline__ void tile_product_n(const Tc* __restrict__ slab, const Tc* __restrict__ Xp, int pw,
+                                               Tc (&acc)[4][CW / 4]) {
   constexpr int CT = CW / 4;
   const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;
   for (int kk = 0; kk < pw; ++kk) {
+    Tc a[SLOTS];
+#pragma unroll
+    for (int i = 0; i < SLOTS; ++i) a[i] = slab[(tr + 32 * i) * SLAB_PAD + kk];
     Tc xv[CT];
     const Tc* xr = Xp + kk * CW + tc * CT;
 #pragma unroll
     for (int c = 0; c < CT; ++c) xv[c] = xr[c];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      if (32 * i < rows) {
-        const Tc a = slab[(tr + 32 * i) * SLAB_PAD + kk];
+    for (int i = 0; i < SLOTS; ++i)
 #pragma unroll
-        for (int c = 0; c < CT; ++c) acc[i][c] = fma(a, xv[c], acc[i][c]);
-      }
-    }
+      for (int c = 0; c < CT; ++c) acc[i][c] = fma(a[i], xv[c], acc[i][c]);
+  }
+}
+
+// Row slots i with 32 i >= rows hold no row of the chunk: the slot count is
+// made a compile-time constant so that the unrolled body carries no
+// predicates.
+template <typename Tc, int CW>
+__device__ __forceinline__ void tile_product(const Tc* __restrict__ slab, const Tc* __restrict__ Xp, int pw,
+                                             int rows, Tc (&acc)[4][CW / 4]) {
+  switch ((rows + 31) >> 5) {
+    case 1: tile_product_n<Tc, CW, 1>(slab, Xp, pw, acc); break;
+    case 2: tile_product_n<Tc, CW, 2>(slab, Xp, pw, acc); break;
+    case 3: tile_product_n<Tc, CW, 3>(slab, Xp, pw, acc); break;
+    default: tile_product_n<Tc, CW, 4>(slab, Xp, pw, acc); break;
   }
 }
 
@@ -210,41 +222,50 @@ __device__ __forceinline__ void solve_block(const LeafArgs& g, int64_t c0, int n
 // column blocks: LEAF_THREADS threads as RG row groups x (LEAF_THREADS / RG)
 // column groups, each thread a 4-row x CT-column register tile (rows strided
 // by RG so that slab reads are conflict-free).  rows <= 4 * RG.
-template <typename Tc, int CW, int RG>
-__device__ __forceinline__ void trailing_update_wide(const Tc* __restrict__ slab, const Tc* __restrict__ Xp,
-                                                     Tc* __restrict__ Xo, int rows, int pw) {
+template <typename Tc, int CW, int RG, int SLOTS>
+__device__ __forceinline__ void trailing_update_wide_n(const Tc* __restrict__ slab, const Tc* __restrict__ Xp,
+                                                       Tc* __restrict__ Xo, int rows, int pw) {
   constexpr int CG = LEAF_THREADS / RG;
   constexpr int CT = CW / CG;
   const int tr = threadIdx.x % RG, tc = threadIdx.x / RG;
-  Tc acc[4][CT];
+  Tc acc[SLOTS][CT];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < SLOTS; ++i)
 #pragma unroll
     for (int c = 0; c < CT; ++c) acc[i][c] = Tc(0);
-  // Row slots with RG * i >= rows hold no row of the chunk and are skipped
-  // (uniform across a warp when rows is a multiple of RG).
-  const int slots = (rows + RG - 1) / RG;
   for (int kk = 0; kk < pw; ++kk) {
-    Tc a[4];
+    Tc a[SLOTS];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) a[i] = i < slots ? slab[(tr + RG * i) * SLAB_PAD + kk] : Tc(0);
+    for (int i = 0; i < SLOTS; ++i) a[i] = slab[(tr + RG * i) * SLAB_PAD + kk];
     const Tc* xr = Xp + kk * CW + tc * CT;
 #pragma unroll
     for (int c = 0; c < CT; ++c) {
       const Tc xv = xr[c];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
-        if (i < slots) acc[i][c] = fma(a[i], xv, acc[i][c]);
+      for (int i = 0; i < SLOTS; ++i) acc[i][c] = fma(a[i], xv, acc[i][c]);
     }
   }
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < SLOTS; ++i) {
     const int r = tr + RG * i;
     if (r < rows) {
       Tc* xo = Xo + r * CW + tc * CT;
 #pragma unroll
       for (int c = 0; c < CT; ++c) xo[c] -= acc[i][c];
     }
+  }
+}
+
+// Row slots with RG * i >= rows hold no row of the chunk and are skipped; the
+// slot count is a compile-time constant of the body.
+template <typename Tc, int CW, int RG>
+__device__ __forceinline__ void trailing_update_wide(const Tc* __restrict__ slab, const Tc* __restrict__ Xp,
+                                                     Tc* __restrict__ Xo, int rows, int pw) {
+  switch ((rows + RG - 1) / RG) {
+    case 1: trailing_update_wide_n<Tc, CW, RG, 1>(slab, Xp, Xo, rows, pw); break;
+    case 2: trailing_update_wide_n<Tc, CW, RG, 2>(slab, Xp, Xo, rows, pw); break;
+    case 3: trailing_update_wide_n<Tc, CW, RG, 3>(slab, Xp, Xo, rows, pw); break;
+    default: trailing_update_wide_n<Tc, CW, RG, 4>(slab, Xp, Xo, rows, pw); break;
   }
 }
 
@@ -275,17 +296,22 @@ __device__ __forceinline__ void solve_block_wide(const LeafArgs& g, int64_t c0, 
     const int pw = min(PANEL, n - p0);
     stage_slab<PANEL, T>(g, diag, p0, pw, p0, pw, [](int i, int j) { return j < i; });
     __syncthreads();
-    if (t < CW) {
+    // The panel's serial chains run on CW threads; the warps that take them
+    // rotate with the panel and the CTA so that co-resident CTAs spread this
+    // FP64 work over all four SM sub-partitions.
+    const int rot = 32 * (int)((p0 / PANEL + blockIdx.x) % (LEAF_THREADS / 32));
+    const int tt = (t - rot + LEAF_THREADS) % LEAF_THREADS;
+    if (tt < CW) {
       Tc x[PANEL];
 #pragma unroll
       for (int r = 0; r < PANEL; ++r) {
         if (r < pw) {
-          Tc y = X[(p0 + r) * CW + t];
+          Tc y = X[(p0 + r) * CW + tt];
 #pragma unroll
           for (int j = 0; j < r; ++j) y = fma(-diag[r * SLAB_PAD + j], x[j], y);
           y *= inv_d[p0 + r];
           x[r] = y;
-          X[(p0 + r) * CW + t] = y;
+          X[(p0 + r) * CW + tt] = y;
         }
       }
     }

@@ -24,6 +24,8 @@
 // that nla_device_status() reports, releases its TMEM and returns.
 #include <cudaTypedefs.h>
 
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <type_traits>
 #include <unordered_map>
@@ -255,9 +257,11 @@ constexpr int EX_THREADS = 320;  // producer, MMA, 8 epilogue warps
 constexpr int EX_CHUNK = 16;     // k-blocks per exact chunk (1024 values)
 constexpr int EX_SLICES = 7;
 constexpr int EX_MAX_PAIRS = 28;
-constexpr int EX_STAGES = 6;
+constexpr int EX_STAGES = 7;                // 224 KiB of stages: the loads in flight bound the rate
 constexpr int EX_STAGE_BYTES = 2 * TILE_BYTES;
 constexpr int EX_DYN_SMEM = EX_STAGES * EX_STAGE_BYTES + 1024 + 256;
+static_assert(EX_DYN_SMEM + 16 <= 232448, "exact kernel shared memory above the per-block limit");
+constexpr int EX_DEFAULT_CLUSTER = 11;  // cluster shape (CM x CN tiles) unless NLA_EXACT_CLUSTER says otherwise
 
 struct ExactParams {
   int M, N, K;
@@ -281,10 +285,11 @@ struct ExactParams {
   const int* eb;
 };
 
-__device__ __forceinline__ void tri_k_range(int tri, int r0, int K, int& lo, int& hi) {
+// K range of the staged triangle that meets rows [r0, r0 + span).
+__device__ __forceinline__ void tri_k_range(int tri, int r0, int span, int K, int& lo, int& hi) {
   lo = 0;
   hi = K - 1;
-  if (tri == 1 || tri == 3) hi = min(K - 1, r0 + BM - 1);
+  if (tri == 1 || tri == 3) hi = min(K - 1, r0 + span - 1);
   else if (tri == 2 || tri == 4) lo = r0;
 }
 
@@ -302,9 +307,18 @@ __device__ __forceinline__ void two_sum_dev(double a, double b, double& s, doubl
   e = (a - (s - bp)) + (b - bp);
 }
 
+// CM x CN: the cluster shape in output tiles.  With a cluster, the CTAs of
+// one tile row share the A tile and those of one tile column the B tile: each
+// CTA loads 1/CN of its A tile and 1/CM of its B tile and multicasts them to
+// the CTAs that share it, so the L2 -> SM traffic per CTA falls from 32 KiB to
+// 16/CN + 16/CM KiB per stage.  A stage of CTA c is free again once every CTA
+// that writes into it (its tile row and tile column) has consumed it; their
+// tensor-core commits arrive on c's `empty` barrier, which counts CM + CN - 1.
+template <int CM, int CN>
 __global__ void __launch_bounds__(EX_THREADS, 1)
     umma_exact_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       const ExactParams p) {
+  constexpr int CS = CM * CN;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + EX_STAGES * EX_STAGE_BYTES);
@@ -316,17 +330,37 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   __shared__ volatile int s_abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int group = 8;
-  const int per_group = group * p.tiles_n;
-  const int g = blockIdx.x / per_group;
+  int cm = 0, cn = 0, cid = (int)blockIdx.x;
+  if constexpr (CS > 1) {
+    const int r = (int)umma::cluster_ctarank();
+    cm = r % CM;
+    cn = r / CM;
+    cid = (int)blockIdx.x / CS;
+  }
+  // Clusters cover CM x CN output tiles and are rasterised in groups of 8
+  // tile rows for L2 reuse.
+  const int stm = (p.tiles_m + CM - 1) / CM, stn = (p.tiles_n + CN - 1) / CN;
+  constexpr int group = 8 / CM;
+  const int per_group = group * stn;
+  const int g = cid / per_group;
   const int first_m = g * group;
-  const int gsize = min(p.tiles_m - first_m, group);
-  const int local = blockIdx.x % per_group;
-  const int m0 = (first_m + local % gsize) * BM, n0 = (local / gsize) * BN;
+  const int gsize = min(stm - first_m, group);
+  const int local = cid % per_group;
+  const int sm0 = (first_m + local % gsize) * CM, sn0 = (local / gsize) * CN;
+  const int m0 = (sm0 + cm) * BM, n0 = (sn0 + cn) * BN;
+  // CTAs sharing this CTA's A tile (same cm) and B tile (same cn).
+  uint16_t row_mask = 0, col_mask = 0;
+#pragma unroll
+  for (int j = 0; j < CN; ++j) row_mask |= (uint16_t)(1u << (cm + CM * j));
+#pragma unroll
+  for (int j = 0; j < CM; ++j) col_mask |= (uint16_t)(1u << (j + CM * cn));
+  const uint16_t peer_mask = row_mask | col_mask;
 
+  // K range: the union over the cluster's tiles, so that all its CTAs walk
+  // the same stage sequence (the extra K meets zeros of the staged triangle).
   int alo, ahi, blo, bhi;
-  tri_k_range(p.tri_a, m0, p.K, alo, ahi);
-  tri_k_range(p.tri_b, n0, p.K, blo, bhi);
+  tri_k_range(p.tri_a, sm0 * BM, CM * BM, p.K, alo, ahi);
+  tri_k_range(p.tri_b, sn0 * BN, CN * BN, p.K, blo, bhi);
   const int klo = max(alo, blo), khi = min(ahi, bhi);
   const int kb0 = klo / BK;
   const int kb1 = khi >= klo ? khi / BK + 1 : kb0;  // empty range when the triangles miss each other
@@ -335,7 +369,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     s_abort = 0;
     for (int s = 0; s < EX_STAGES; ++s) {
       umma::mbar_init(umma::smem_u32(&full[s]), 1);
-      umma::mbar_init(umma::smem_u32(&empty[s]), 1);
+      umma::mbar_init(umma::smem_u32(&empty[s]), CM + CN - 1);
     }
     for (int b = 0; b < 2; ++b) {
       umma::mbar_init(umma::smem_u32(&cfull[b]), 1);
@@ -347,6 +381,9 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   if (warp == 1) umma::tmem_alloc(umma::smem_u32(tmem_slot), 256);
   umma::fence_before_sync();
   __syncthreads();
+  // Peers multicast into this CTA's stages and barriers only after all of
+  // the cluster's barriers are initialised.
+  if constexpr (CS > 1) umma::cluster_sync();
   umma::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
   bool ok = true;
@@ -368,9 +405,28 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
             const uint32_t fb = umma::smem_u32(&full[s]);
             umma::mbar_arrive_expect_tx(fb, (uint32_t)EX_STAGE_BYTES);
             uint8_t* st = smem + s * EX_STAGE_BYTES;
-            umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, p.pa[pr] * p.a_rows + m0);
-            umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), &tmB, fb, kb * BK, p.pb[pr] * p.b_rows + n0);
+            // Rows of a tile are 128 bytes: part j of a tile split in parts of
+            // R rows starts j * R * 128 bytes in (a multiple of the 1024-byte
+            // swizzle atom).
+            if constexpr (CN > 1)
+              umma::tma_load_2d_mc(umma::smem_u32(st + cn * (BM / CN) * 128), &tmA, fb, kb * BK,
+                                   p.pa[pr] * p.a_rows + m0 + cn * (BM / CN), row_mask);
+            else
+              umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, p.pa[pr] * p.a_rows + m0);
+            if constexpr (CM > 1)
+              umma::tma_load_2d_mc(umma::smem_u32(st + TILE_BYTES + cm * (BN / CM) * 128), &tmB, fb, kb * BK,
+                                   p.pb[pr] * p.b_rows + n0 + cm * (BN / CM), col_mask);
+            else
+              umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), &tmB, fb, kb * BK, p.pb[pr] * p.b_rows + n0);
           }
+        }
+      }
+      if constexpr (CS > 1) {
+        // Wait for the last release of every stage used: every peer's commit
+        // that targets this CTA's barriers has landed before it exits.
+        for (int s = 0; s < EX_STAGES && s < it && ok; ++s) {
+          const uint32_t rounds = (uint32_t)((it - s + EX_STAGES - 1) / EX_STAGES);
+          ok = umma::mbar_wait(umma::smem_u32(&empty[s]), (rounds & 1u) ^ 1u, &s_abort, &g_device_error, 16);
         }
       }
     }
@@ -403,7 +459,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
             for (int kk = 0; kk < BK / 16; ++kk)
               umma::mma_f16(tmem + (uint32_t)(b * BN), umma::desc_kmajor_sw128(a0 + kk * 32),
                             umma::desc_kmajor_sw128(b0 + kk * 32), idesc, (kb > c0 || kk > 0) ? 1u : 0u);
-            umma::mma_commit(umma::smem_u32(&empty[s]));
+            if constexpr (CS > 1)
+              umma::mma_commit_mc(umma::smem_u32(&empty[s]), peer_mask);
+            else
+              umma::mma_commit(umma::smem_u32(&empty[s]));
           }
           if (ok) umma::mma_commit(umma::smem_u32(&cfull[b]));
         }
@@ -494,6 +553,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
 
   umma::fence_before_sync();
   __syncthreads();
+  if constexpr (CS > 1) umma::cluster_sync();
   if (warp == 1) {
     __syncwarp();
     umma::fence_after_sync();
@@ -533,7 +593,12 @@ __device__ __forceinline__ bool in_tri(int tri, int64_t i, int64_t k) {
 }
 
 // Per-row maximum exponent of a rows x cols view (op(X) = X or X^T), one
-// 64 x 64 tile per CTA, reduced into e[] with atomicMax.
+// 64 x 64 tile per CTA, reduced into e[] with atomicMax.  Exponents of zeros
+// (SENTINEL_EXP) sort below every finite one and non-finite values
+// (NONFINITE_EXP) above, so a plain maximum carries both.  Each thread first
+// reduces its own elements of a row; with K contiguous (t = 1) a warp owns a
+// row and reduces it with one warp-wide max, so no shared-memory atomics
+// collide.
 template <typename T>
 __global__ void __launch_bounds__(256) row_exp_kernel(const T* __restrict__ X, int64_t ld, int t, int64_t rows,
                                                       int64_t cols, int tri, int* __restrict__ e) {
@@ -541,14 +606,29 @@ __global__ void __launch_bounds__(256) row_exp_kernel(const T* __restrict__ X, i
   if (threadIdx.x < 64) se[threadIdx.x] = SENTINEL_EXP;
   __syncthreads();
   const int64_t i0 = (int64_t)blockIdx.x * 64, k0 = (int64_t)blockIdx.y * 64;
-  for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
-    int i, k;
-    if (!t) { i = idx & 63; k = idx >> 6; } else { k = idx & 63; i = idx >> 6; }
+  auto ex_at = [&](int i, int k) -> int {
     const int64_t gi = i0 + i, gk = k0 + k;
-    if (gi < rows && gk < cols && in_tri(tri, gi, gk)) {
-      const int ex = exp_of(to_double(X[mat_off(gi, gk, ld, t)]));
-      if (ex != SENTINEL_EXP) atomicMax(&se[i], ex);
+    if (gi < rows && gk < cols && in_tri(tri, gi, gk)) return exp_of(to_double(X[mat_off(gi, gk, ld, t)]));
+    return SENTINEL_EXP;
+  };
+  // The loops are unrolled so that every load of a thread is in flight at
+  // once (the kernel is bound by memory-level parallelism).
+  if (t) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int m[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) m[r] = max(ex_at(warp + 8 * r, lane), ex_at(warp + 8 * r, lane + 32));
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int v = __reduce_max_sync(0xffffffffu, m[r]);
+      if (lane == 0) se[warp + 8 * r] = v;
     }
+  } else {
+    const int i = threadIdx.x & 63;
+    int m = SENTINEL_EXP;
+#pragma unroll
+    for (int k = threadIdx.x >> 6, j = 0; j < 16; k += 4, ++j) m = max(m, ex_at(i, k));
+    atomicMax(&se[i], m);
   }
   __syncthreads();
   if (threadIdx.x < 64 && i0 + threadIdx.x < rows && se[threadIdx.x] != SENTINEL_EXP)
@@ -604,11 +684,23 @@ __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int
   constexpr int BETA = std::is_same<Sl, __nv_bfloat16>::value ? 8 : 11;
   __shared__ double tile[32][65];
   const int64_t i0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 64;
-  for (int idx = threadIdx.x; idx < 32 * 64; idx += 256) {
+  // All eight loads of a thread are issued before any is used (the kernel is
+  // bound by memory-level parallelism, not by its integer work).
+  double v[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int idx = threadIdx.x + 256 * j;
     int i, k;
     if (!t) { i = idx & 31; k = idx >> 5; } else { k = idx & 63; i = idx >> 6; }
     const int64_t gi = i0 + i, gk = k0 + k;
-    tile[i][k] = (gi < rows && gk < cols && in_tri(tri, gi, gk)) ? to_double(X[mat_off(gi, gk, ld, t)]) : 0.0;
+    v[j] = (gi < rows && gk < cols && in_tri(tri, gi, gk)) ? to_double(X[mat_off(gi, gk, ld, t)]) : 0.0;
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int idx = threadIdx.x + 256 * j;
+    int i, k;
+    if (!t) { i = idx & 31; k = idx >> 5; } else { k = idx & 63; i = idx >> 6; }
+    tile[i][k] = v[j];
   }
   __syncthreads();
   const int64_t slice_elems = rows_pad * cols_pad;
@@ -661,13 +753,14 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-int make_map(CUtensorMap* map, const void* base, bool bf16, uint64_t cols_pad, uint64_t total_rows) {
+int make_map(CUtensorMap* map, const void* base, bool bf16, uint64_t cols_pad, uint64_t total_rows,
+             uint32_t box_rows = BM) {
   auto fn = encode_fn();
   if (!fn) return fail(NLA_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available from the driver");
   if ((reinterpret_cast<uintptr_t>(base) & 15) != 0) return fail(NLA_ERR_ARG, "staged operand is not 16-byte aligned");
   cuuint64_t dims[2] = {cols_pad, total_rows};
   cuuint64_t strides[1] = {cols_pad * 2};
-  cuuint32_t box[2] = {BK, BM};
+  cuuint32_t box[2] = {BK, box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
                   const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -701,13 +794,51 @@ int ensure_gemm_smem() {
   return status == cudaSuccess ? NLA_OK : cuda_status(status, "cudaFuncSetAttribute(umma_gemm_kernel)");
 }
 
+template <int CM, int CN>
 int ensure_exact_smem() {
   static std::once_flag once;
   static cudaError_t status = cudaSuccess;
   std::call_once(once, [] {
-    status = cudaFuncSetAttribute(umma_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, EX_DYN_SMEM);
+    status = cudaFuncSetAttribute(umma_exact_kernel<CM, CN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  EX_DYN_SMEM);
   });
   return status == cudaSuccess ? NLA_OK : cuda_status(status, "cudaFuncSetAttribute(umma_exact_kernel)");
+}
+
+// Cluster shape of the exact kernel, CM x CN output tiles: NLA_EXACT_CLUSTER
+// = "11", "21", "12" or "22" (read once).
+int exact_cluster_shape() {
+  static int shape = [] {
+    const char* v = getenv("NLA_EXACT_CLUSTER");
+    if (v && (!strcmp(v, "11") || !strcmp(v, "21") || !strcmp(v, "12") || !strcmp(v, "22"))) return atoi(v);
+    return EX_DEFAULT_CLUSTER;
+  }();
+  return shape;
+}
+
+template <int CM, int CN>
+int launch_exact_shape(const ExactParams& p, const Staged& A, const Staged& B, cudaStream_t s) {
+  CUtensorMap mA, mB;
+  NLA_TRY(make_map(&mA, A.slices, true, (uint64_t)A.K_pad, (uint64_t)(EX_SLICES * A.rows_pad), BM / CN));
+  NLA_TRY(make_map(&mB, B.slices, true, (uint64_t)B.K_pad, (uint64_t)(EX_SLICES * B.rows_pad), BN / CM));
+  NLA_TRY((ensure_exact_smem<CM, CN>()));
+  const int64_t grid = (int64_t)CM * CN * ((p.tiles_m + CM - 1) / CM) * ((p.tiles_n + CN - 1) / CN);
+  if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "too many output tiles");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(EX_THREADS);
+  cfg.dynamicSmemBytes = EX_DYN_SMEM;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CM * CN;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = CM * CN > 1 ? 1 : 0;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, umma_exact_kernel<CM, CN>, mA, mB, p);
+  if (e != cudaSuccess) return cuda_status(e, "umma_exact_kernel launch");
+  return NLA_OK;
 }
 
 }  // namespace
@@ -918,9 +1049,6 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
     return fail(NLA_ERR_ARG, "exact update: operands not staged for it");
   if (C.t) return fail(NLA_ERR_UNSUPPORTED, "exact update: transposed output view");
   if (K > (1LL << 30)) return fail(NLA_ERR_UNSUPPORTED, "exact update: K too large");
-  CUtensorMap mA, mB;
-  NLA_TRY(make_map(&mA, A.slices, true, (uint64_t)A.K_pad, (uint64_t)(EX_SLICES * A.rows_pad)));
-  NLA_TRY(make_map(&mB, B.slices, true, (uint64_t)B.K_pad, (uint64_t)(EX_SLICES * B.rows_pad)));
   ExactParams p{};
   p.M = (int)M;
   p.N = (int)N;
@@ -951,17 +1079,17 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
   p.alpha = alpha;
   p.ea = A.e;
   p.eb = B.e;
-  const int64_t grid = (int64_t)p.tiles_m * p.tiles_n;
-  if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "too many output tiles");
-  NLA_TRY(ensure_exact_smem());
   // Executed flops of the slice pairs: 2 M N K per pair, half of that when
   // one operand is a staged triangle (its tiles' K ranges are clipped).
   const double tri_frac = (A.tri != 0 || B.tri != 0) ? 0.5 : 1.0;
   TraceScope trace(NLA_K_GEMM_UMMA, s, 2.0 * (double)M * N * (double)K * p.npairs * tri_frac,
                    (double)EX_SLICES * (A.rows_pad + B.rows_pad) * A.K_pad * 2 + 16.0 * (double)M * N);
-  umma_exact_kernel<<<(unsigned)grid, EX_THREADS, EX_DYN_SMEM, s>>>(mA, mB, p);
-  NLA_CHECK_LAUNCH("umma_exact_kernel");
-  return NLA_OK;
+  switch (exact_cluster_shape()) {
+    case 21: return launch_exact_shape<2, 1>(p, A, B, s);
+    case 12: return launch_exact_shape<1, 2>(p, A, B, s);
+    case 22: return launch_exact_shape<2, 2>(p, A, B, s);
+    default: return launch_exact_shape<1, 1>(p, A, B, s);
+  }
 }
 
 // Reads and clears the device error word after synchronising the stream.
