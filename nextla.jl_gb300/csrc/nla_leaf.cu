@@ -11,6 +11,8 @@
 //             in-place update has no hazard).
 #include <mutex>
 
+#include <cstdlib>
+
 #include "nla_leaf.cuh"
 
 namespace nla {
@@ -33,6 +35,13 @@ __global__ void __launch_bounds__(LEAF_THREADS) leaf_solve_wide_kernel(LeafArgs 
   const int64_t c0 = (int64_t)blockIdx.x * CW;
   const int ncols = (int)(g.m - c0 < CW ? g.m - c0 : CW);
   solve_block_wide<T, CW>(g, c0, ncols, smem_raw, typename Elem<T>::compute(1));
+}
+
+__global__ void __launch_bounds__(LEAF_THREADS, 1) leaf_solve_cols_kernel(LeafArgs g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t c0 = (int64_t)blockIdx.x * LEAF_THREADS;
+  const int ncols = (int)(g.m - c0 < LEAF_THREADS ? g.m - c0 : LEAF_THREADS);
+  solve_cols_f64(g, c0, ncols, smem_raw, 1.0);
 }
 
 // Canonical lower-left multiply: X := L X for CW columns.
@@ -139,6 +148,32 @@ int launch_leaf_wide(const LeafArgs& g, cudaStream_t s) {
   return NLA_OK;
 }
 
+bool leaf_cols_enabled() {
+  static const bool on = [] {
+    const char* v = getenv("NLA_LEAF_COLS");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
+int launch_leaf_cols(const LeafArgs& g, cudaStream_t s) {
+  const size_t smem = leaf_cols_smem_elems(g.n) * sizeof(double);
+  const int64_t grid = (g.m + LEAF_THREADS - 1) / LEAF_THREADS;
+  if (g.n > COLS_MAX_N || smem > 200 * 1024) return fail(NLA_ERR_UNSUPPORTED, "leaf: shared memory plan too large");
+  if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "leaf: too many right-hand sides");
+  static std::once_flag once;
+  static cudaError_t st = cudaSuccess;
+  std::call_once(once, [] {
+    st = cudaFuncSetAttribute(leaf_solve_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  });
+  if (st != cudaSuccess) return cuda_status(st, "cudaFuncSetAttribute(leaf_solve_cols_kernel)");
+  TraceScope trace(NLA_K_LEAF_SOLVE, s, (double)g.n * g.n * (double)g.m,
+                   8.0 * ((double)g.n * (g.n + 1) / 2 + 2.0 * (double)g.n * g.m));
+  leaf_solve_cols_kernel<<<(unsigned)grid, LEAF_THREADS, smem, s>>>(g);
+  NLA_CHECK_LAUNCH("leaf_solve_cols_kernel");
+  return NLA_OK;
+}
+
 // Wide solve blocks: the widest of 128/64/32 right-hand sides whose block
 // fits 128 KiB of shared memory and still gives two CTAs per SM; 0 when the
 // row-parallel kernel is the better choice (few right-hand sides).
@@ -191,6 +226,11 @@ int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m
   }
   g.rev = uplo == 'U';
   if (func == 'S') {
+    // Float64 blocks of up to 128 rows with enough right-hand sides to fill
+    // the GPU: one right-hand side per thread (NLA_LEAF_COLS=0 selects the
+    // panel-parallel kernel instead).
+    if (dtype == NLA_F64 && n <= COLS_MAX_N && m >= 8 * LEAF_THREADS && leaf_cols_enabled())
+      return launch_leaf_cols(g, s);
     const int cw = wide_cols(n, m, dtype == NLA_F64 ? 8 : 4);
     if (cw) {
       switch (dtype) {

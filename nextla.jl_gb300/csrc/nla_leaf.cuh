@@ -70,15 +70,31 @@ __device__ __forceinline__ void stage_slab(const LeafArgs& g, Tc* slab, int r0, 
   }
 }
 
-template <typename T, typename Tc, int CW>
+// With BATCH > 1 the loads are issued in batches of BATCH per thread before
+// any is used, so that a CTA that is alone on its SM keeps many requests in
+// flight; kernels with several CTAs per SM use BATCH = 1 (fewer registers).
+template <typename T, typename Tc, int CW, int BATCH = 1>
 __device__ __forceinline__ void load_block(const LeafArgs& g, Tc* X, int64_t c0, int ncols, Tc alpha = Tc(1)) {
   const T* B = static_cast<const T*>(g.B);
   const int total = g.n * CW;
-  for (int idx = threadIdx.x; idx < total; idx += LEAF_THREADS) {
-    int i, c;
-    if (!g.tB) { i = idx % g.n; c = idx / g.n; }
-    else { c = idx % CW; i = idx / CW; }
-    X[i * CW + c] = c < ncols ? alpha * Elem<T>::load(B + b_off<T>(g, i, c0 + c)) : Tc(0);
+  for (int base = threadIdx.x; base < total; base += LEAF_THREADS * BATCH) {
+    Tc v[BATCH];
+#pragma unroll
+    for (int u = 0; u < BATCH; ++u) {
+      const int idx = base + u * LEAF_THREADS;
+      int i, c;
+      if (!g.tB) { i = idx % g.n; c = idx / g.n; }
+      else { c = idx % CW; i = idx / CW; }
+      v[u] = idx < total && c < ncols ? alpha * Elem<T>::load(B + b_off<T>(g, i, c0 + c)) : Tc(0);
+    }
+#pragma unroll
+    for (int u = 0; u < BATCH; ++u) {
+      const int idx = base + u * LEAF_THREADS;
+      int i, c;
+      if (!g.tB) { i = idx % g.n; c = idx / g.n; }
+      else { c = idx % CW; i = idx / CW; }
+      if (idx < total) X[i * CW + c] = v[u];
+    }
   }
 }
 
@@ -326,6 +342,91 @@ __device__ __forceinline__ void solve_block_wide(const LeafArgs& g, int64_t c0, 
   }
   __syncthreads();
   store_block<T, Tc, CW>(g, X, c0, ncols);
+}
+
+// Float64 solve with one right-hand side per thread, for n <= COLS_MAX_N and
+// LEAF_THREADS columns per CTA.  GB300 issues FP64 at two fused multiply-adds
+// per clock per SM: a warp instruction holds its sub-partition's FP64 unit for
+// 64 clocks.  The fastest schedule therefore keeps one warp per
+// sub-partition issuing independent FMAs and has no serial single-warp phase.
+//
+// The kernel works left-looking over 32-row panels.  Each thread keeps its
+// panel's 32 values in registers, y, and does two steps:
+//   1. Subtract the already solved rows of its column,
+//      y -= A[p0:p0+32, 0:p0] x[0:p0]. These are 32 independent FMA chains.
+//   2. Solve the panel's triangle column by column, so that y_i gets its
+//      update as soon as x_j is known.
+// Each thread does n(n-1)/2 FMAs in total. The A rows of the panel are staged
+// once per panel in shared memory and read as warp-wide broadcasts. X stays in
+// shared memory, one column per thread, so accesses are conflict-free.
+constexpr int COLS_MAX_N = 128;
+constexpr int LOAD_BATCH = 16;  // loads in flight per thread (one CTA per SM)
+
+__host__ __device__ constexpr size_t leaf_cols_smem_elems(int n) {
+  return (size_t)n * LEAF_THREADS + (size_t)PANEL * COLS_MAX_N + (size_t)n;
+}
+
+__device__ __forceinline__ void solve_cols_f64(const LeafArgs& g, int64_t c0, int ncols, unsigned char* smem_raw,
+                                               double alpha) {
+  constexpr int CW = LEAF_THREADS;
+  double* X = reinterpret_cast<double*>(smem_raw);  // n x CW
+  double* L = X + (size_t)g.n * CW;                 // PANEL x COLS_MAX_N: rows p0.., columns 0..
+  double* inv_d = L + PANEL * COLS_MAX_N;           // n
+  const int n = g.n;
+  const double* A = static_cast<const double*>(g.A);
+  const int t = threadIdx.x;
+
+  load_block<double, double, CW, LOAD_BATCH>(g, X, c0, ncols, alpha);
+  for (int i = t; i < n; i += LEAF_THREADS) inv_d[i] = 1.0 / A[a_off<double>(g, i, i)];
+  for (int p0 = 0; p0 < n; p0 += PANEL) {
+    const int pw = min(PANEL, n - p0);
+    const int kw = p0 + pw;  // columns of A the panel's rows reach (through the diagonal)
+    __syncthreads();         // previous panel done with L (and X, inv_d ready)
+    // Stage A[p0 + i][k], i < PANEL, k < kw; zero on and above the diagonal
+    // and below the block.  Threads run along the index contiguous in memory.
+    for (int base = t; base < PANEL * kw; base += LEAF_THREADS * LOAD_BATCH) {
+      double v[LOAD_BATCH];
+#pragma unroll
+      for (int u = 0; u < LOAD_BATCH; ++u) {
+        const int idx = base + u * LEAF_THREADS;
+        int i, k;
+        if (!g.tA) { i = idx % PANEL; k = idx / PANEL; }
+        else { k = idx % kw; i = idx / kw; }
+        v[u] = idx < PANEL * kw && i < pw && k < p0 + i ? A[a_off<double>(g, p0 + i, k)] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < LOAD_BATCH; ++u) {
+        const int idx = base + u * LEAF_THREADS;
+        int i, k;
+        if (!g.tA) { i = idx % PANEL; k = idx / PANEL; }
+        else { k = idx % kw; i = idx / kw; }
+        if (idx < PANEL * kw) L[i * COLS_MAX_N + k] = v[u];
+      }
+    }
+    __syncthreads();
+    double y[PANEL];
+#pragma unroll
+    for (int i = 0; i < PANEL; ++i) y[i] = i < pw ? X[(p0 + i) * CW + t] : 0.0;
+    for (int k = 0; k < p0; ++k) {
+      const double xk = X[k * CW + t];
+#pragma unroll
+      for (int i = 0; i < PANEL; ++i) y[i] = fma(-L[i * COLS_MAX_N + k], xk, y[i]);
+    }
+#pragma unroll
+    for (int j = 0; j < PANEL; ++j) {
+      if (j < pw) {
+        const double xj = y[j] * inv_d[p0 + j];
+        y[j] = xj;
+#pragma unroll
+        for (int i = j + 1; i < PANEL; ++i) y[i] = fma(-L[i * COLS_MAX_N + p0 + j], xj, y[i]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < PANEL; ++i)
+      if (i < pw) X[(p0 + i) * CW + t] = y[i];
+  }
+  __syncthreads();
+  store_block<double, double, CW>(g, X, c0, ncols);
 }
 
 __host__ __device__ constexpr size_t leaf_solve_smem_elems(int n, int CW) {

@@ -257,7 +257,7 @@ constexpr int EX_THREADS = 320;  // producer, MMA, 8 epilogue warps
 constexpr int EX_CHUNK = 16;     // k-blocks per exact chunk (1024 values)
 constexpr int EX_SLICES = 7;
 constexpr int EX_MAX_PAIRS = 28;
-constexpr int EX_STAGES = 7;                // 224 KiB of stages: the loads in flight bound the rate
+constexpr int EX_STAGES = 6;  // 192 KiB of stages (seven measured no faster)
 constexpr int EX_STAGE_BYTES = 2 * TILE_BYTES;
 constexpr int EX_DYN_SMEM = EX_STAGES * EX_STAGE_BYTES + 1024 + 256;
 static_assert(EX_DYN_SMEM + 16 <= 232448, "exact kernel shared memory above the per-block limit");
@@ -635,11 +635,16 @@ __global__ void __launch_bounds__(256) row_exp_kernel(const T* __restrict__ X, i
     atomicMax(&e[i0 + threadIdx.x], se[threadIdx.x]);
 }
 
-template <typename S> __device__ __forceinline__ S from_int(int v);
-template <> __device__ __forceinline__ __nv_bfloat16 from_int<__nv_bfloat16>(int v) {
-  return __float2bfloat16_rn((float)v);
+// Two slice values (small integers held exactly in floats) packed for one
+// 32-bit store.  A BF16 slice value has at most 8 significant bits, so its
+// BF16 pattern is the upper half of its float pattern.
+template <typename S> __device__ __forceinline__ uint32_t pack_slices(float a, float b);
+template <> __device__ __forceinline__ uint32_t pack_slices<__nv_bfloat16>(float a, float b) {
+  return (__float_as_uint(a) >> 16) | (__float_as_uint(b) & 0xFFFF0000u);
 }
-template <> __device__ __forceinline__ __half from_int<__half>(int v) { return __float2half_rn((float)v); }
+template <> __device__ __forceinline__ uint32_t pack_slices<__half>(float a, float b) {
+  return (uint32_t)__half_as_ushort(__float2half_rn(a)) | ((uint32_t)__half_as_ushort(__float2half_rn(b)) << 16);
+}
 
 // Two adjacent slice values packed for one 32-bit store.
 template <typename S> __device__ __forceinline__ uint32_t pack2(S a, S b) {
@@ -714,18 +719,33 @@ __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int
       continue;
     } else {
       const int ex = gi < rows ? e[gi] : SENTINEL_EXP;
-      long long y0 = fixed_of(tile[i][k], ex), y1 = fixed_of(tile[i][k + 1], ex);
+      // Balanced digits by bias: with Z = Y + sum_p 2^(beta-1) 2^(sigma_p)
+      // + 2^(sigma_last - 1) and sigma_p = 62 - beta (p + 1), the digit
+      // s_p = ((Z >> sigma_p) mod 2^beta) - 2^(beta-1) (the top digit keeps
+      // all high bits) lies in [-2^(beta-1), 2^(beta-1)), and sum_p s_p
+      // 2^(sigma_p) is Y rounded half up at 2^(sigma_last).  Each digit is a
+      // constant shift and mask; |Y| < 2^61 keeps Z inside 64 bits.
+      constexpr long long BIAS = [] {
+        long long b = 1ll << (62 - BETA * NS - 1);
+        for (int p = 0; p < NS; ++p) b += 1ll << (62 - BETA * (p + 1) + BETA - 1);
+        return b;
+      }();
+      const long long z0 = fixed_of(tile[i][k], ex) + BIAS, z1 = fixed_of(tile[i][k + 1], ex) + BIAS;
       float mag = 0.0f;
 #pragma unroll
       for (int sl = 0; sl < NS; ++sl) {
-        const int shift = 62 - BETA * (sl + 1);
-        const long long s0 = (y0 + (1ll << (shift - 1))) >> shift;
-        const long long s1 = (y1 + (1ll << (shift - 1))) >> shift;
-        y0 -= s0 << shift;
-        y1 -= s1 << shift;
-        o[sl * (slice_elems / 2)] = pack2<Sl>(from_int<Sl>((int)s0), from_int<Sl>((int)s1));
+        const int sigma = 62 - BETA * (sl + 1);
+        constexpr int HALF = 1 << (BETA - 1);
+        const int d0 = sl == 0 ? (int)(z0 >> sigma) - HALF : (int)((unsigned long long)z0 >> sigma & (2 * HALF - 1)) - HALF;
+        const int d1 = sl == 0 ? (int)(z1 >> sigma) - HALF : (int)((unsigned long long)z1 >> sigma & (2 * HALF - 1)) - HALF;
+        // Small integers as floats without a conversion instruction: the
+        // integer added to the bit pattern of 1.5 * 2^23 lands in the
+        // mantissa's last place.
+        const float f0 = __int_as_float(0x4B400000 + d0) - 12582912.0f;
+        const float f1 = __int_as_float(0x4B400000 + d1) - 12582912.0f;
+        o[sl * (slice_elems / 2)] = pack_slices<Sl>(f0, f1);
         // 2^(-beta (sl + 1)) built from its exponent bits (exact).
-        mag += (fabsf((float)s0) + fabsf((float)s1)) * __int_as_float((127 - BETA * (sl + 1)) << 23);
+        mag += (fabsf(f0) + fabsf(f1)) * __int_as_float((127 - BETA * (sl + 1)) << 23);
       }
       if (nrm) {
         for (int off = 16; off > 0; off >>= 1) mag += __shfl_xor_sync(0xffffffffu, mag, off);

@@ -205,3 +205,36 @@ def test_gemm_update_matches_oracle(pkg, oracle, cuda):
         pkg.GEMM_SUB_(Cd, a.T if t1 else a, b.T if t2 else b)
         torch.cuda.synchronize()
         assert oracle.rel_err(to_host(Cd), ref) < TOL[dtype]
+
+
+@pytest.mark.parametrize("side,uplo", [("L", "L"), ("L", "U"), ("R", "L"), ("R", "U")])
+def test_f64_leaf_one_rhs_per_thread(pkg, oracle, workloads, cuda, side, uplo):
+    """Float64 diagonal blocks of up to 128 rows with at least 1024 right-hand
+    sides take the one-right-hand-side-per-thread kernel (left-looking 32-row
+    panels): partial panels, a partial last CTA (1100 = 8 x 128 + 76), both
+    transposes, against the oracle and BLAS at the Float64 bound."""
+    for n, trans in itertools.product([1, 5, 31, 32, 33, 100, 128], "NT"):
+        A, B = workloads.problem(n, 1100, side, uplo, seed=n)
+        X = _run(pkg, cuda, side, uplo, trans, 0.5, "S", A, B, np.float64, True)
+        ref = oracle.rectrxm(side, uplo, trans, 0.5, "S", A, B)
+        assert oracle.rel_err(X, ref) < 1e-14, (n, side, uplo, trans)
+        assert oracle.rel_err(X, oracle.blas_rectrxm(side, uplo, trans, 0.5, "S", A, B)) < 1e-14
+
+
+def test_f64_leaf_one_rhs_per_thread_exact(pkg, cuda):
+    """Integer systems with power-of-two diagonals are solved exactly by every
+    operation order: the one-right-hand-side-per-thread kernel must return the
+    integers bit for bit."""
+    import torch
+
+    rng = np.random.default_rng(11)
+    for n in (64, 100, 128):
+        L = np.tril(rng.integers(-3, 4, (n, n)), -1).astype(np.int64)
+        L[np.diag_indices(n)] = 2 ** rng.integers(0, 3, n)
+        X = rng.integers(-8, 9, (n, 1100)).astype(np.int64)
+        B = L @ X
+        Ad = to_dev(L.astype(np.float64), np.float64, cuda)
+        Bd = to_dev(B.astype(np.float64), np.float64, cuda)
+        pkg.unified_rectrxm_("L", "L", "N", 1.0, "S", Ad, Bd, native=True)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(to_host(Bd), X.astype(np.float64))
