@@ -264,6 +264,32 @@ def run_batched(args):
     trace = _lib.trace_summary()
     loop_ms = timed("loop", max(1, min(args.steps, 2)))
     items, grid, _ = plan.info()
+    mixed = None
+    if dtype == torch.float64:
+        # Mixed-precision form: Float32 solves refined with Float64 residuals,
+        # against the plain Float64 answer of the same batch.
+        B.copy_(B0)
+        plan.solve(1.0, A, B, mode="graph")
+        X64 = B.clone()
+        ref = float(torch.linalg.norm(X64))
+        mixed = []
+        for sweeps in (0, 1, 2, 3):
+            def mstep():
+                B.copy_(B0)
+                plan.solve_mixed(1.0, A, B, sweeps=sweeps)
+            for _ in range(args.warmup):
+                mstep()
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                mstep()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            mms = e0.elapsed_time(e1) / args.steps
+            mixed.append({"sweeps": sweeps, "ms": mms, "tflops": flops / (mms / 1e3) / 1e12,
+                          "rel_err_vs_fp64": float(torch.linalg.norm(B - X64)) / ref})
+        del X64
     line = {
         "metric": "batched_trsm_tflops", "value": flops / (ms / 1e3) / 1e12, "unit": "TFLOP/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -275,6 +301,8 @@ def run_batched(args):
         "speedup_vs_one_launch_per_system": loop_ms / ms,
         "trace": {k: {"launches": v[0], "ms": v[1]} for k, v in trace.items()},
     }
+    if mixed is not None:
+        line["mixed_refined"] = mixed
     print(json.dumps(line), flush=True)
     plan.close()
     return 0

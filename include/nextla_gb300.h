@@ -236,6 +236,18 @@ NLA_API int nla_batch_solve(nla_batch_plan plan, double alpha, const void* A_poo
 NLA_API int nla_batch_plan_destroy(nla_batch_plan plan);
 
 /*
+ * Mixed-precision form of a Float64 batch (plan created with NLA_F64; no
+ * counterpart in the reference).  Every system is solved in Float32 (A_i and
+ * alpha B_i rounded to Float32) and then refined `sweeps` times (0..8):
+ * R_i = alpha B_i - op(A_i) X_i in Float64, a Float32 solve of op(A_i) D_i =
+ * R_i, X_i += D_i.  X_i (Float64) replaces B_i.  The elements of A and B must
+ * lie in the Float32 range.  The plan allocates Float32 copies of the pools
+ * and a Float64 residual buffer on first use and keeps them until destroyed.
+ */
+NLA_API int nla_batch_solve_mixed(nla_batch_plan plan, double alpha, const void* A_pool, void* B_pool, int sweeps,
+                                  void* stream);
+
+/*
  * Measured throughput (TFLOP/s) of the pipes the plain paths use on the
  * current GPU (no counterpart in the reference): FP64 FMA on CUDA cores,
  * FP64 mma.sync m8n8k4, FP32 FMA.  Any output pointer may be NULL.  Runs a

@@ -77,6 +77,7 @@ SIGNATURES.update({
     "nla_batch_plan_info": ([_p, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_d)], _i32),
     "nla_batch_solve": ([_p, _d, _p, _p, _i32, _p], _i32),
     "nla_batch_plan_destroy": ([_p], _i32),
+    "nla_batch_solve_mixed": ([_p, _d, _p, _p, _i32, _p], _i32),
 })
 
 SIGNATURES["nla_measure_pipes"] = ([ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d), _p], _i32)

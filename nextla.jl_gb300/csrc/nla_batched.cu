@@ -38,6 +38,13 @@ struct nla_batch_plan_s {
   const void* g_A;
   void* g_B;
   double flops;
+  // Mixed-precision form (Float64 plans): pool extents in elements and the
+  // plan-owned Float32 pools and Float64 residual buffer (allocated on first
+  // use).
+  int64_t a_elems, b_elems;
+  float* a32;
+  float* x32;
+  double* r64;
 };
 
 namespace nla {
@@ -93,6 +100,131 @@ __global__ void __launch_bounds__(LEAF_THREADS) batched_solve_kernel(BatchArgs a
     else solve_block<T, 32>(g, w.c0, ncols, smem_raw, al);
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision batch (Float32 solves, Float64 residuals).  Every kernel
+// below works on the plan's items, one CTA per item, so only the systems'
+// own elements of the caller's pools are read or written.
+// ---------------------------------------------------------------------------
+enum MapOp { MAP_INIT = 0, MAP_SET = 1, MAP_ADD = 2 };
+
+struct MapArgs {
+  const nla_batch_desc* descs;
+  const BatchItem* items;
+  const double* A64;
+  float* A32;
+  double* B64;
+  double* R64;
+  float* X32;
+  double alpha;
+  int op;
+};
+
+// MAP_INIT: R = alpha B (Float64), X32 = (float) R, and (first item of each
+// system) A32 = (float) A over the n x n block; MAP_SET: B = (double) X32;
+// MAP_ADD: B += (double) X32.  Elements are the item's n x ncols block.
+__global__ void __launch_bounds__(256) batched_map_kernel(MapArgs a) {
+  const BatchItem w = a.items[blockIdx.x];
+  const nla_batch_desc d = a.descs[w.sys];
+  const int n = (int)d.n;
+  const int ncols = (int)(d.m - w.c0 < w.cw ? d.m - w.c0 : w.cw);
+  const int total = n * ncols;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int64_t o = d.b_off + (int64_t)(idx % n) + (int64_t)(w.c0 + idx / n) * d.ldb;
+    if (a.op == MAP_INIT) {
+      const double r = a.alpha * a.B64[o];
+      a.R64[o] = r;
+      a.X32[o] = (float)r;
+    } else if (a.op == MAP_SET) {
+      a.B64[o] = (double)a.X32[o];
+    } else {
+      a.B64[o] += (double)a.X32[o];
+    }
+  }
+  if (a.op == MAP_INIT && w.c0 == 0) {
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+      const int64_t o = d.a_off + (int64_t)(idx % n) + (int64_t)(idx / n) * d.lda;
+      a.A32[o] = (float)a.A64[o];
+    }
+  }
+}
+
+struct ResidualArgs {
+  const nla_batch_desc* descs;
+  const BatchItem* items;
+  const double* A64;
+  const double* X64;  // current solution (the caller's B pool)
+  const double* R64;  // alpha B
+  float* D32;         // out: the residual, rounded to Float32
+  int tA, rev;
+};
+
+// D32 = (float)(R - L X) on the item's n x ncols block, L the canonical lower
+// triangle (diagonal included) of op(A): the block's X is staged in shared
+// memory and each 128-row band is formed with the register-tiled product of
+// the diagonal-block kernels, summing in Float64.
+template <int CW>
+__device__ __forceinline__ void residual_block(const ResidualArgs& a, const BatchItem& w, const nla_batch_desc& d,
+                                               unsigned char* smem_raw) {
+  LeafArgs g;
+  g.A = a.A64 + d.a_off;
+  g.lda = d.lda;
+  g.tA = a.tA;
+  g.B = const_cast<double*>(a.X64) + d.b_off;
+  g.ldb = d.ldb;
+  g.tB = 0;
+  g.rev = a.rev;
+  g.n = (int)d.n;
+  g.m = d.m;
+  const int ncols = (int)(d.m - w.c0 < CW ? d.m - w.c0 : CW);
+  double* X = reinterpret_cast<double*>(smem_raw);  // n x CW
+  double* slab = X + (size_t)g.n * CW;              // 128 x 33
+  load_block<double, double, CW>(g, X, w.c0, ncols);
+  __syncthreads();
+  constexpr int CT = CW / 4;
+  const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;
+  const double* R = a.R64 + d.b_off;
+  float* D = a.D32 + d.b_off;
+  for (int r0 = 0; r0 < g.n; r0 += LEAF_THREADS) {
+    const int rows = min(LEAF_THREADS, g.n - r0);
+    const int kmax = min(g.n, r0 + rows);
+    double acc[4][CT];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int c = 0; c < CT; ++c) acc[i][c] = 0.0;
+    for (int k0 = 0; k0 < kmax; k0 += PANEL) {
+      const int kw = min(PANEL, kmax - k0);
+      stage_slab<LEAF_THREADS, double>(g, slab, r0, rows, k0, kw, [](int i, int j) { return j <= i; });
+      __syncthreads();
+      tile_product<double, CW>(slab, X + (size_t)k0 * CW, kw, rows, acc);
+      __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = tr + 32 * i;
+      if (r < rows) {
+#pragma unroll
+        for (int c = 0; c < CT; ++c) {
+          const int col = tc * CT + c;
+          if (col < ncols) {
+            const int64_t o = b_off<double>(g, r0 + r, w.c0 + col);
+            D[o] = (float)(R[o] - acc[i][c]);
+          }
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(LEAF_THREADS, 1) batched_residual_kernel(ResidualArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const BatchItem w = a.items[blockIdx.x];
+  const nla_batch_desc d = a.descs[w.sys];
+  if (w.cw == 8) residual_block<8>(a, w, d, smem_raw);
+  else if (w.cw == 16) residual_block<16>(a, w, d, smem_raw);
+  else residual_block<32>(a, w, d, smem_raw);
 }
 
 int bucket_of(int64_t n) {
@@ -181,6 +313,11 @@ int nla_batch_plan_create(nla_batch_plan* out, int dtype, char uplo, char trans,
   p->n_max = 1;
   p->cw_max = 8;
   p->flops = 0;
+  p->a_elems = 0;
+  p->b_elems = 0;
+  p->a32 = nullptr;
+  p->x32 = nullptr;
+  p->r64 = nullptr;
   for (int64_t i = 0; i < count; ++i) {
     const nla_batch_desc& d = descs[i];
     if (d.n < 0 || d.m < 0 || d.n > 1024 || d.lda < (d.n > 1 ? d.n : 1) || d.ldb < (d.n > 1 ? d.n : 1) ||
@@ -189,6 +326,8 @@ int nla_batch_plan_create(nla_batch_plan* out, int dtype, char uplo, char trans,
       return fail(NLA_ERR_ARG, "system " + std::to_string(i) + ": bad size, leading dimension or offset");
     }
     if (d.n == 0 || d.m == 0) continue;
+    p->a_elems = std::max<int64_t>(p->a_elems, d.a_off + (d.n - 1) * d.lda + d.n);
+    p->b_elems = std::max<int64_t>(p->b_elems, d.b_off + (d.m - 1) * d.ldb + d.n);
     const int c = cw[bucket_of(d.n)];
     p->n_max = std::max<int>(p->n_max, (int)d.n);
     p->cw_max = std::max(p->cw_max, c);
@@ -300,9 +439,70 @@ int nla_batch_solve(nla_batch_plan p, double alpha, const void* A_pool, void* B_
   return e == cudaSuccess ? NLA_OK : cuda_status(e, "batch graph launch");
 }
 
+int nla_batch_solve_mixed(nla_batch_plan p, double alpha, const void* A_pool, void* B_pool, int sweeps,
+                          void* stream) {
+  clear_error();
+  if (!p) return fail(NLA_ERR_ARG, "null plan");
+  if (p->dtype != NLA_F64) return fail(NLA_ERR_DTYPE, "mixed batch: the plan must be Float64");
+  if (sweeps < 0 || sweeps > 8) return fail(NLA_ERR_ARG, "mixed batch: sweeps must be 0..8");
+  if (p->nitems == 0) return NLA_OK;
+  if (!A_pool || !B_pool) return fail(NLA_ERR_ARG, "null pool pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!p->a32) {
+    cudaError_t e = cudaMalloc(&p->a32, sizeof(float) * (size_t)p->a_elems);
+    if (e == cudaSuccess) e = cudaMalloc(&p->x32, sizeof(float) * (size_t)p->b_elems);
+    if (e == cudaSuccess) e = cudaMalloc(&p->r64, sizeof(double) * (size_t)p->b_elems);
+    if (e != cudaSuccess) {
+      cudaFree(p->a32);
+      cudaFree(p->x32);
+      cudaFree(p->r64);
+      p->a32 = nullptr;
+      p->x32 = nullptr;
+      p->r64 = nullptr;
+      return cuda_status(e, "mixed batch buffers");
+    }
+  }
+  NLA_TRY(batched_smem_attr<float>(p->smem));
+  static std::once_flag once;
+  static cudaError_t st = cudaSuccess;
+  std::call_once(once, [] {
+    st = cudaFuncSetAttribute(batched_residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  });
+  if (st != cudaSuccess) return cuda_status(st, "cudaFuncSetAttribute(batched_residual_kernel)");
+  const auto* descs = static_cast<const nla_batch_desc*>(p->d_descs);
+  const auto* items = static_cast<const BatchItem*>(p->d_items);
+  double* B64 = static_cast<double*>(B_pool);
+  const double* A64 = static_cast<const double*>(A_pool);
+  TraceScope trace(NLA_K_BATCHED, s, p->flops, 0.0);
+  MapArgs m{descs, items, A64, p->a32, B64, p->r64, p->x32, alpha, MAP_INIT};
+  batched_map_kernel<<<p->nitems, 256, 0, s>>>(m);
+  NLA_CHECK_LAUNCH("batched_map_kernel");
+  auto solve32 = [&]() -> int {
+    cudaMemsetAsync(p->d_counter, 0, sizeof(int), s);
+    return launch_batched<float>(p, 1.0, p->a32, p->x32, s);
+  };
+  NLA_TRY(solve32());
+  m.op = MAP_SET;
+  batched_map_kernel<<<p->nitems, 256, 0, s>>>(m);
+  NLA_CHECK_LAUNCH("batched_map_kernel");
+  const ResidualArgs r{descs, items, A64, B64, p->r64, p->x32, p->tA, p->rev};
+  for (int k = 0; k < sweeps; ++k) {
+    batched_residual_kernel<<<p->nitems, LEAF_THREADS, p->smem, s>>>(r);
+    NLA_CHECK_LAUNCH("batched_residual_kernel");
+    NLA_TRY(solve32());
+    m.op = MAP_ADD;
+    batched_map_kernel<<<p->nitems, 256, 0, s>>>(m);
+    NLA_CHECK_LAUNCH("batched_map_kernel");
+  }
+  return NLA_OK;
+}
+
 int nla_batch_plan_destroy(nla_batch_plan p) {
   clear_error();
   if (!p) return NLA_OK;
+  cudaFree(p->a32);
+  cudaFree(p->x32);
+  cudaFree(p->r64);
   if (p->exec) cudaGraphExecDestroy(p->exec);
   cudaStreamDestroy(p->cap_stream);
   cudaFree(p->d_descs);

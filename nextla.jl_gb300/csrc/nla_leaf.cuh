@@ -380,7 +380,9 @@ __device__ __forceinline__ void solve_cols_f64(const LeafArgs& g, int64_t c0, in
   for (int i = t; i < n; i += LEAF_THREADS) inv_d[i] = 1.0 / A[a_off<double>(g, i, i)];
   for (int p0 = 0; p0 < n; p0 += PANEL) {
     const int pw = min(PANEL, n - p0);
-    const int kw = p0 + pw;  // columns of A the panel's rows reach (through the diagonal)
+    // Columns of A staged for the panel's rows: through the diagonal, rounded
+    // up to even for the paired loads (the extra column is zero).
+    const int kw = (p0 + pw + 1) & ~1;
     __syncthreads();         // previous panel done with L (and X, inv_d ready)
     // Stage A[p0 + i][k], i < PANEL, k < kw; zero on and above the diagonal
     // and below the block.  Threads run along the index contiguous in memory.
@@ -407,18 +409,48 @@ __device__ __forceinline__ void solve_cols_f64(const LeafArgs& g, int64_t c0, in
     double y[PANEL];
 #pragma unroll
     for (int i = 0; i < PANEL; ++i) y[i] = i < pw ? X[(p0 + i) * CW + t] : 0.0;
-    for (int k = 0; k < p0; ++k) {
-      const double xk = X[k * CW + t];
+    // Two k per step with one 16-byte broadcast load of A per row (p0 is a
+    // multiple of 32): half a shared-memory load per FMA, and the unrolled
+    // steps let the loads of the next step overlap the FMAs of this one
+    // (with one warp per SM sub-partition nothing else hides their latency).
+    // The two FMAs into each y[i] of a step are PANEL instructions apart (a
+    // DFMA result is not ready for the next instruction of the same warp).
+    for (int k = 0; k < p0; k += 2) {
+      const double xk0 = X[k * CW + t], xk1 = X[(k + 1) * CW + t];
+      double2 a[PANEL];
 #pragma unroll
-      for (int i = 0; i < PANEL; ++i) y[i] = fma(-L[i * COLS_MAX_N + k], xk, y[i]);
+      for (int i = 0; i < PANEL; ++i) a[i] = *reinterpret_cast<const double2*>(&L[i * COLS_MAX_N + k]);
+#pragma unroll
+      for (int i = 0; i < PANEL; ++i) y[i] = fma(-a[i].x, xk0, y[i]);
+#pragma unroll
+      for (int i = 0; i < PANEL; ++i) y[i] = fma(-a[i].y, xk1, y[i]);
     }
+    if (pw == PANEL) {
+      // Full panel: the triangle two columns at a time (x_j, then x_{j+1},
+      // then one paired load and two FMAs for each row below).
 #pragma unroll
-    for (int j = 0; j < PANEL; ++j) {
-      if (j < pw) {
+      for (int jj = 0; jj < PANEL / 2; ++jj) {
+        const int j = 2 * jj;
         const double xj = y[j] * inv_d[p0 + j];
+        const double xj1 = fma(-L[(j + 1) * COLS_MAX_N + p0 + j], xj, y[j + 1]) * inv_d[p0 + j + 1];
         y[j] = xj;
+        y[j + 1] = xj1;
 #pragma unroll
-        for (int i = j + 1; i < PANEL; ++i) y[i] = fma(-L[i * COLS_MAX_N + p0 + j], xj, y[i]);
+        for (int i = j + 2; i < PANEL; ++i) {
+          const double2 a = *reinterpret_cast<const double2*>(&L[i * COLS_MAX_N + p0 + j]);
+          y[i] = fma(-a.x, xj, y[i]);
+          y[i] = fma(-a.y, xj1, y[i]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < PANEL; ++j) {
+        if (j < pw) {
+          const double xj = y[j] * inv_d[p0 + j];
+          y[j] = xj;
+#pragma unroll
+          for (int i = j + 1; i < PANEL; ++i) y[i] = fma(-L[i * COLS_MAX_N + p0 + j], xj, y[i]);
+        }
       }
     }
 #pragma unroll

@@ -92,3 +92,34 @@ def test_tuner_writes_cache(pkg, cuda, tmp_path, monkeypatch):
     data = json.load(open(tmp_path / "tune.json"))
     assert tune.lookup(torch.float32, cuda) == chosen
     assert torch.cuda.get_device_name(cuda) in data
+
+
+def test_batched_mixed_refinement_converges(pkg, cuda):
+    """Float32 solves refined with Float64 residuals (nla_batch_solve_mixed):
+    with no sweep the batch carries Float32-level error; each sweep shrinks it
+    and two sweeps reach the plain Float64 answer to Float64 accuracy.  Systems
+    span every size bucket, both transposes and a partial last item."""
+    import torch
+
+    from nextla_gb300 import batched
+
+    rng = np.random.default_rng(21)
+    n = rng.integers(1, 700, 60)
+    n[:6] = [1, 16, 31, 64, 513, 1024]
+    m = rng.integers(1, 70, 60)
+    for trans in "NT":
+        A, B0, systems = batched.make_batch(n, m, torch.float64, cuda, seed=5)
+        plan = batched.BatchPlan(torch.float64, "L", trans, systems)
+        X = B0.clone()
+        plan.solve(0.5, A, X, mode="persistent")
+        ref = float(torch.linalg.norm(X))
+        errs = []
+        for sweeps in (0, 1, 2):
+            Y = B0.clone()
+            plan.solve_mixed(0.5, A, Y, sweeps=sweeps)
+            torch.cuda.synchronize()
+            errs.append(float(torch.linalg.norm(Y - X)) / ref)
+        plan.close()
+        assert 1e-9 < errs[0] < 1e-5, (trans, errs)
+        assert errs[1] < errs[0] * 1e-3, (trans, errs)
+        assert errs[2] < 1e-14, (trans, errs)
