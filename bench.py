@@ -724,6 +724,20 @@ def main():
     barrier()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_value = world * flops / e2e_s / 1e12
+    # One more step, outside the timed ones, with device events between its
+    # phases: where the end-to-end time goes.
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(stream)
+    Ae.copy_(A_pin, non_blocking=True)
+    Be.copy_(B_pin, non_blocking=True)
+    ev[1].record(stream)
+    solve_fn(Ae.T, Be.T)
+    ev[2].record(stream)
+    X_pin.copy_(Be, non_blocking=True)
+    ev[3].record(stream)
+    barrier()
+    e2e_phases = {"h2d_ms": ev[0].elapsed_time(ev[1]), "solve_ms": ev[1].elapsed_time(ev[2]),
+                  "d2h_ms": ev[2].elapsed_time(ev[3])}
 
     # Roofline of the dominant kernel class.
     pk, pk_kind = peaks()
@@ -777,7 +791,8 @@ def main():
                                        "residual in double-double"},
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (value / plain["tflops"]) if plain else None,
-            "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": int(A_h.nbytes + B_h.nbytes),
+            "e2e": {"value": e2e_value, "unit": "TFLOP/s", "phases_ms": e2e_phases,
+                    "h2d_bytes_per_step": int(A_h.nbytes + B_h.nbytes),
                     "d2h_bytes_per_step": int(B_h.nbytes)},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": gpu_launches,
             "trace": {k: {"launches": v[0], "ms": v[1], "tflops": v[2] / max(v[1], 1e-9) / 1e9}

@@ -160,13 +160,18 @@ struct ResidualArgs {
   int tA, rev;
 };
 
-// D32 = (float)(R - L X) on the item's n x ncols block, L the canonical lower
-// triangle (diagonal included) of op(A): the block's X is staged in shared
-// memory and each 128-row band is formed with the register-tiled product of
-// the diagonal-block kernels, summing in Float64.
+// D32 = (float)(R - L X) on one 128-row band of an item's n x ncols block,
+// L the canonical lower triangle (diagonal included) of op(A).  A band is
+// its own CTA (blockIdx.y), and the X rows it needs are streamed through
+// shared memory 32 at a time, so a CTA holds about 45 KB and several run per
+// SM (the update is bound by the 2-FMA-per-clock DFMA rate, and one CTA per
+// SM leaves it waiting on shared memory).  Each panel is formed with the
+// register-tiled product of the diagonal-block kernels, summing in Float64.
+constexpr int RES_PANEL_ELEMS = PANEL * 32 + LEAF_THREADS * SLAB_PAD;  // X panel (CW <= 32) + slab
+
 template <int CW>
-__device__ __forceinline__ void residual_block(const ResidualArgs& a, const BatchItem& w, const nla_batch_desc& d,
-                                               unsigned char* smem_raw) {
+__device__ __forceinline__ void residual_band(const ResidualArgs& a, const BatchItem& w, const nla_batch_desc& d,
+                                              int r0, double* smem) {
   LeafArgs g;
   g.A = a.A64 + d.a_off;
   g.lda = d.lda;
@@ -178,53 +183,58 @@ __device__ __forceinline__ void residual_block(const ResidualArgs& a, const Batc
   g.n = (int)d.n;
   g.m = d.m;
   const int ncols = (int)(d.m - w.c0 < CW ? d.m - w.c0 : CW);
-  double* X = reinterpret_cast<double*>(smem_raw);  // n x CW
-  double* slab = X + (size_t)g.n * CW;              // 128 x 33
-  load_block<double, double, CW>(g, X, w.c0, ncols);
-  __syncthreads();
+  const int rows = min(LEAF_THREADS, g.n - r0);
+  const int kmax = r0 + rows;  // k <= r
+  double* Xs = smem;                 // PANEL x CW
+  double* slab = smem + PANEL * 32;  // 128 x 33
   constexpr int CT = CW / 4;
   const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;
+  double acc[4][CT];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int c = 0; c < CT; ++c) acc[i][c] = 0.0;
+  const double* X = a.X64 + d.b_off;
+  for (int k0 = 0; k0 < kmax; k0 += PANEL) {
+    const int kw = min(PANEL, kmax - k0);
+    // X rows k0 .. k0 + kw of the item's columns (threads along the rows,
+    // which are contiguous in memory).
+    for (int idx = threadIdx.x; idx < PANEL * CW; idx += LEAF_THREADS) {
+      const int k = idx % PANEL, c = idx / PANEL;
+      Xs[k * CW + c] = k < kw && c < ncols ? X[b_off<double>(g, k0 + k, w.c0 + c)] : 0.0;
+    }
+    stage_slab<LEAF_THREADS, double>(g, slab, r0, rows, k0, kw, [](int i, int j) { return j <= i; });
+    __syncthreads();
+    tile_product<double, CW>(slab, Xs, kw, rows, acc);
+    __syncthreads();
+  }
   const double* R = a.R64 + d.b_off;
   float* D = a.D32 + d.b_off;
-  for (int r0 = 0; r0 < g.n; r0 += LEAF_THREADS) {
-    const int rows = min(LEAF_THREADS, g.n - r0);
-    const int kmax = min(g.n, r0 + rows);
-    double acc[4][CT];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < 4; ++i) {
+    const int r = tr + 32 * i;
+    if (r < rows) {
 #pragma unroll
-      for (int c = 0; c < CT; ++c) acc[i][c] = 0.0;
-    for (int k0 = 0; k0 < kmax; k0 += PANEL) {
-      const int kw = min(PANEL, kmax - k0);
-      stage_slab<LEAF_THREADS, double>(g, slab, r0, rows, k0, kw, [](int i, int j) { return j <= i; });
-      __syncthreads();
-      tile_product<double, CW>(slab, X + (size_t)k0 * CW, kw, rows, acc);
-      __syncthreads();
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int r = tr + 32 * i;
-      if (r < rows) {
-#pragma unroll
-        for (int c = 0; c < CT; ++c) {
-          const int col = tc * CT + c;
-          if (col < ncols) {
-            const int64_t o = b_off<double>(g, r0 + r, w.c0 + col);
-            D[o] = (float)(R[o] - acc[i][c]);
-          }
+      for (int c = 0; c < CT; ++c) {
+        const int col = tc * CT + c;
+        if (col < ncols) {
+          const int64_t o = b_off<double>(g, r0 + r, w.c0 + col);
+          D[o] = (float)(R[o] - acc[i][c]);
         }
       }
     }
   }
 }
 
-__global__ void __launch_bounds__(LEAF_THREADS, 1) batched_residual_kernel(ResidualArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__global__ void __launch_bounds__(LEAF_THREADS) batched_residual_kernel(ResidualArgs a) {
+  __shared__ __align__(16) double smem[RES_PANEL_ELEMS];
   const BatchItem w = a.items[blockIdx.x];
   const nla_batch_desc d = a.descs[w.sys];
-  if (w.cw == 8) residual_block<8>(a, w, d, smem_raw);
-  else if (w.cw == 16) residual_block<16>(a, w, d, smem_raw);
-  else residual_block<32>(a, w, d, smem_raw);
+  const int r0 = (int)blockIdx.y * LEAF_THREADS;
+  if (r0 >= d.n) return;
+  if (w.cw == 8) residual_band<8>(a, w, d, r0, smem);
+  else if (w.cw == 16) residual_band<16>(a, w, d, r0, smem);
+  else residual_band<32>(a, w, d, r0, smem);
 }
 
 int bucket_of(int64_t n) {
@@ -310,6 +320,7 @@ int nla_batch_plan_create(nla_batch_plan* out, int dtype, char uplo, char trans,
   p->count = count;
   p->h_descs.assign(descs, descs + count);
   std::vector<BatchItem> items;
+  int bucket_n_max[NLA_BATCH_BUCKETS] = {0, 0, 0, 0, 0, 0};
   p->n_max = 1;
   p->cw_max = 8;
   p->flops = 0;
@@ -328,7 +339,9 @@ int nla_batch_plan_create(nla_batch_plan* out, int dtype, char uplo, char trans,
     if (d.n == 0 || d.m == 0) continue;
     p->a_elems = std::max<int64_t>(p->a_elems, d.a_off + (d.n - 1) * d.lda + d.n);
     p->b_elems = std::max<int64_t>(p->b_elems, d.b_off + (d.m - 1) * d.ldb + d.n);
-    const int c = cw[bucket_of(d.n)];
+    const int bk = bucket_of(d.n);
+    const int c = cw[bk];
+    bucket_n_max[bk] = std::max<int>(bucket_n_max[bk], (int)d.n);
     p->n_max = std::max<int>(p->n_max, (int)d.n);
     p->cw_max = std::max(p->cw_max, c);
     p->flops += (double)d.n * d.n * d.m;
@@ -342,7 +355,13 @@ int nla_batch_plan_create(nla_batch_plan* out, int dtype, char uplo, char trans,
   });
   p->nitems = (int)items.size();
   const size_t esz = dtype == NLA_F64 ? 8 : 4;
-  p->smem = leaf_solve_smem_elems(p->n_max, p->cw_max) * esz;
+  // Shared memory for the largest block any item stages: n_max of a bucket
+  // times that bucket's width (narrow items for the large systems keep the
+  // plan at two or more CTAs per SM).
+  p->smem = 0;
+  for (int b = 0; b < NLA_BATCH_BUCKETS; ++b)
+    if (bucket_n_max[b] > 0)
+      p->smem = std::max(p->smem, leaf_solve_smem_elems(bucket_n_max[b], cw[b]) * esz);
   int rc = NLA_OK;
   int per_sm = 0;
   if (dtype == NLA_F64) rc = batched_smem_attr<double>(p->smem);
@@ -463,12 +482,6 @@ int nla_batch_solve_mixed(nla_batch_plan p, double alpha, const void* A_pool, vo
     }
   }
   NLA_TRY(batched_smem_attr<float>(p->smem));
-  static std::once_flag once;
-  static cudaError_t st = cudaSuccess;
-  std::call_once(once, [] {
-    st = cudaFuncSetAttribute(batched_residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  });
-  if (st != cudaSuccess) return cuda_status(st, "cudaFuncSetAttribute(batched_residual_kernel)");
   const auto* descs = static_cast<const nla_batch_desc*>(p->d_descs);
   const auto* items = static_cast<const BatchItem*>(p->d_items);
   double* B64 = static_cast<double*>(B_pool);
@@ -487,7 +500,8 @@ int nla_batch_solve_mixed(nla_batch_plan p, double alpha, const void* A_pool, vo
   NLA_CHECK_LAUNCH("batched_map_kernel");
   const ResidualArgs r{descs, items, A64, B64, p->r64, p->x32, p->tA, p->rev};
   for (int k = 0; k < sweeps; ++k) {
-    batched_residual_kernel<<<p->nitems, LEAF_THREADS, p->smem, s>>>(r);
+    batched_residual_kernel<<<dim3((unsigned)p->nitems, (unsigned)((p->n_max + LEAF_THREADS - 1) / LEAF_THREADS)),
+                              LEAF_THREADS, 0, s>>>(r);
     NLA_CHECK_LAUNCH("batched_residual_kernel");
     NLA_TRY(solve32());
     m.op = MAP_ADD;

@@ -37,11 +37,12 @@ __global__ void __launch_bounds__(LEAF_THREADS) leaf_solve_wide_kernel(LeafArgs 
   solve_block_wide<T, CW>(g, c0, ncols, smem_raw, typename Elem<T>::compute(1));
 }
 
-__global__ void __launch_bounds__(LEAF_THREADS, 1) leaf_solve_cols_kernel(LeafArgs g) {
+template <int HALVES>
+__global__ void __launch_bounds__(LEAF_THREADS * HALVES, 1) leaf_solve_cols_kernel(LeafArgs g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int64_t c0 = (int64_t)blockIdx.x * LEAF_THREADS;
   const int ncols = (int)(g.m - c0 < LEAF_THREADS ? g.m - c0 : LEAF_THREADS);
-  solve_cols_f64(g, c0, ncols, smem_raw, 1.0);
+  solve_cols_f64<HALVES>(g, c0, ncols, smem_raw, 1.0);
 }
 
 // Canonical lower-left multiply: X := L X for CW columns.
@@ -148,28 +149,33 @@ int launch_leaf_wide(const LeafArgs& g, cudaStream_t s) {
   return NLA_OK;
 }
 
-bool leaf_cols_enabled() {
-  static const bool on = [] {
+// Threads per right-hand side of the Float64 column-per-thread leaf:
+// NLA_LEAF_COLS = 0 (use the panel-parallel kernels), 1 or 2 (default 2).
+int leaf_cols_mode() {
+  static const int mode = [] {
     const char* v = getenv("NLA_LEAF_COLS");
-    return !(v && v[0] == '0');
+    if (v && (v[0] == '0' || v[0] == '1' || v[0] == '2') && v[1] == 0) return v[0] - '0';
+    return 2;
   }();
-  return on;
+  return mode;
 }
 
+template <int HALVES>
 int launch_leaf_cols(const LeafArgs& g, cudaStream_t s) {
-  const size_t smem = leaf_cols_smem_elems(g.n) * sizeof(double);
+  const size_t smem = leaf_cols_smem_elems(g.n, HALVES) * sizeof(double);
   const int64_t grid = (g.m + LEAF_THREADS - 1) / LEAF_THREADS;
   if (g.n > COLS_MAX_N || smem > 200 * 1024) return fail(NLA_ERR_UNSUPPORTED, "leaf: shared memory plan too large");
   if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "leaf: too many right-hand sides");
   static std::once_flag once;
   static cudaError_t st = cudaSuccess;
   std::call_once(once, [] {
-    st = cudaFuncSetAttribute(leaf_solve_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    st = cudaFuncSetAttribute(leaf_solve_cols_kernel<HALVES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              200 * 1024);
   });
   if (st != cudaSuccess) return cuda_status(st, "cudaFuncSetAttribute(leaf_solve_cols_kernel)");
   TraceScope trace(NLA_K_LEAF_SOLVE, s, (double)g.n * g.n * (double)g.m,
                    8.0 * ((double)g.n * (g.n + 1) / 2 + 2.0 * (double)g.n * g.m));
-  leaf_solve_cols_kernel<<<(unsigned)grid, LEAF_THREADS, smem, s>>>(g);
+  leaf_solve_cols_kernel<HALVES><<<(unsigned)grid, LEAF_THREADS * HALVES, smem, s>>>(g);
   NLA_CHECK_LAUNCH("leaf_solve_cols_kernel");
   return NLA_OK;
 }
@@ -227,10 +233,10 @@ int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m
   g.rev = uplo == 'U';
   if (func == 'S') {
     // Float64 blocks of up to 128 rows with enough right-hand sides to fill
-    // the GPU: one right-hand side per thread (NLA_LEAF_COLS=0 selects the
-    // panel-parallel kernel instead).
-    if (dtype == NLA_F64 && n <= COLS_MAX_N && m >= 8 * LEAF_THREADS && leaf_cols_enabled())
-      return launch_leaf_cols(g, s);
+    // the GPU: one right-hand side per thread, or two threads per right-hand
+    // side (NLA_LEAF_COLS=0 selects the panel-parallel kernels instead).
+    if (dtype == NLA_F64 && n <= COLS_MAX_N && m >= 8 * LEAF_THREADS && leaf_cols_mode() != 0)
+      return leaf_cols_mode() == 1 ? launch_leaf_cols<1>(g, s) : launch_leaf_cols<2>(g, s);
     const int cw = wide_cols(n, m, dtype == NLA_F64 ? 8 : 4);
     if (cw) {
       switch (dtype) {

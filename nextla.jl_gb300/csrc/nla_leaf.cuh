@@ -111,41 +111,30 @@ __device__ __forceinline__ void store_block(const LeafArgs& g, const Tc* X, int6
 }
 
 // acc[i][c] += sum_kk slab[tr + 32 i][kk] * Xp[kk, tc * CW/4 + c] for
-// kk < pw and row slots i < SLOTS: LEAF_THREADS threads as 32 row lanes (tr)
-// x 4 column groups (tc, one warp each, so the X reads are warp-wide
-// broadcasts).  Each k step reads SLOTS slab values and CW/4 values of X for
-// SLOTS * CW/4 fused multiply-adds.
-template <typename Tc, int CW, int SLOTS>
-__device__ __forceinline__ void tile_product_n(const Tc* __restrict__ slab, const Tc* __restrict__ Xp, int pw,
-                                               Tc (&acc)[4][CW / 4]) {
+// kk < pw: LEAF_THREADS threads as 32 row lanes (tr) x 4 column groups (tc,
+// one warp each, so the X reads are warp-wide broadcasts).  Each k step reads
+// 4 slab values and CW/4 values of X for 4 * CW/4 fused multiply-adds.  Row
+// slots past `rows` multiply zeros of the slab: skipping them (with
+// predicates or per-slot-count copies of the body) measured slower in the
+// persistent batched solver, whose CTAs see every chunk height.
+template <typename Tc, int CW>
+__device__ __forceinline__ void tile_product(const Tc* __restrict__ slab, const Tc* __restrict__ Xp, int pw,
+                                             int rows, Tc (&acc)[4][CW / 4]) {
+  (void)rows;
   constexpr int CT = CW / 4;
   const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;
   for (int kk = 0; kk < pw; ++kk) {
-    Tc a[SLOTS];
+    Tc a[4];
 #pragma unroll
-    for (int i = 0; i < SLOTS; ++i) a[i] = slab[(tr + 32 * i) * SLAB_PAD + kk];
+    for (int i = 0; i < 4; ++i) a[i] = slab[(tr + 32 * i) * SLAB_PAD + kk];
     Tc xv[CT];
     const Tc* xr = Xp + kk * CW + tc * CT;
 #pragma unroll
     for (int c = 0; c < CT; ++c) xv[c] = xr[c];
 #pragma unroll
-    for (int i = 0; i < SLOTS; ++i)
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
       for (int c = 0; c < CT; ++c) acc[i][c] = fma(a[i], xv[c], acc[i][c]);
-  }
-}
-
-// Row slots i with 32 i >= rows hold no row of the chunk: the slot count is
-// made a compile-time constant so that the unrolled body carries no
-// predicates.
-template <typename Tc, int CW>
-__device__ __forceinline__ void tile_product(const Tc* __restrict__ slab, const Tc* __restrict__ Xp, int pw,
-                                             int rows, Tc (&acc)[4][CW / 4]) {
-  switch ((rows + 31) >> 5) {
-    case 1: tile_product_n<Tc, CW, 1>(slab, Xp, pw, acc); break;
-    case 2: tile_product_n<Tc, CW, 2>(slab, Xp, pw, acc); break;
-    case 3: tile_product_n<Tc, CW, 3>(slab, Xp, pw, acc); break;
-    default: tile_product_n<Tc, CW, 4>(slab, Xp, pw, acc); break;
   }
 }
 
@@ -362,35 +351,64 @@ __device__ __forceinline__ void solve_block_wide(const LeafArgs& g, int64_t c0, 
 constexpr int COLS_MAX_N = 128;
 constexpr int LOAD_BATCH = 16;  // loads in flight per thread (one CTA per SM)
 
-__host__ __device__ constexpr size_t leaf_cols_smem_elems(int n) {
-  return (size_t)n * LEAF_THREADS + (size_t)PANEL * COLS_MAX_N + (size_t)n;
+// HALVES = 2 runs two threads per right-hand side (256 per CTA): the halves
+// split the already-solved rows of each panel's update, so that every SM
+// sub-partition has two warps issuing FMAs in that phase; half 1 hands its
+// partial sums over through shared memory and half 0 solves the triangle.
+__host__ __device__ constexpr size_t leaf_cols_smem_elems(int n, int halves) {
+  return (size_t)n * LEAF_THREADS + (size_t)PANEL * COLS_MAX_N + (size_t)n +
+         (halves > 1 ? (size_t)PANEL * LEAF_THREADS : 0);
 }
 
+template <int HALVES>
 __device__ __forceinline__ void solve_cols_f64(const LeafArgs& g, int64_t c0, int ncols, unsigned char* smem_raw,
                                                double alpha) {
-  constexpr int CW = LEAF_THREADS;
-  double* X = reinterpret_cast<double*>(smem_raw);  // n x CW
-  double* L = X + (size_t)g.n * CW;                 // PANEL x COLS_MAX_N: rows p0.., columns 0..
-  double* inv_d = L + PANEL * COLS_MAX_N;           // n
+  constexpr int CW = LEAF_THREADS;            // right-hand sides per CTA
+  constexpr int NT = LEAF_THREADS * HALVES;   // threads per CTA
   const int n = g.n;
+  double* X = reinterpret_cast<double*>(smem_raw);  // n x CW
+  double* L = X + (size_t)n * CW;                   // PANEL x COLS_MAX_N: rows p0.., columns 0..
+  double* inv_d = L + PANEL * COLS_MAX_N;           // n
+  double* Y1 = inv_d + n;                           // PANEL x CW partial sums of half 1
   const double* A = static_cast<const double*>(g.A);
-  const int t = threadIdx.x;
+  const double* Bp = static_cast<const double*>(g.B);
+  const int t = threadIdx.x, c = t % CW, h = t / CW;
 
-  load_block<double, double, CW, LOAD_BATCH>(g, X, c0, ncols, alpha);
-  for (int i = t; i < n; i += LEAF_THREADS) inv_d[i] = 1.0 / A[a_off<double>(g, i, i)];
+  // Block of B (times alpha), LOAD_BATCH loads in flight per thread.
+  const int total = n * CW;
+  for (int base = t; base < total; base += NT * LOAD_BATCH) {
+    double v[LOAD_BATCH];
+#pragma unroll
+    for (int u = 0; u < LOAD_BATCH; ++u) {
+      const int idx = base + u * NT;
+      int i, cc;
+      if (!g.tB) { i = idx % n; cc = idx / n; }
+      else { cc = idx % CW; i = idx / CW; }
+      v[u] = idx < total && cc < ncols ? alpha * Bp[b_off<double>(g, i, c0 + cc)] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < LOAD_BATCH; ++u) {
+      const int idx = base + u * NT;
+      int i, cc;
+      if (!g.tB) { i = idx % n; cc = idx / n; }
+      else { cc = idx % CW; i = idx / CW; }
+      if (idx < total) X[i * CW + cc] = v[u];
+    }
+  }
+  for (int i = t; i < n; i += NT) inv_d[i] = 1.0 / A[a_off<double>(g, i, i)];
   for (int p0 = 0; p0 < n; p0 += PANEL) {
     const int pw = min(PANEL, n - p0);
     // Columns of A staged for the panel's rows: through the diagonal, rounded
     // up to even for the paired loads (the extra column is zero).
     const int kw = (p0 + pw + 1) & ~1;
-    __syncthreads();         // previous panel done with L (and X, inv_d ready)
+    __syncthreads();  // previous panel done with L and Y1 (and X, inv_d ready)
     // Stage A[p0 + i][k], i < PANEL, k < kw; zero on and above the diagonal
     // and below the block.  Threads run along the index contiguous in memory.
-    for (int base = t; base < PANEL * kw; base += LEAF_THREADS * LOAD_BATCH) {
+    for (int base = t; base < PANEL * kw; base += NT * LOAD_BATCH) {
       double v[LOAD_BATCH];
 #pragma unroll
       for (int u = 0; u < LOAD_BATCH; ++u) {
-        const int idx = base + u * LEAF_THREADS;
+        const int idx = base + u * NT;
         int i, k;
         if (!g.tA) { i = idx % PANEL; k = idx / PANEL; }
         else { k = idx % kw; i = idx / kw; }
@@ -398,7 +416,7 @@ __device__ __forceinline__ void solve_cols_f64(const LeafArgs& g, int64_t c0, in
       }
 #pragma unroll
       for (int u = 0; u < LOAD_BATCH; ++u) {
-        const int idx = base + u * LEAF_THREADS;
+        const int idx = base + u * NT;
         int i, k;
         if (!g.tA) { i = idx % PANEL; k = idx / PANEL; }
         else { k = idx % kw; i = idx / kw; }
@@ -408,15 +426,14 @@ __device__ __forceinline__ void solve_cols_f64(const LeafArgs& g, int64_t c0, in
     __syncthreads();
     double y[PANEL];
 #pragma unroll
-    for (int i = 0; i < PANEL; ++i) y[i] = i < pw ? X[(p0 + i) * CW + t] : 0.0;
-    // Two k per step with one 16-byte broadcast load of A per row (p0 is a
-    // multiple of 32): half a shared-memory load per FMA, and the unrolled
-    // steps let the loads of the next step overlap the FMAs of this one
-    // (with one warp per SM sub-partition nothing else hides their latency).
-    // The two FMAs into each y[i] of a step are PANEL instructions apart (a
-    // DFMA result is not ready for the next instruction of the same warp).
-    for (int k = 0; k < p0; k += 2) {
-      const double xk0 = X[k * CW + t], xk1 = X[(k + 1) * CW + t];
+    for (int i = 0; i < PANEL; ++i) y[i] = h == 0 && i < pw ? X[(p0 + i) * CW + c] : 0.0;
+    // Already-solved rows: half h takes k in [h p0 / HALVES, (h+1) p0 / HALVES)
+    // (p0 is a multiple of 32, so both ranges have even bounds).  Two k per
+    // step with one 16-byte broadcast load of A per row; the two FMAs into
+    // each y[i] of a step are PANEL instructions apart.
+    const int ka = h * (p0 / HALVES), kb = (h + 1) * (p0 / HALVES);
+    for (int k = ka; k < kb; k += 2) {
+      const double xk0 = X[k * CW + c], xk1 = X[(k + 1) * CW + c];
       double2 a[PANEL];
 #pragma unroll
       for (int i = 0; i < PANEL; ++i) a[i] = *reinterpret_cast<const double2*>(&L[i * COLS_MAX_N + k]);
@@ -425,40 +442,59 @@ __device__ __forceinline__ void solve_cols_f64(const LeafArgs& g, int64_t c0, in
 #pragma unroll
       for (int i = 0; i < PANEL; ++i) y[i] = fma(-a[i].y, xk1, y[i]);
     }
-    if (pw == PANEL) {
-      // Full panel: the triangle two columns at a time (x_j, then x_{j+1},
-      // then one paired load and two FMAs for each row below).
+    if constexpr (HALVES > 1) {
+      if (h == 1) {
 #pragma unroll
-      for (int jj = 0; jj < PANEL / 2; ++jj) {
-        const int j = 2 * jj;
-        const double xj = y[j] * inv_d[p0 + j];
-        const double xj1 = fma(-L[(j + 1) * COLS_MAX_N + p0 + j], xj, y[j + 1]) * inv_d[p0 + j + 1];
-        y[j] = xj;
-        y[j + 1] = xj1;
-#pragma unroll
-        for (int i = j + 2; i < PANEL; ++i) {
-          const double2 a = *reinterpret_cast<const double2*>(&L[i * COLS_MAX_N + p0 + j]);
-          y[i] = fma(-a.x, xj, y[i]);
-          y[i] = fma(-a.y, xj1, y[i]);
-        }
+        for (int i = 0; i < PANEL; ++i) Y1[i * CW + c] = y[i];
       }
-    } else {
+      __syncthreads();
+      if (h == 0) {
 #pragma unroll
-      for (int j = 0; j < PANEL; ++j) {
-        if (j < pw) {
-          const double xj = y[j] * inv_d[p0 + j];
-          y[j] = xj;
-#pragma unroll
-          for (int i = j + 1; i < PANEL; ++i) y[i] = fma(-L[i * COLS_MAX_N + p0 + j], xj, y[i]);
-        }
+        for (int i = 0; i < PANEL; ++i) y[i] += Y1[i * CW + c];
       }
     }
+    if (h == 0) {
+      if (pw == PANEL) {
+        // Full panel: the triangle two columns at a time (x_j, then x_{j+1},
+        // then one paired load and two FMAs for each row below).
 #pragma unroll
-    for (int i = 0; i < PANEL; ++i)
-      if (i < pw) X[(p0 + i) * CW + t] = y[i];
+        for (int jj = 0; jj < PANEL / 2; ++jj) {
+          const int j = 2 * jj;
+          const double xj = y[j] * inv_d[p0 + j];
+          const double xj1 = fma(-L[(j + 1) * COLS_MAX_N + p0 + j], xj, y[j + 1]) * inv_d[p0 + j + 1];
+          y[j] = xj;
+          y[j + 1] = xj1;
+#pragma unroll
+          for (int i = j + 2; i < PANEL; ++i) {
+            const double2 a = *reinterpret_cast<const double2*>(&L[i * COLS_MAX_N + p0 + j]);
+            y[i] = fma(-a.x, xj, y[i]);
+            y[i] = fma(-a.y, xj1, y[i]);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < PANEL; ++j) {
+          if (j < pw) {
+            const double xj = y[j] * inv_d[p0 + j];
+            y[j] = xj;
+#pragma unroll
+            for (int i = j + 1; i < PANEL; ++i) y[i] = fma(-L[i * COLS_MAX_N + p0 + j], xj, y[i]);
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < PANEL; ++i)
+        if (i < pw) X[(p0 + i) * CW + c] = y[i];
+    }
   }
   __syncthreads();
-  store_block<double, double, CW>(g, X, c0, ncols);
+  double* Bo = static_cast<double*>(g.B);
+  for (int idx = t; idx < total; idx += NT) {
+    int i, cc;
+    if (!g.tB) { i = idx % n; cc = idx / n; }
+    else { cc = idx % CW; i = idx / CW; }
+    if (cc < ncols) Bo[b_off<double>(g, i, c0 + cc)] = X[i * CW + cc];
+  }
 }
 
 __host__ __device__ constexpr size_t leaf_solve_smem_elems(int n, int CW) {
