@@ -74,7 +74,7 @@ def parse():
     ap.add_argument("--sweep-plain", action="store_true",
                     help="plain F32/F64 TRSM and TRMM over the 8 side/uplo/trans forms, alpha 0.5 (config 1)")
     ap.add_argument("--sizes", default="4096,8192,16384")
-    ap.add_argument("--kernel-case", choices=["exact", "fast", "leaf", "dfma"], default=None,
+    ap.add_argument("--kernel-case", choices=["exact", "fast", "leaf", "dfma", "feed"], default=None,
                     help="run single launches of one kernel on a moderate case (for ncu captures)")
     ap.add_argument("--case-size", type=int, default=4096)
     ap.add_argument("--case-reps", type=int, default=2)
@@ -511,14 +511,21 @@ def run_config3(args):
         X16.copy_(B16)
         pkg.unified_rectrxm_("L", "L", "N", 1.0, "S", A16, X16, native=True)
 
+    from nextla_gb300 import _lib
+
     ms = timed(f16)
+    _lib.trace_enable(True)
+    f16()
+    torch.cuda.synchronize(dev)
+    _lib.trace_enable(False)
+    trace = {k: {"launches": v[0], "ms": v[1]} for k, v in _lib.trace_summary().items()}
     A64 = A16.double().T.contiguous().T
     X64 = B16.double().T.contiguous().T
     pkg.unified_rectrxm_("L", "L", "N", 1.0, "S", A64, X64, native=True)
     torch.cuda.synchronize(dev)
     rel = float(torch.linalg.norm(X16.double() - X64) / torch.linalg.norm(X64))
     print(json.dumps({"case": "trsm_LLN_f16_n8192_m4096", "ms": ms, "tflops": float(n) * n * m / ms / 1e9,
-                      "rel_err_vs_fp64": rel, "unit_roundoff_f16": 2.0 ** -11}), flush=True)
+                      "rel_err_vs_fp64": rel, "unit_roundoff_f16": 2.0 ** -11, "trace": trace}), flush=True)
     return 0
 
 
@@ -530,7 +537,8 @@ def run_kernel_case(args):
       fast   the same with 3 BF16 slices (FP32 accumulation);
       leaf   one FP64 diagonal-block solve of order 128 with 8 s right-hand
              sides;
-      dfma   one FP64 update on CUDA cores, s x s x s."""
+      dfma   one FP64 update on CUDA cores, s x s x s;
+      feed   the tensor-core feed probes (nla_measure_tensor_feed)."""
     import torch
 
     import __graft_entry__ as graft
@@ -544,6 +552,12 @@ def run_kernel_case(args):
     def cm(r, c):
         return torch.randn(c, r, generator=g, device=dev, dtype=torch.float64).T
 
+    if args.kernel_case == "feed":
+        from nextla_gb300 import _lib
+
+        print(json.dumps({"kernel_case": "feed", "sms": torch.cuda.get_device_properties(dev).multi_processor_count,
+                          **_lib.measure_tensor_feed(torch.cuda.current_stream(dev).cuda_stream)}), flush=True)
+        return 0
     times = []
     for _ in range(args.case_reps):
         if args.kernel_case in ("exact", "fast"):

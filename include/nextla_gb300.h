@@ -256,6 +256,20 @@ NLA_API int nla_batch_solve_mixed(nla_batch_plan plan, double alpha, const void*
 NLA_API int nla_measure_pipes(double* dfma_tflops, double* dmma_tflops, double* ffma_tflops, void* stream);
 
 /*
+ * What feeds the tensor cores on the current GPU, one CTA per SM
+ * (no counterpart in the reference):
+ *   mma_tflops     128 x 128 x 16 BF16 tcgen05 MMAs from operands resident in
+ *                  shared memory;
+ *   tma_gbs_1/2    TMA tile loads into shared memory per SM (GB/s), issued by
+ *                  one or two producer warps;
+ *   pipe_tflops_1/2  TMA loads released by four MMAs per stage (the exact
+ *                  kernels' main loop without their epilogue), one or two
+ *                  producer warps.
+ */
+NLA_API int nla_measure_tensor_feed(double* mma_tflops, double* tma_gbs_1, double* tma_gbs_2, double* pipe_tflops_1,
+                                    double* pipe_tflops_2, void* stream);
+
+/*
  * Kernel tracing (no counterpart in the reference, which has no tracing).
  * nla_trace_enable(1) clears earlier records and starts recording; every
  * library kernel launched afterwards is bracketed by CUDA events on its

@@ -81,6 +81,7 @@ SIGNATURES.update({
 })
 
 SIGNATURES["nla_measure_pipes"] = ([ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d), _p], _i32)
+SIGNATURES["nla_measure_tensor_feed"] = ([ctypes.POINTER(_d)] * 5 + [_p], _i32)
 
 
 def measure_pipes(stream=None) -> dict:
@@ -88,6 +89,16 @@ def measure_pipes(stream=None) -> dict:
     a, b, c = _d(), _d(), _d()
     check(load().nla_measure_pipes(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), stream))
     return {"dfma": a.value, "dmma": b.value, "ffma": c.value}
+
+
+def measure_tensor_feed(stream=None) -> dict:
+    """nla_measure_tensor_feed: MMA-only TFLOP/s, TMA GB/s per SM with one and
+    two producer warps, and TMA-fed MMA TFLOP/s with one and two producers."""
+    v = [_d() for _ in range(5)]
+    check(load().nla_measure_tensor_feed(*[ctypes.byref(x) for x in v], stream))
+    keys = ["mma_tflops", "tma_gbs_per_sm_1_producer", "tma_gbs_per_sm_2_producers", "pipe_tflops_1_producer",
+            "pipe_tflops_2_producers"]
+    return {k: x.value for k, x in zip(keys, v)}
 
 
 KERNEL_CLASSES = ["leaf_solve", "leaf_mult", "gemm_simt", "gemm_umma", "split", "scale", "residual", "batched"]

@@ -20,6 +20,8 @@
 // rounded once when stored.
 #pragma once
 
+#include <type_traits>
+
 #include "nla_common.cuh"
 
 namespace nla {
@@ -261,11 +263,17 @@ __device__ __forceinline__ void trailing_update_wide_n(const Tc* __restrict__ sl
   }
 }
 
-// Row slots with RG * i >= rows hold no row of the chunk and are skipped; the
-// slot count is a compile-time constant of the body.
+// Float64: row slots with RG * i >= rows hold no row of the chunk and are
+// skipped (the slot count is a compile-time constant of the body), which pays
+// on the 2-FMA-per-clock DFMA pipe.  Float32 keeps the single full-height
+// body, which measured faster there.
 template <typename Tc, int CW, int RG>
 __device__ __forceinline__ void trailing_update_wide(const Tc* __restrict__ slab, const Tc* __restrict__ Xp,
                                                      Tc* __restrict__ Xo, int rows, int pw) {
+  if constexpr (!std::is_same<Tc, double>::value) {
+    trailing_update_wide_n<Tc, CW, RG, 4>(slab, Xp, Xo, rows, pw);
+    return;
+  }
   switch ((rows + RG - 1) / RG) {
     case 1: trailing_update_wide_n<Tc, CW, RG, 1>(slab, Xp, Xo, rows, pw); break;
     case 2: trailing_update_wide_n<Tc, CW, RG, 2>(slab, Xp, Xo, rows, pw); break;
@@ -301,10 +309,10 @@ __device__ __forceinline__ void solve_block_wide(const LeafArgs& g, int64_t c0, 
     const int pw = min(PANEL, n - p0);
     stage_slab<PANEL, T>(g, diag, p0, pw, p0, pw, [](int i, int j) { return j < i; });
     __syncthreads();
-    // The panel's serial chains run on CW threads; the warps that take them
-    // rotate with the panel and the CTA so that co-resident CTAs spread this
-    // FP64 work over all four SM sub-partitions.
-    const int rot = 32 * (int)((p0 / PANEL + blockIdx.x) % (LEAF_THREADS / 32));
+    // The panel's serial chains run on CW threads.  In Float64 the warps
+    // that take them rotate with the panel and the CTA so that co-resident
+    // CTAs spread this FP64 work over all four SM sub-partitions.
+    const int rot = std::is_same<Tc, double>::value ? 32 * (int)((p0 / PANEL + blockIdx.x) % (LEAF_THREADS / 32)) : 0;
     const int tt = (t - rot + LEAF_THREADS) % LEAF_THREADS;
     if (tt < CW) {
       Tc x[PANEL];

@@ -43,7 +43,7 @@ constexpr int BM = 128;
 constexpr int BN = 128;
 constexpr int BK = 64;                     // 64 16-bit elements = one 128-byte swizzle row
 constexpr int TILE_BYTES = BM * BK * 2;    // 16 KiB per slice tile (BN == BM)
-constexpr int GEMM_THREADS = 192;
+constexpr int GEMM_THREADS = 224;  // A producer, MMA, 4 epilogue warps, B producer
 constexpr int MAX_PAIRS = 16;
 constexpr int MAX_ACC = 4;
 constexpr int SENTINEL_EXP = -2139062144;  // 0x80808080: "no element seen"
@@ -71,6 +71,7 @@ struct GemmParams {
   const int* ea;
   const int* eb;
   int exp_bias;
+  int producers;  // TMA-issuing warps: 2 (A and B apart) or 1 (warp 0 loads both)
 };
 
 __device__ __forceinline__ double scaled_double(float v, int e) {
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   if (threadIdx.x == 0) {
     s_abort = 0;
     for (int s = 0; s < p.stages; ++s) {
-      umma::mbar_init(umma::smem_u32(&full[s]), 1);
+      umma::mbar_init(umma::smem_u32(&full[s]), p.producers);  // the A and the B producer
       umma::mbar_init(umma::smem_u32(&empty[s]), 1);
     }
     umma::mbar_init(umma::smem_u32(accf), 1);
@@ -129,19 +130,27 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   umma::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0) {
-    if (lane == 0) {
+  if (warp == 0 || warp == GEMM_THREADS / 32 - 1) {
+    // Producers: warp 0 loads the A slices and the last warp the B slices
+    // (p.producers = 2), or warp 0 loads both (1).  One issuing thread is
+    // limited to about 110 GB/s of TMA tile loads per SM, two reach about
+    // 175 GB/s.  Each producer arrives on full[s] for its own bytes.
+    const bool is_a = warp == 0;
+    const bool both = p.producers == 1;
+    if (lane == 0 && (is_a || !both)) {
       for (int kb = 0; kb < p.num_kb; ++kb) {
         const int s = kb % p.stages;
         const uint32_t round = (uint32_t)(kb / p.stages);
         if (!umma::mbar_wait(umma::smem_u32(&empty[s]), (round & 1u) ^ 1u, &s_abort, &g_device_error, 1)) break;
         const uint32_t fb = umma::smem_u32(&full[s]);
-        umma::mbar_arrive_expect_tx(fb, (uint32_t)p.stage_bytes);
         uint8_t* st = smem + (size_t)s * p.stage_bytes;
-        for (int sl = 0; sl < p.sa; ++sl)
-          umma::tma_load_2d(umma::smem_u32(st + sl * TILE_BYTES), &tmA, fb, kb * BK, sl * p.a_rows + m0);
-        for (int sl = 0; sl < p.sb; ++sl)
-          umma::tma_load_2d(umma::smem_u32(st + (p.sa + sl) * TILE_BYTES), &tmB, fb, kb * BK, sl * p.b_rows + n0);
+        umma::mbar_arrive_expect_tx(fb, (uint32_t)(((both ? p.sa + p.sb : is_a ? p.sa : p.sb)) * TILE_BYTES));
+        if (is_a)
+          for (int sl = 0; sl < p.sa; ++sl)
+            umma::tma_load_2d(umma::smem_u32(st + sl * TILE_BYTES), &tmA, fb, kb * BK, sl * p.a_rows + m0);
+        if (!is_a || both)
+          for (int sl = 0; sl < p.sb; ++sl)
+            umma::tma_load_2d(umma::smem_u32(st + (p.sa + sl) * TILE_BYTES), &tmB, fb, kb * BK, sl * p.b_rows + n0);
       }
     }
   } else if (warp == 1) {
@@ -253,7 +262,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 // outside its triangle) costs only its triangle.
 // ---------------------------------------------------------------------------
 
-constexpr int EX_THREADS = 320;  // producer, MMA, 8 epilogue warps
+constexpr int EX_THREADS = 352;  // A producer, MMA, B producer, 8 epilogue warps
 constexpr int EX_CHUNK = 16;     // k-blocks per exact chunk (1024 values)
 constexpr int EX_SLICES = 7;
 constexpr int EX_MAX_PAIRS = 28;
@@ -305,6 +314,72 @@ __device__ __forceinline__ void two_sum_dev(double a, double b, double& s, doubl
   s = a + b;
   const double bp = s - a;
   e = (a - (s - bp)) + (b - bp);
+}
+
+// Fixed point of an output row of the exact kernels: LSB 2^-Lb in units of
+// 2^(ea+eb).  Every partial sum is bounded by nrm_a[i] * (1/2 + 2^-8), so Lb
+// keeps it below 2^61 while giving short or small rows the finest resolution.
+__device__ __forceinline__ int exact_row_lb(const ExactParams& p, int i) {
+  int Lb = 60;
+  if (i < p.M) {
+    const float bound = p.nrm_a[i] * (0.5f + 0.00390625f) * 1.001f;
+    if (bound > 0.0f) Lb = 61 - (int)ceilf(log2f(bound));
+    Lb = min(max(Lb, 0), 77);
+  }
+  return Lb;
+}
+
+// Adds one exact FP32 chunk sum (64 TMEM columns of this thread's lane at ta)
+// into the int64 fixed point, shifted by sh (rounded half up when sh < 0).
+__device__ __forceinline__ void exact_drain(long long (&acc)[64], uint32_t ta, int sh) {
+#pragma unroll
+  for (int j0 = 0; j0 < 64; j0 += 16) {
+    uint32_t r[16];
+    umma::tmem_ld16(ta + (uint32_t)j0, r);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const long long v = (long long)__float2int_rn(__uint_as_float(r[j]));
+      acc[j0 + j] += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
+    }
+  }
+}
+
+// C update of the exact kernels for output row i and the 64 columns from c0:
+// C += alpha * P, or the residual form C := C - P - d_i x (P exact in acc,
+// formed with error-free transformations and rounded once).
+__device__ __forceinline__ void exact_store(const ExactParams& p, const long long (&acc)[64], int i, int c0, int Lb) {
+  if (i >= p.M) return;
+  int ei = p.ea[i];
+  const bool row_nan = ei == NONFINITE_EXP;
+  ei = max(ei, -4000);
+#pragma unroll
+  for (int j = 0; j < 64; ++j) {
+    const int col = c0 + j;
+    if (col >= p.N) continue;
+    double* cp = static_cast<double*>(p.C) +
+                 (p.trans_out ? (int64_t)col + (int64_t)i * p.ldc : (int64_t)i + (int64_t)col * p.ldc);
+    const int ej = p.eb[col];
+    if (row_nan || ej == NONFINITE_EXP) {
+      *cp = __longlong_as_double(0x7ff8000000000000ull);
+    } else if (p.res_x == nullptr) {
+      const double d = scale_pow2(__ll2double_rn(acc[j]), ei + max(ej, -4000) - Lb);
+      *cp = fma(p.alpha, d, *cp);
+    } else {
+      const int e = ei + max(ej, -4000) - Lb;
+      const double hi_u = __ll2double_rn(acc[j]);
+      const double lo_u = __ll2double_rn(acc[j] - (long long)hi_u);
+      const double s_hi = scale_pow2(hi_u, e), s_lo = scale_pow2(lo_u, e);
+      const double dg = p.res_d[(int64_t)i * p.res_dstride];
+      const double xv = p.res_x[p.trans_out ? (int64_t)col + (int64_t)i * p.res_ldx
+                                            : (int64_t)i + (int64_t)col * p.res_ldx];
+      const double pr = dg * xv;
+      const double pe = fma(dg, xv, -pr);
+      double t1, e1, t2, e2;
+      two_sum_dev(*cp, -s_hi, t1, e1);
+      two_sum_dev(t1, -pr, t2, e2);
+      *cp = t2 + (((e1 + e2) - pe) - s_lo);
+    }
+  }
 }
 
 // CM x CN: the cluster shape in output tiles.  With a cluster, the CTAs of
@@ -368,7 +443,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   if (threadIdx.x == 0) {
     s_abort = 0;
     for (int s = 0; s < EX_STAGES; ++s) {
-      umma::mbar_init(umma::smem_u32(&full[s]), 1);
+      umma::mbar_init(umma::smem_u32(&full[s]), 2);  // the A and the B producer
       umma::mbar_init(umma::smem_u32(&empty[s]), CM + CN - 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -388,7 +463,12 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   const uint32_t tmem = *tmem_slot;
   bool ok = true;
 
-  if (warp == 0) {
+  if (warp == 0 || warp == 2) {
+    // Two producers, one per operand: a thread issues TMA tile loads at a
+    // limited rate (about 110 GB/s per SM measured with 16 KiB boxes), and two
+    // issuing warps reach about 175 GB/s.  Each arrives on full[s] for its
+    // own 16 KiB.
+    const bool is_a = warp == 0;
     if (lane == 0) {
       int it = 0;
       for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
@@ -403,21 +483,24 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
               break;
             }
             const uint32_t fb = umma::smem_u32(&full[s]);
-            umma::mbar_arrive_expect_tx(fb, (uint32_t)EX_STAGE_BYTES);
+            umma::mbar_arrive_expect_tx(fb, (uint32_t)TILE_BYTES);
             uint8_t* st = smem + s * EX_STAGE_BYTES;
             // Rows of a tile are 128 bytes: part j of a tile split in parts of
             // R rows starts j * R * 128 bytes in (a multiple of the 1024-byte
             // swizzle atom).
-            if constexpr (CN > 1)
-              umma::tma_load_2d_mc(umma::smem_u32(st + cn * (BM / CN) * 128), &tmA, fb, kb * BK,
-                                   p.pa[pr] * p.a_rows + m0 + cn * (BM / CN), row_mask);
-            else
-              umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, p.pa[pr] * p.a_rows + m0);
-            if constexpr (CM > 1)
-              umma::tma_load_2d_mc(umma::smem_u32(st + TILE_BYTES + cm * (BN / CM) * 128), &tmB, fb, kb * BK,
-                                   p.pb[pr] * p.b_rows + n0 + cm * (BN / CM), col_mask);
-            else
-              umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), &tmB, fb, kb * BK, p.pb[pr] * p.b_rows + n0);
+            if (is_a) {
+              if constexpr (CN > 1)
+                umma::tma_load_2d_mc(umma::smem_u32(st + cn * (BM / CN) * 128), &tmA, fb, kb * BK,
+                                     p.pa[pr] * p.a_rows + m0 + cn * (BM / CN), row_mask);
+              else
+                umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, p.pa[pr] * p.a_rows + m0);
+            } else {
+              if constexpr (CM > 1)
+                umma::tma_load_2d_mc(umma::smem_u32(st + TILE_BYTES + cm * (BN / CM) * 128), &tmB, fb, kb * BK,
+                                     p.pb[pr] * p.b_rows + n0 + cm * (BN / CM), col_mask);
+              else
+                umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), &tmB, fb, kb * BK, p.pb[pr] * p.b_rows + n0);
+            }
           }
         }
       }
@@ -472,21 +555,13 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     }
   } else {
     const int q = warp & 3;
-    const int h = (warp - 2) >> 2;  // column half: 0 or 1
+    const int h = (warp - 3) >> 2;  // column half: 0 (warps 3-6) or 1 (warps 7-10)
     const int row = q * 32 + lane;
     const int i = m0 + row;
     long long acc[64];
 #pragma unroll
     for (int j = 0; j < 64; ++j) acc[j] = 0;
-    // Fixed point of this row: LSB 2^-Lb in units of 2^(ea+eb).  Every
-    // partial sum is bounded by nrm_a[i] * (1/2 + 2^-8), so Lb keeps it
-    // below 2^61 while giving short or small rows the finest resolution.
-    int Lb = 60;
-    if (i < p.M) {
-      const float bound = p.nrm_a[i] * (0.5f + 0.00390625f) * 1.001f;
-      if (bound > 0.0f) Lb = 61 - (int)ceilf(log2f(bound));
-      Lb = min(max(Lb, 0), 77);
-    }
+    const int Lb = exact_row_lb(p, i);
     int ch = 0;
     for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
       if (max(kb0, cc * EX_CHUNK) >= min(kb1, (cc + 1) * EX_CHUNK)) continue;
@@ -498,57 +573,13 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
                         umma::mbar_wait(umma::smem_u32(&cfull[b]), use & 1u, &s_abort, &g_device_error, 15));
         if (!ok) break;
         umma::fence_after_sync();
-        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + h * 64);
-#pragma unroll
-        for (int j0 = 0; j0 < 64; j0 += 16) {
-          uint32_t r[16];
-          umma::tmem_ld16(ta + (uint32_t)j0, r);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const long long v = (long long)__float2int_rn(__uint_as_float(r[j]));
-            acc[j0 + j] += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
-          }
-        }
+        exact_drain(acc, tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + h * 64), sh);
         umma::fence_before_sync();
         __syncwarp();
         if (lane == 0) umma::mbar_arrive(umma::smem_u32(&cempty[b]));
       }
     }
-    if (ok && i < p.M) {
-      int ei = p.ea[i];
-      const bool row_nan = ei == NONFINITE_EXP;
-      ei = max(ei, -4000);
-#pragma unroll
-      for (int j = 0; j < 64; ++j) {
-        const int col = n0 + h * 64 + j;
-        if (col >= p.N) continue;
-        double* cp = static_cast<double*>(p.C) +
-                     (p.trans_out ? (int64_t)col + (int64_t)i * p.ldc : (int64_t)i + (int64_t)col * p.ldc);
-        const int ej = p.eb[col];
-        if (row_nan || ej == NONFINITE_EXP) {
-          *cp = __longlong_as_double(0x7ff8000000000000ull);
-        } else if (p.res_x == nullptr) {
-          const double d = scale_pow2(__ll2double_rn(acc[j]), ei + max(ej, -4000) - Lb);
-          *cp = fma(p.alpha, d, *cp);
-        } else {
-          // Residual epilogue: C := C - P - d_i x with P exact in acc, formed
-          // with error-free transformations and rounded once.
-          const int e = ei + max(ej, -4000) - Lb;
-          const double hi_u = __ll2double_rn(acc[j]);
-          const double lo_u = __ll2double_rn(acc[j] - (long long)hi_u);
-          const double s_hi = scale_pow2(hi_u, e), s_lo = scale_pow2(lo_u, e);
-          const double dg = p.res_d[(int64_t)i * p.res_dstride];
-          const double xv = p.res_x[p.trans_out ? (int64_t)col + (int64_t)i * p.res_ldx
-                                                : (int64_t)i + (int64_t)col * p.res_ldx];
-          const double pr = dg * xv;
-          const double pe = fma(dg, xv, -pr);
-          double t1, e1, t2, e2;
-          two_sum_dev(*cp, -s_hi, t1, e1);
-          two_sum_dev(t1, -pr, t2, e2);
-          *cp = t2 + (((e1 + e2) - pe) - s_lo);
-        }
-      }
-    }
+    if (ok) exact_store(p, acc, i, n0 + h * 64, Lb);
   }
 
   umma::fence_before_sync();
@@ -804,6 +835,16 @@ int64_t pad_to(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 // static shared memory, so it is set to what the launches actually use.
 constexpr int GEMM_DYN_SMEM = 200 * 1024;
 
+// TMA-issuing warps of the fast tensor-core kernel (NLA_GEMM_PRODUCERS = 1
+// or 2, default 2; read once).
+int gemm_producers() {
+  static const int n = [] {
+    const char* v = getenv("NLA_GEMM_PRODUCERS");
+    return v && v[0] == '1' && v[1] == 0 ? 1 : 2;
+  }();
+  return n;
+}
+
 template <int EPI>
 int ensure_gemm_smem() {
   static std::once_flag once;
@@ -1011,6 +1052,7 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
   p.b_rows = (int)Np;
   p.sa = S;
   p.sb = S;
+  p.producers = gemm_producers();
   p.stage_bytes = 2 * S * TILE_BYTES;
   p.stages = (GEMM_DYN_SMEM - 1024 - 256) / p.stage_bytes;
   if (p.stages > 6) p.stages = 6;
