@@ -55,7 +55,7 @@ struct GemmParams {
   int M, N;
   int num_kb;
   int tiles_m, tiles_n;
-  int a_rows, b_rows;  // padded rows of one slice (row offset between stacked slices)
+  int a_rows, b_rows;  // padded rows of the operands (multiples of 128)
   int sa, sb;          // slices of A and B loaded per stage
   int stages;
   int stage_bytes;
@@ -147,10 +147,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         umma::mbar_arrive_expect_tx(fb, (uint32_t)(((both ? p.sa + p.sb : is_a ? p.sa : p.sb)) * TILE_BYTES));
         if (is_a)
           for (int sl = 0; sl < p.sa; ++sl)
-            umma::tma_load_2d(umma::smem_u32(st + sl * TILE_BYTES), &tmA, fb, kb * BK, sl * p.a_rows + m0);
+            umma::tma_load_2d(umma::smem_u32(st + sl * TILE_BYTES), &tmA, fb, kb * BK, m0 * p.sa + sl * BM);
         if (!is_a || both)
           for (int sl = 0; sl < p.sb; ++sl)
-            umma::tma_load_2d(umma::smem_u32(st + (p.sa + sl) * TILE_BYTES), &tmB, fb, kb * BK, sl * p.b_rows + n0);
+            umma::tma_load_2d(umma::smem_u32(st + (p.sa + sl) * TILE_BYTES), &tmB, fb, kb * BK, n0 * p.sb + sl * BN);
       }
     }
   } else if (warp == 1) {
@@ -491,15 +491,15 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
             if (is_a) {
               if constexpr (CN > 1)
                 umma::tma_load_2d_mc(umma::smem_u32(st + cn * (BM / CN) * 128), &tmA, fb, kb * BK,
-                                     p.pa[pr] * p.a_rows + m0 + cn * (BM / CN), row_mask);
+                                     m0 * EX_SLICES + p.pa[pr] * BM + cn * (BM / CN), row_mask);
               else
-                umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, p.pa[pr] * p.a_rows + m0);
+                umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, m0 * EX_SLICES + p.pa[pr] * BM);
             } else {
               if constexpr (CM > 1)
                 umma::tma_load_2d_mc(umma::smem_u32(st + TILE_BYTES + cm * (BN / CM) * 128), &tmB, fb, kb * BK,
-                                     p.pb[pr] * p.b_rows + n0 + cm * (BN / CM), col_mask);
+                                     n0 * EX_SLICES + p.pb[pr] * BN + cm * (BN / CM), col_mask);
               else
-                umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), &tmB, fb, kb * BK, p.pb[pr] * p.b_rows + n0);
+                umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), &tmB, fb, kb * BK, n0 * EX_SLICES + p.pb[pr] * BN);
             }
           }
         }
@@ -589,6 +589,209 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     __syncwarp();
     umma::fence_after_sync();
     umma::tmem_dealloc(tmem, 256);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Exact kernel with coupled pairs.  The 28 pairs (p, q) are walked as 16
+// groups: for each B slice q, the A slices p = 0, 2, 4, 6 each with its
+// successor p + 1 while p + 1 <= 6 - q.  A group's stage holds A_p, A_p+1
+// and B_q (48 KiB, three boxes) and feeds two accumulators, so a pair costs
+// 24 KiB of tile loads instead of 32: the TMA feed, not the tensor core,
+// bounds these kernels (about 100-120 GB/s per SM with 16 KiB boxes).
+// Each group's two accumulators (weights p + q and p + 1 + q) take half of a
+// 256-column TMEM buffer; two buffers fill the 512 columns.
+// Warps: 0 loads A, 1 issues the MMAs, 2 loads B, 3-10 drain.
+// ---------------------------------------------------------------------------
+constexpr int CP_STAGES = 4;
+constexpr int CP_STAGE_BYTES = 3 * TILE_BYTES;
+constexpr int CP_DYN_SMEM = CP_STAGES * CP_STAGE_BYTES + 1024 + 256;
+constexpr int CP_GROUPS = 16;
+static_assert(CP_DYN_SMEM + 16 <= 232448, "coupled exact kernel shared memory above the per-block limit");
+
+// Group g -> (p, q, coupled): q-major, p = 0, 2, 4, ... (a coupled group
+// also takes p + 1, while p + 1 <= 6 - q).  Packed as p | q << 4 | coupled << 8.
+__constant__ uint16_t c_cp_groups[CP_GROUPS] = {
+    0x100, 0x102, 0x104, 0x006,   // q = 0: (0,1) (2,3) (4,5) (6)
+    0x110, 0x112, 0x114,          // q = 1: (0,1) (2,3) (4,5)
+    0x120, 0x122, 0x024,          // q = 2: (0,1) (2,3) (4)
+    0x130, 0x132,                 // q = 3: (0,1) (2,3)
+    0x140, 0x042,                 // q = 4: (0,1) (2)
+    0x150,                        // q = 5: (0,1)
+    0x060};                       // q = 6: (0)
+
+__device__ __forceinline__ void cp_group(int g, int& pa, int& qb, bool& two) {
+  const int v = c_cp_groups[g];
+  pa = v & 15;
+  qb = (v >> 4) & 15;
+  two = (v >> 8) & 1;
+}
+
+__global__ void __launch_bounds__(EX_THREADS, 1)
+    umma_exact_coupled_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmA2,
+                              const __grid_constant__ CUtensorMap tmB, const ExactParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + CP_STAGES * CP_STAGE_BYTES);
+  uint64_t* empty = full + CP_STAGES;
+  uint64_t* cfull = empty + CP_STAGES;
+  uint64_t* cempty = cfull + 2;
+  uint64_t* drain = cempty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  __shared__ volatile int s_abort;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int group = 8;
+  const int per_group = group * p.tiles_n;
+  const int gr = blockIdx.x / per_group;
+  const int first_m = gr * group;
+  const int gsize = min(p.tiles_m - first_m, group);
+  const int local = blockIdx.x % per_group;
+  const int m0 = (first_m + local % gsize) * BM, n0 = (local / gsize) * BN;
+  int alo, ahi, blo, bhi;
+  tri_k_range(p.tri_a, m0, BM, p.K, alo, ahi);
+  tri_k_range(p.tri_b, n0, BN, p.K, blo, bhi);
+  const int klo = max(alo, blo), khi = min(ahi, bhi);
+  const int kb0 = klo / BK;
+  const int kb1 = khi >= klo ? khi / BK + 1 : kb0;  // empty range when the triangles miss each other
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int s = 0; s < CP_STAGES; ++s) {
+      umma::mbar_init(umma::smem_u32(&full[s]), 2);  // the A and the B producer
+      umma::mbar_init(umma::smem_u32(&empty[s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      umma::mbar_init(umma::smem_u32(&cfull[b]), 1);
+      umma::mbar_init(umma::smem_u32(&cempty[b]), 8);
+    }
+    umma::mbar_init(umma::smem_u32(drain), 1);
+    umma::fence_barrier_init();
+  }
+  if (warp == 1) umma::tmem_alloc(umma::smem_u32(tmem_slot), 512);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  bool ok = true;
+
+  if (warp == 0 || warp == 2) {
+    const bool is_a = warp == 0;
+    if (lane == 0) {
+      int it = 0;
+      for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
+        const int c0 = max(kb0, cc * EX_CHUNK), c1 = min(kb1, (cc + 1) * EX_CHUNK);
+        if (c0 >= c1) continue;
+        for (int g = 0; g < CP_GROUPS && ok; ++g) {
+          int pa, qb;
+          bool two;
+          cp_group(g, pa, qb, two);
+          for (int kb = c0; kb < c1; ++kb, ++it) {
+            const int s = it % CP_STAGES;
+            const uint32_t round = (uint32_t)(it / CP_STAGES);
+            if (!umma::mbar_wait(umma::smem_u32(&empty[s]), (round & 1u) ^ 1u, &s_abort, &g_device_error, 31)) {
+              ok = false;
+              break;
+            }
+            const uint32_t fb = umma::smem_u32(&full[s]);
+            uint8_t* st = smem + s * CP_STAGE_BYTES;
+            // Staged rows: slice sl of the tile at row r0 starts at r0 * 7 + sl * 128,
+            // so A_p and A_p+1 are one 256-row box.
+            if (is_a) {
+              umma::mbar_arrive_expect_tx(fb, (uint32_t)((two ? 2 : 1) * TILE_BYTES));
+              umma::tma_load_2d(umma::smem_u32(st), two ? &tmA2 : &tmA, fb, kb * BK, m0 * EX_SLICES + pa * BM);
+            } else {
+              umma::mbar_arrive_expect_tx(fb, (uint32_t)TILE_BYTES);
+              umma::tma_load_2d(umma::smem_u32(st + 2 * TILE_BYTES), &tmB, fb, kb * BK, n0 * EX_SLICES + qb * BN);
+            }
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = umma::idesc_f16(BM, BN, true);
+      int it = 0, ch = 0;
+      for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
+        const int c0 = max(kb0, cc * EX_CHUNK), c1 = min(kb1, (cc + 1) * EX_CHUNK);
+        if (c0 >= c1) continue;
+        for (int g = 0; g < CP_GROUPS && ok; ++g, ++ch) {
+          int pa, qb;
+          bool two;
+          cp_group(g, pa, qb, two);
+          const int b = ch & 1;
+          if (!umma::mbar_wait(umma::smem_u32(&cempty[b]), ((uint32_t)(ch >> 1) & 1u) ^ 1u, &s_abort,
+                               &g_device_error, 32)) {
+            ok = false;
+            break;
+          }
+          umma::fence_after_sync();
+          const uint32_t d0 = tmem + (uint32_t)(b * 2 * BN), d1 = d0 + (uint32_t)BN;
+          for (int kb = c0; kb < c1; ++kb, ++it) {
+            const int s = it % CP_STAGES;
+            if (!umma::mbar_wait(umma::smem_u32(&full[s]), (uint32_t)(it / CP_STAGES) & 1u, &s_abort,
+                                 &g_device_error, 33)) {
+              ok = false;
+              break;
+            }
+            umma::fence_after_sync();
+            const uint32_t a0 = umma::smem_u32(smem + s * CP_STAGE_BYTES);
+            const uint32_t a1 = a0 + TILE_BYTES, b0 = a0 + 2 * TILE_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk)
+              umma::mma_f16(d0, umma::desc_kmajor_sw128(a0 + kk * 32), umma::desc_kmajor_sw128(b0 + kk * 32), idesc,
+                            (kb > c0 || kk > 0) ? 1u : 0u);
+            if (two) {
+#pragma unroll
+              for (int kk = 0; kk < BK / 16; ++kk)
+                umma::mma_f16(d1, umma::desc_kmajor_sw128(a1 + kk * 32), umma::desc_kmajor_sw128(b0 + kk * 32),
+                              idesc, (kb > c0 || kk > 0) ? 1u : 0u);
+            }
+            umma::mma_commit(umma::smem_u32(&empty[s]));
+          }
+          if (ok) umma::mma_commit(umma::smem_u32(&cfull[b]));
+        }
+      }
+      umma::mma_commit(umma::smem_u32(drain));
+      umma::mbar_wait(umma::smem_u32(drain), 0, &s_abort, &g_device_error, 34, false);
+    }
+  } else {
+    const int q = warp & 3;
+    const int h = (warp - 3) >> 2;  // column half: 0 (warps 3-6) or 1 (warps 7-10)
+    const int i = m0 + q * 32 + lane;
+    long long acc[64];
+#pragma unroll
+    for (int j = 0; j < 64; ++j) acc[j] = 0;
+    const int Lb = exact_row_lb(p, i);
+    int ch = 0;
+    for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
+      if (max(kb0, cc * EX_CHUNK) >= min(kb1, (cc + 1) * EX_CHUNK)) continue;
+      for (int g = 0; g < CP_GROUPS && ok; ++g, ++ch) {
+        int pa, qb;
+        bool two;
+        cp_group(g, pa, qb, two);
+        const int b = ch & 1;
+        ok = __all_sync(0xffffffffu, umma::mbar_wait(umma::smem_u32(&cfull[b]), (uint32_t)(ch >> 1) & 1u, &s_abort,
+                                                     &g_device_error, 35));
+        if (!ok) break;
+        umma::fence_after_sync();
+        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * 2 * BN + h * 64);
+        exact_drain(acc, ta, Lb - 8 * (pa + qb + 2));
+        if (two) exact_drain(acc, ta + (uint32_t)BN, Lb - 8 * (pa + 1 + qb + 2));
+        umma::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) umma::mbar_arrive(umma::smem_u32(&cempty[b]));
+      }
+    }
+    if (ok) exact_store(p, acc, i, n0 + h * 64, Lb);
+  }
+
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    umma::fence_after_sync();
+    umma::tmem_dealloc(tmem, 512);
   }
 }
 
@@ -702,7 +905,9 @@ __device__ __forceinline__ long long fixed_of(double x, int ex) {
 
 // Split a rows x cols view into NS K-major slices of type Sl (rows padded to
 // rows_pad, K padded to cols_pad, zeros in the padding and outside the staged
-// triangle).  The slices are the integers s_p of
+// triangle).  Layout: the slices of one 128-row tile are adjacent, row
+// (t * NS + sl) * 128 + r holding row t * 128 + r of slice sl, so that one
+// TMA box of 256 rows brings slices sl and sl + 1 of a tile.  The slices are the integers s_p of
 //   x = 2^e[row] * sum_p s_p 2^(-beta p),  beta = 8 (BF16) or 11 (FP16),
 // peeled from the top of the 63-bit fixed-point value with round-to-nearest
 // so that |s_p| <= 2^(beta-1).  NS = 0 stages the element itself (a Float16
@@ -739,12 +944,13 @@ __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int
     tile[i][k] = v[j];
   }
   __syncthreads();
-  const int64_t slice_elems = rows_pad * cols_pad;
+  (void)rows_pad;
+  constexpr int NSL = NS == 0 ? 1 : NS;
   // One row per warp and pass (idx >> 5 is warp-uniform), two K values per lane.
   for (int idx = threadIdx.x; idx < 32 * 32; idx += 256) {
     const int i = idx >> 5, k = (idx & 31) * 2;
     const int64_t gi = i0 + i, gk = k0 + k;
-    uint32_t* o = reinterpret_cast<uint32_t*>(out + gi * cols_pad + gk);
+    uint32_t* o = reinterpret_cast<uint32_t*>(out + ((gi >> 7) * NSL * 128 + (gi & 127)) * cols_pad + gk);
     if constexpr (NS == 0) {
       *o = pack2<Sl>((Sl)(float)tile[i][k], (Sl)(float)tile[i][k + 1]);
       continue;
@@ -774,7 +980,7 @@ __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int
         // mantissa's last place.
         const float f0 = __int_as_float(0x4B400000 + d0) - 12582912.0f;
         const float f1 = __int_as_float(0x4B400000 + d1) - 12582912.0f;
-        o[sl * (slice_elems / 2)] = pack_slices<Sl>(f0, f1);
+        o[sl * (128 * cols_pad / 2)] = pack_slices<Sl>(f0, f1);
         // 2^(-beta (sl + 1)) built from its exponent bits (exact).
         mag += (fabsf(f0) + fabsf(f1)) * __int_as_float((127 - BETA * (sl + 1)) << 23);
       }
@@ -875,6 +1081,34 @@ int exact_cluster_shape() {
     return EX_DEFAULT_CLUSTER;
   }();
   return shape;
+}
+
+// Exact-kernel variant: coupled pairs (default) or pair by pair with its
+// cluster options (NLA_EXACT_KERNEL=pairs; read once).
+bool exact_coupled() {
+  static const bool on = [] {
+    const char* v = getenv("NLA_EXACT_KERNEL");
+    return !(v && !strcmp(v, "pairs"));
+  }();
+  return on;
+}
+
+int launch_exact_coupled(const ExactParams& p, const Staged& A, const Staged& B, cudaStream_t s) {
+  CUtensorMap mA, mA2, mB;
+  NLA_TRY(make_map(&mA, A.slices, true, (uint64_t)A.K_pad, (uint64_t)(EX_SLICES * A.rows_pad)));
+  NLA_TRY(make_map(&mA2, A.slices, true, (uint64_t)A.K_pad, (uint64_t)(EX_SLICES * A.rows_pad), 2 * BM));
+  NLA_TRY(make_map(&mB, B.slices, true, (uint64_t)B.K_pad, (uint64_t)(EX_SLICES * B.rows_pad)));
+  static std::once_flag once;
+  static cudaError_t st = cudaSuccess;
+  std::call_once(once, [] {
+    st = cudaFuncSetAttribute(umma_exact_coupled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, CP_DYN_SMEM);
+  });
+  if (st != cudaSuccess) return cuda_status(st, "cudaFuncSetAttribute(umma_exact_coupled_kernel)");
+  const int64_t grid = (int64_t)p.tiles_m * p.tiles_n;
+  if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "too many output tiles");
+  umma_exact_coupled_kernel<<<(unsigned)grid, EX_THREADS, CP_DYN_SMEM, s>>>(mA, mA2, mB, p);
+  NLA_CHECK_LAUNCH("umma_exact_coupled_kernel");
+  return NLA_OK;
 }
 
 template <int CM, int CN>
@@ -1146,6 +1380,7 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
   const double tri_frac = (A.tri != 0 || B.tri != 0) ? 0.5 : 1.0;
   TraceScope trace(NLA_K_GEMM_UMMA, s, 2.0 * (double)M * N * (double)K * p.npairs * tri_frac,
                    (double)EX_SLICES * (A.rows_pad + B.rows_pad) * A.K_pad * 2 + 16.0 * (double)M * N);
+  if (exact_coupled() && exact_cluster_shape() == 11) return launch_exact_coupled(p, A, B, s);
   switch (exact_cluster_shape()) {
     case 21: return launch_exact_shape<2, 1>(p, A, B, s);
     case 12: return launch_exact_shape<1, 2>(p, A, B, s);
