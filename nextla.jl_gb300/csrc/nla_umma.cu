@@ -1083,12 +1083,13 @@ int exact_cluster_shape() {
   return shape;
 }
 
-// Exact-kernel variant: coupled pairs (default) or pair by pair with its
-// cluster options (NLA_EXACT_KERNEL=pairs; read once).
+// Exact-kernel variant (NLA_EXACT_KERNEL, read once): "coupled" (pairs
+// sharing a B tile, the default) or "pairs" (pair by pair, with the cluster
+// options).
 bool exact_coupled() {
   static const bool on = [] {
-    const char* v = getenv("NLA_EXACT_KERNEL");
-    return !(v && !strcmp(v, "pairs"));
+    const char* e = getenv("NLA_EXACT_KERNEL");
+    return !(e && !strcmp(e, "pairs"));
   }();
   return on;
 }
@@ -1380,7 +1381,7 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
   const double tri_frac = (A.tri != 0 || B.tri != 0) ? 0.5 : 1.0;
   TraceScope trace(NLA_K_GEMM_UMMA, s, 2.0 * (double)M * N * (double)K * p.npairs * tri_frac,
                    (double)EX_SLICES * (A.rows_pad + B.rows_pad) * A.K_pad * 2 + 16.0 * (double)M * N);
-  if (exact_coupled() && exact_cluster_shape() == 11) return launch_exact_coupled(p, A, B, s);
+  if (exact_cluster_shape() == 11 && exact_coupled()) return launch_exact_coupled(p, A, B, s);
   switch (exact_cluster_shape()) {
     case 21: return launch_exact_shape<2, 1>(p, A, B, s);
     case 12: return launch_exact_shape<1, 2>(p, A, B, s);
