@@ -83,6 +83,16 @@ NLA_API int nla_trxm_ex(char side, char uplo, char trans, double alpha, char fun
                 const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, void* stream);
 
 /*
+ * nla_trxm with a unit-diagonal option: diag 'U' takes the diagonal of A as
+ * ones and never reads it; 'N' is nla_trxm.  Backs the trsm()/trmm() wrappers
+ * (src/trsm.jl:186-204, src/trmm.jl:430-448), which take a diag argument the
+ * reference accepts but does not apply; here the wrappers run the recursion,
+ * so they also honour transa and any n.
+ */
+NLA_API int nla_trxm_diag(char side, char uplo, char trans, char diag, double alpha, char func, int dtype, int64_t n,
+                          int64_t m, const void* A, int64_t lda, void* B, int64_t ldb, void* stream);
+
+/*
  * One base case of the recursion on a diagonal block.
  * Replaces LeftLowerTRSM!/LeftUpperTRSM!/RightLowerTRSM!/RightUpperTRSM!
  * (src/trsm.jl:128-150, kernels :5-126) for func 'S' and

@@ -206,7 +206,7 @@ int64_t split_point(int64_t n) {
 // Recursion (unified_rec, src/rectrxm.jl:101-198).
 // ---------------------------------------------------------------------------
 int recurse(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
-  if (n <= c.threshold) return launch_leaf(c.func, c.side, c.uplo, c.dtype, n, c.m, A, B, c.s);
+  if (n <= c.threshold) return launch_leaf(c.func, c.side, c.uplo, c.dtype, n, c.m, A, B, c.s, c.unit);
   const int64_t mid = split_point(n), rem = n - mid;
   const int d = c.dtype;
   const Mat A11 = A, A22 = sub(A, mid, mid, d), A21 = sub(A, mid, 0, d), A12 = sub(A, 0, mid, d);
@@ -251,8 +251,8 @@ int64_t default_cutoff(char func, int dtype) {
 }
 
 int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
-              const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m,
-              cudaStream_t s) {
+              const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, cudaStream_t s,
+              bool unit) {
   NLA_TRY(check_flags(side, uplo, trans, func, dtype));
   if (n < 0 || m < 0) return fail(NLA_ERR_ARG, "n and m must be non-negative");
   NLA_TRY(check_matrix("A", A, n, n, lda));
@@ -266,6 +266,7 @@ int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dty
   }
   const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
   RecPlan c{func, side, uplo, dtype, m, 0, s, GEMM_PLAIN, 1, false};
+  c.unit = unit;
   if (func == 'S') {
     c.threshold = cutoff_s > 0 ? cutoff_s : default_cutoff('S', dtype);
     if (c.threshold > 1024) c.threshold = 1024;
@@ -333,6 +334,14 @@ int nla_trxm_ex(char side, char uplo, char trans, double alpha, char func, int d
   clear_error();
   return trxm_impl(side, uplo, trans, alpha, func, dtype, n, m, A, lda, B, ldb, cutoff_s, cutoff_m,
                    (cudaStream_t)stream);
+}
+
+int nla_trxm_diag(char side, char uplo, char trans, char diag, double alpha, char func, int dtype, int64_t n,
+                  int64_t m, const void* A, int64_t lda, void* B, int64_t ldb, void* stream) {
+  clear_error();
+  if (diag != 'N' && diag != 'U') return fail(NLA_ERR_ARG, std::string("diag must be 'N' or 'U', got '") + diag + "'");
+  return trxm_impl(side, uplo, trans, alpha, func, dtype, n, m, A, lda, B, ldb, 0, 0, (cudaStream_t)stream,
+                   diag == 'U');
 }
 
 int nla_diag_block(char func, char side, char uplo, int transA, int dtype, int64_t n, int64_t m, const void* A,

@@ -91,6 +91,7 @@ __global__ void __launch_bounds__(LEAF_THREADS) batched_solve_kernel(BatchArgs a
     g.ldb = d.ldb;
     g.tB = 0;
     g.rev = a.rev;
+    g.unit = 0;
     g.n = (int)d.n;
     g.m = d.m;
     const int ncols = (int)(d.m - w.c0 < w.cw ? d.m - w.c0 : w.cw);
@@ -180,6 +181,7 @@ __device__ __forceinline__ void residual_band(const ResidualArgs& a, const Batch
   g.ldb = d.ldb;
   g.tB = 0;
   g.rev = a.rev;
+  g.unit = 0;
   g.n = (int)d.n;
   g.m = d.m;
   const int ncols = (int)(d.m - w.c0 < CW ? d.m - w.c0 : CW);
@@ -286,8 +288,7 @@ int enqueue(nla_batch_plan p, double alpha, const void* A, void* B, cudaStream_t
 
 }  // namespace
 
-int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
-              const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, cudaStream_t s);
+
 
 }  // namespace nla
 

@@ -113,7 +113,7 @@ int launch_gemm(int dtype, int64_t N, int64_t M, int64_t K, double alpha, const 
 
 // Base case on a diagonal block: func 'S' (solve) or 'M' (multiply).
 int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m, const Mat& A, const Mat& B,
-                cudaStream_t s);
+                cudaStream_t s, bool unit = false);
 
 // B .= alpha .* B on a rows x cols view.
 int launch_scale(int dtype, int64_t rows, int64_t cols, double alpha, const Mat& B, cudaStream_t s);
@@ -172,8 +172,13 @@ struct RecPlan {
   int mode;
   int S;
   bool bf16;
+  bool unit = false;  // unit diagonal (plain path only)
 };
 int recurse(const RecPlan& c, const Mat& A, int64_t n, const Mat& B);
+// The plain recursion behind nla_trxm / nla_trxm_ex / nla_trxm_diag.
+int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
+              const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, cudaStream_t s,
+              bool unit = false);
 int64_t split_point(int64_t n);
 int check_flags(char side, char uplo, char trans, char func, int dtype);
 int check_matrix(const char* name, const void* p, int64_t rows, int64_t cols, int64_t ld);

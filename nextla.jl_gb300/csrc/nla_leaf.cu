@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(LEAF_THREADS) leaf_mult_kernel(LeafArgs g) {
       for (int c = 0; c < CT; ++c) acc[i][c] = Tc(0);
     for (int k0 = 0; k0 < kmax; k0 += PANEL) {
       const int kw = min(PANEL, kmax - k0);
-      stage_slab<LEAF_THREADS, T>(g, slab, r0, rows, k0, kw, [](int i, int j) { return j <= i; });
+      const bool unit = g.unit != 0;
+      stage_slab<LEAF_THREADS, T>(g, slab, r0, rows, k0, kw, [unit](int i, int j) { return unit ? j < i : j <= i; });
       __syncthreads();
       tile_product<Tc, CW>(slab, X + (size_t)k0 * CW, kw, rows, acc);
       __syncthreads();
@@ -84,7 +85,11 @@ __global__ void __launch_bounds__(LEAF_THREADS) leaf_mult_kernel(LeafArgs g) {
       if (r < rows) {
 #pragma unroll
         for (int c = 0; c < CT; ++c)
-          if (tc * CT + c < ncols) Elem<T>::store(Bp + b_off<T>(g, r0 + r, c0 + tc * CT + c), acc[i][c]);
+          if (tc * CT + c < ncols) {
+            // A unit diagonal contributes the row's own value of X.
+            const Tc v = g.unit ? acc[i][c] + X[(size_t)(r0 + r) * CW + tc * CT + c] : acc[i][c];
+            Elem<T>::store(Bp + b_off<T>(g, r0 + r, c0 + tc * CT + c), v);
+          }
       }
     }
   }
@@ -212,7 +217,7 @@ int launch_solve_wide<double>(const LeafArgs& g, int, cudaStream_t s) {
 }  // namespace
 
 int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m, const Mat& A, const Mat& B,
-                cudaStream_t s) {
+                cudaStream_t s, bool unit) {
   if (n <= 0 || m <= 0) return NLA_OK;
   if (n > 1024) return fail(NLA_ERR_ARG, "diag block: n must be <= 1024");
   if (B.t) return fail(NLA_ERR_UNSUPPORTED, "diag block: transposed B view");
@@ -223,6 +228,7 @@ int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m
   g.B = B.p;
   g.ldb = B.ld;
   g.tB = 0;
+  g.unit = unit ? 1 : 0;
   g.n = (int)n;
   g.m = m;
   if (side == 'R') {  // X op(A) = B  <=>  op(A)^T X^T = B^T

@@ -39,6 +39,7 @@ struct LeafArgs {
   int64_t ldb;
   int tB;
   int rev;
+  int unit;  // unit diagonal: the diagonal of A is taken as 1 and not read
   int n;
   int64_t m;
 };
@@ -178,7 +179,8 @@ __device__ __forceinline__ void solve_block(const LeafArgs& g, int64_t c0, int n
   const T* A = static_cast<const T*>(g.A);
 
   load_block<T, Tc, CW>(g, X, c0, ncols, alpha);
-  for (int i = threadIdx.x; i < n; i += LEAF_THREADS) inv_d[i] = Tc(1) / Elem<T>::load(A + a_off<T>(g, i, i));
+  for (int i = threadIdx.x; i < n; i += LEAF_THREADS)
+    inv_d[i] = g.unit ? Tc(1) : Tc(1) / Elem<T>::load(A + a_off<T>(g, i, i));
   __syncthreads();
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -301,7 +303,8 @@ __device__ __forceinline__ void solve_block_wide(const LeafArgs& g, int64_t c0, 
   const T* A = static_cast<const T*>(g.A);
 
   load_block<T, Tc, CW>(g, X, c0, ncols, alpha);
-  for (int i = threadIdx.x; i < n; i += LEAF_THREADS) inv_d[i] = Tc(1) / Elem<T>::load(A + a_off<T>(g, i, i));
+  for (int i = threadIdx.x; i < n; i += LEAF_THREADS)
+    inv_d[i] = g.unit ? Tc(1) : Tc(1) / Elem<T>::load(A + a_off<T>(g, i, i));
   __syncthreads();
 
   const int t = threadIdx.x;
@@ -403,7 +406,7 @@ __device__ __forceinline__ void solve_cols_f64(const LeafArgs& g, int64_t c0, in
       if (idx < total) X[i * CW + cc] = v[u];
     }
   }
-  for (int i = t; i < n; i += NT) inv_d[i] = 1.0 / A[a_off<double>(g, i, i)];
+  for (int i = t; i < n; i += NT) inv_d[i] = g.unit ? 1.0 : 1.0 / A[a_off<double>(g, i, i)];
   for (int p0 = 0; p0 < n; p0 += PANEL) {
     const int pw = min(PANEL, n - p0);
     // Columns of A staged for the panel's rows: through the diagonal, rounded

@@ -21,7 +21,7 @@ module NextLA_GB300
 using CUDA
 using LinearAlgebra
 
-export unified_rectrxm!, unified_rectrxm_julia!, unified_rectrxm_mixed!
+export unified_rectrxm!, unified_rectrxm_julia!, unified_rectrxm_mixed!, trsm, trmm
 
 const libnla = get(ENV, "NEXTLA_GB300_LIB", joinpath(@__DIR__, "..", "libnextla_gb300.so"))
 
@@ -78,6 +78,36 @@ function unified_rectrxm!(side::Char, uplo::Char, transpose::Char, alpha::Number
                 side, up, tr, Float64(alpha), func, dtype_code(T), n, m, pA, lda, pB, ldb, stream_handle()))
     return B
 end
+
+"""
+    trsm(side, uplo, transa, diag, A, B, alpha=one(eltype(A))) -> B
+    trmm(side, uplo, transa, diag, A, B, alpha=one(eltype(A))) -> B
+
+The reference's wrappers (src/trsm.jl:186-204, src/trmm.jl:430-448) with the
+same arguments, run through the recursion (`nla_trxm_diag`): transa is applied
+and diag 'U' takes the diagonal of A as ones (the reference accepts both but
+calls one base-case kernel with op(A) = A and the stored diagonal).
+"""
+function trxm_diag!(func::Char, side::Char, uplo::Char, transa::Char, diag::Char,
+                    A::AbstractMatrix{T}, B::AbstractMatrix{T}, alpha) where {T<:Union{Float16,Float32,Float64}}
+    n = size(A, 1)
+    m = side == 'L' ? size(B, 2) : size(B, 1)
+    pA, lda, tA = operand(A)
+    pB, ldb, tB = operand(B)
+    tB && throw(ArgumentError("B must be column-major"))
+    tr, up = transa, uplo
+    if tA
+        tr = transa in ('T', 'C') ? 'N' : 'T'
+        up = uplo == 'L' ? 'U' : 'L'
+    end
+    check(ccall((:nla_trxm_diag, libnla), Cint,
+                (Cchar, Cchar, Cchar, Cchar, Cdouble, Cchar, Cint, Int64, Int64, CuPtr{Cvoid}, Int64, CuPtr{Cvoid},
+                 Int64, Ptr{Cvoid}),
+                side, up, tr, diag, Float64(alpha), func, dtype_code(T), n, m, pA, lda, pB, ldb, stream_handle()))
+    return B
+end
+trsm(side, uplo, transa, diag, A, B, alpha=one(eltype(A))) = trxm_diag!('S', side, uplo, transa, diag, A, B, alpha)
+trmm(side, uplo, transa, diag, A, B, alpha=one(eltype(A))) = trxm_diag!('M', side, uplo, transa, diag, A, B, alpha)
 
 # --- the reference's recursion driven from Julia ------------------------------
 

@@ -267,6 +267,44 @@ def unified_rec(func, side, uplo, A, n, B, threshold=256):
     return B
 
 
+def _trxm_diag(func, side, uplo, transa, diag, A, B, alpha):
+    _check_flags(side, uplo, transa, func)
+    if diag not in ("N", "U"):
+        raise ValueError("diag must be 'N' or 'U', got %r" % (diag,))
+    _check_operands(A, B, side)
+    n = A.shape[0]
+    a, lda, ta = _mat(A)
+    b, ldb, tb = _mat(B)
+    if tb:
+        raise ValueError("B must be a column-major view")
+    tr, up = transa, uplo
+    if ta:  # A is a transposed view of its parent: fold that into the flags
+        tr = "N" if transa in ("T", "C") else "T"
+        up = "U" if uplo == "L" else "L"
+    m = B.shape[1] if side == "L" else B.shape[0]
+    _lib.check(_lib.load().nla_trxm_diag(_lib.ch(side), _lib.ch(up), _lib.ch(tr), _lib.ch(diag), float(alpha),
+                                         _lib.ch(func), _dtype_code(B), n, m, a, lda, b, ldb, _stream(B)))
+    return B
+
+
+def trsm(side, uplo, transa, diag, A, B, alpha=1.0):
+    """trsm(side, uplo, transa, diag, A, B, alpha) (src/trsm.jl:186-204):
+    solves op(A) X = alpha B (side 'L') or X op(A) = alpha B ('R') in place in
+    B and returns B.  The reference scales B and calls one base-case kernel,
+    ignoring transa and diag (so it is limited to n <= 1024 and op(A) = A);
+    here the call runs the whole recursion (nla_trxm_diag), honours transa
+    and applies diag 'U' (unit diagonal, never read)."""
+    return _trxm_diag("S", side, uplo, transa, diag, A, B, alpha)
+
+
+def trmm(side, uplo, transa, diag, A, B, alpha=1.0):
+    """trmm(side, uplo, transa, diag, A, B, alpha) (src/trmm.jl:430-448):
+    B := alpha op(A) B (side 'L') or alpha B op(A) ('R'), in place, through
+    the recursion; transa and diag 'U' are applied (the reference ignores
+    both)."""
+    return _trxm_diag("M", side, uplo, transa, diag, A, B, alpha)
+
+
 def unified_rectrxm_(side, uplo, transpose, alpha, func, A, B, *, native=False, thresholds=None):
     """unified_rectrxm!(side, uplo, transpose, alpha, func, A, B) (src/rectrxm.jl:43-76).
 

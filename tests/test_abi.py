@@ -81,3 +81,12 @@ def test_python_mirror_rejects_bad_flags(pkg):
         pkg.unified_rectrxm_("Q", "L", "N", 1.0, "S", A, A)
     with pytest.raises(ValueError):
         pkg.unified_rectrxm_("L", "L", "N", 1.0, "X", A, A)
+
+
+def test_trxm_diag_rejects_bad_diag(lib):
+    """nla_trxm_diag validates diag before any device work."""
+    import ctypes
+
+    rc = lib.nla_trxm_diag(b"L", b"L", b"N", b"X", 1.0, b"S", 2, 4, 4, ctypes.c_void_p(16), 4,
+                           ctypes.c_void_p(16), 4, None)
+    assert rc == -1

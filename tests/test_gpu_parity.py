@@ -238,3 +238,29 @@ def test_f64_leaf_one_rhs_per_thread_exact(pkg, cuda):
         pkg.unified_rectrxm_("L", "L", "N", 1.0, "S", Ad, Bd, native=True)
         torch.cuda.synchronize()
         np.testing.assert_array_equal(to_host(Bd), X.astype(np.float64))
+
+
+@pytest.mark.parametrize("func", ["S", "M"])
+def test_trsm_trmm_wrappers_with_diag(pkg, oracle, workloads, cuda, func):
+    """trsm()/trmm() (src/trsm.jl:186-204, src/trmm.jl:430-448) through the
+    recursion: every side/uplo/transa, diag 'N' and 'U' (unit diagonal, never
+    read: the stored diagonal is NaN), n from one base case to a recursive
+    300, against BLAS at the Float64 bound."""
+    import torch
+
+    fn = pkg.trsm if func == "S" else pkg.trmm
+    for n, m, side, uplo, transa, diag in itertools.product([17, 300], [9], "LR", "LU", "NT", "NU"):
+        A, B = workloads.problem(n, m, side, uplo, seed=n + (diag == "U"))
+        An = A.copy()
+        if diag == "U":
+            An[np.diag_indices(n)] = np.nan
+        Ad, Bd = to_dev(An, np.float64, cuda), to_dev(B, np.float64, cuda)
+        fn(side, uplo, transa, diag, Ad, Bd, 0.5)
+        torch.cuda.synchronize()
+        Aref = A.copy()
+        if diag == "U":
+            Aref[np.diag_indices(n)] = 1.0
+        ref = oracle.blas_rectrxm(side, uplo, transa, 0.5, func, Aref, B)
+        got = to_host(Bd)
+        assert np.isfinite(got).all(), (n, side, uplo, transa, diag)
+        assert oracle.rel_err(got, ref) < 1e-14, (n, side, uplo, transa, diag)
