@@ -596,9 +596,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
 // Exact kernel with coupled pairs.  The 28 pairs (p, q) are walked as 16
 // groups: for each B slice q, the A slices p = 0, 2, 4, 6 each with its
 // successor p + 1 while p + 1 <= 6 - q.  A group's stage holds A_p, A_p+1
-// and B_q (48 KiB, three boxes) and feeds two accumulators, so a pair costs
+// (one 256-row box: the staging puts the slices of a tile next to each
+// other) and B_q, 48 KiB in all, and feeds two accumulators, so a pair costs
 // 24 KiB of tile loads instead of 32: the TMA feed, not the tensor core,
-// bounds these kernels (about 100-120 GB/s per SM with 16 KiB boxes).
+// bounds these kernels (about 100-120 GB/s per SM).
 // Each group's two accumulators (weights p + q and p + 1 + q) take half of a
 // 256-column TMEM buffer; two buffers fill the 512 columns.
 // Warps: 0 loads A, 1 issues the MMAs, 2 loads B, 3-10 drain.
