@@ -21,8 +21,10 @@ Variants:
           FP64-residual iterative refinement.
 
 Also reported on the same JSON line:
-  e2e           the same metric through the C ABI with host buffers: pinned
-                host A and B copied in, solved, B copied out, every step;
+  e2e           the same metric through the C ABI with host buffers
+                (nla_trxm_mixed_host / nla_trxm_host): pinned host A and B
+                copied in, solved and X copied out every step, the copies
+                pipelined with the recursion's top levels;
   roofline      the dominant kernel's achieved rate from live CUDA-event
                 tracing inside the timed region against the measured peak;
   cpu_baseline  the oracle (a C restatement of the reference algorithm) on the
@@ -60,6 +62,8 @@ def parse():
     ap.add_argument("--sweeps", type=int, default=0)
     ap.add_argument("--residual", choices=["split", "fp64"], default="split")
     ap.add_argument("--cutoff", type=int, default=0)
+    ap.add_argument("--host-levels", type=int, default=0,
+                    help="recursion levels the host-buffer call pipelines its copies over (0: library default)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison step")
     ap.add_argument("--workload", choices=["single", "batched"], default="single",
                     help="single: one n x m system; batched: 10,000 uneven systems in one persistent launch")
@@ -584,6 +588,19 @@ def run_kernel_case(args):
     return 0
 
 
+def staged_a_elems(n, levels, cutoff):
+    """Elements of A the host-buffer call copies in: the diagonal blocks where
+    its staged walk stops and the off-diagonal blocks of the triangle above
+    them."""
+    if levels <= 0 or n <= cutoff:
+        return n * n
+    p = 1
+    while p * 2 <= n:
+        p *= 2
+    mid = n // 2 if p == n else p
+    return staged_a_elems(mid, levels - 1, cutoff) + mid * (n - mid) + staged_a_elems(n - mid, levels - 1, cutoff)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -697,7 +714,9 @@ def main():
         xn = float(Xs_.abs().sum(dim=1).max())
         return rn / (an * xn * n * 2.0 ** -53), {"r_inf": rn, "a_inf": an, "x_inf": xn}
 
-    # End to end through the C ABI with host buffers.
+    # End to end through the C ABI with host buffers: the host-buffer entry
+    # point copies A's triangle and B in and X out in blocks pipelined with
+    # the recursion.
     A_pin = torch.from_numpy(np.ascontiguousarray(A_h.T)).pin_memory()
     B_pin = torch.from_numpy(np.ascontiguousarray(B_h.T)).pin_memory()
     X_pin = torch.empty_like(B_pin).pin_memory()
@@ -705,6 +724,16 @@ def main():
     Be = torch.empty_like(B0.T)
 
     def e2e_step():
+        if args.variant == "mixed":
+            _lib.check(L.nla_trxm_mixed_host(b"L", b"L", b"N", 1.0, b"S", n, m, A_pin.data_ptr(), n,
+                                             B_pin.data_ptr(), n, X_pin.data_ptr(), n, Ae.data_ptr(), n,
+                                             Be.data_ptr(), n, ctypes.byref(opts), args.host_levels, sptr))
+        else:
+            _lib.check(L.nla_trxm_host(b"L", b"L", b"N", 1.0, b"S", _lib.NLA_F64, n, m, A_pin.data_ptr(), n,
+                                       B_pin.data_ptr(), n, X_pin.data_ptr(), n, Ae.data_ptr(), n, Be.data_ptr(),
+                                       n, args.host_levels, sptr))
+
+    def sequential_step():
         Ae.copy_(A_pin, non_blocking=True)
         Be.copy_(B_pin, non_blocking=True)
         solve_fn(Ae.T, Be.T)
@@ -712,19 +741,29 @@ def main():
 
     # Each end-to-end step ends when its result is back on the host (a
     # synchronize, as a caller reading X must); the median step is reported.
-    e2e_steps = max(3, min(args.steps, 5))
-    e2e_step()
-    barrier()
-    e2e_times = []
-    for _ in range(e2e_steps):
-        t0 = time.perf_counter()
-        e2e_step()
+    def timed_steps(fn, count):
+        fn()
         barrier()
-        e2e_times.append(time.perf_counter() - t0)
+        times = []
+        for _ in range(count):
+            t0 = time.perf_counter()
+            fn()
+            barrier()
+            times.append(time.perf_counter() - t0)
+        return times
+
+    e2e_steps = max(3, min(args.steps, 5))
+    e2e_times = timed_steps(e2e_step, e2e_steps)
     e2e_s = statistics.median(e2e_times)
     e2e_value = world * flops / e2e_s / 1e12
-    # One more step, outside the timed ones, with device events between its
-    # phases: where the end-to-end time goes.
+    host_levels = args.host_levels if args.host_levels > 0 else int(os.environ.get("NLA_HOST_LEVELS", "3"))
+    host_cutoff = args.cutoff if args.cutoff > 0 else (128 if args.variant == "mixed" else 256)
+    # The host-buffer result against the device-resident solve of the timed loop.
+    e2e_same = bool(torch.equal(X_pin, B.T.cpu()))
+    # The same with copy-in, solve and copy-out one after another, and one
+    # more such step with device events between its phases: where the time
+    # goes without the pipelining.
+    seq_times = timed_steps(sequential_step, e2e_steps)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     ev[0].record(stream)
     Ae.copy_(A_pin, non_blocking=True)
@@ -736,7 +775,8 @@ def main():
     ev[3].record(stream)
     barrier()
     e2e_phases = {"h2d_ms": ev[0].elapsed_time(ev[1]), "solve_ms": ev[1].elapsed_time(ev[2]),
-                  "d2h_ms": ev[2].elapsed_time(ev[3])}
+                  "d2h_ms": ev[2].elapsed_time(ev[3]),
+                  "sequential_step_ms": round(statistics.median(seq_times) * 1e3, 2)}
 
     berr, berr_parts = backward_error(B)
     plain = None
@@ -811,8 +851,9 @@ def main():
             "speedup_vs_plain_fp64": (value / plain["tflops"]) if plain else None,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "phases_ms": e2e_phases,
                     "step_ms": [round(t * 1e3, 2) for t in e2e_times],
-                    "h2d_bytes_per_step": int(A_h.nbytes + B_h.nbytes),
-                    "d2h_bytes_per_step": int(B_h.nbytes)},
+                    "h2d_bytes_per_step": int(8 * staged_a_elems(n, host_levels, host_cutoff) + B_h.nbytes),
+                    "d2h_bytes_per_step": int(B_h.nbytes), "host_levels": host_levels,
+                    "matches_device_result": e2e_same},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": gpu_launches,
             "trace": {k: {"launches": v[0], "ms": v[1], "tflops": v[2] / max(v[1], 1e-9) / 1e9}
                       for k, v in trace.items()},

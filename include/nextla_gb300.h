@@ -159,6 +159,38 @@ NLA_API int nla_trxm_mixed(char side, char uplo, char trans, double alpha, char 
                            void* stream);
 
 /*
+ * Host-buffer forms of nla_trxm and nla_trxm_mixed: what a Julia caller does
+ * with host arrays around unified_rectrxm! (CuArray(A), CuArray(B), the call,
+ * copyto!(B, dB); src/rectrxm.jl:43-76), as one call.
+ *
+ * A_host and B_host are column-major host arrays (page-locked for the copies
+ * to overlap); A_dev and B_dev are caller-owned device arrays of the same
+ * shapes with leading dimensions lda_dev and ldb_dev.  The result goes to
+ * the host array X_host of B's shape (X_host == B_host with ldx == ldb is
+ * the reference's in-place form); B_dev holds it too.  B_host is only read
+ * and must not overlap X_host otherwise.  The top `host_levels` levels of the
+ * recursion (<= 0: the library default, 3) are split into blocks: each block
+ * of A and of B is copied to the device on a copy stream just before the
+ * recursion first touches it, and each block of the result is copied back
+ * on a second copy stream as soon as it is final, so copies overlap the
+ * solve.  Only the diagonal blocks and the off-diagonal blocks of the
+ * `uplo` triangle that the recursion reads are copied; the rest of A_dev is
+ * left as it was.  Refinement sweeps (nla_trxm_mixed with sweeps > 0) need
+ * all of the first solution, so that form copies in, solves and copies out
+ * without overlap.  The results are bit-identical to nla_trxm /
+ * nla_trxm_mixed on A_dev and B_dev.  Asynchronous on `stream`: B_host holds
+ * the result once the stream has been synchronised.
+ */
+NLA_API int nla_trxm_host(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
+                          const void* A_host, int64_t lda, const void* B_host, int64_t ldb, void* X_host,
+                          int64_t ldx, void* A_dev, int64_t lda_dev, void* B_dev, int64_t ldb_dev, int host_levels,
+                          void* stream);
+NLA_API int nla_trxm_mixed_host(char side, char uplo, char trans, double alpha, char func, int64_t n, int64_t m,
+                                const double* A_host, int64_t lda, const double* B_host, int64_t ldb, double* X_host,
+                                int64_t ldx, double* A_dev, int64_t lda_dev, double* B_dev, int64_t ldb_dev,
+                                const nla_mixed_opts* opts, int host_levels, void* stream);
+
+/*
  * One mixed-precision off-diagonal update (no counterpart in the reference;
  * the mixed form of matmul!, src/matmul.jl:5-66): out (N x M, FP64) +=
  * alpha * op(in1) (N x R) * op(in2) (R x M) from `split_terms` BF16/FP16

@@ -14,14 +14,15 @@ from ._lib import NLAArgumentError, NLAError
 from .rectrxm import (GEMM_ADD_, GEMM_SUB_, LeftLowerTRMM_, LeftLowerTRSM_, LeftUpperTRMM_, LeftUpperTRSM_,
                       RightLowerTRMM_, RightLowerTRSM_, RightUpperTRMM_, RightUpperTRSM_, device_status,
                       matmul_, matmul_mixed_, residual_, scale_, split_point, trmm, trsm, unified_rec,
-                      unified_rectrxm_, unified_rectrxm_mixed_)
+                      unified_rectrxm_, unified_rectrxm_host_, unified_rectrxm_mixed_,
+                      unified_rectrxm_mixed_host_)
 
 __all__ = [
     "unified_rectrxm_", "unified_rec", "split_point", "matmul_", "scale_", "GEMM_ADD_", "GEMM_SUB_",
     "LeftLowerTRSM_", "LeftUpperTRSM_", "RightLowerTRSM_", "RightUpperTRSM_",
     "LeftLowerTRMM_", "LeftUpperTRMM_", "RightLowerTRMM_", "RightUpperTRMM_",
     "NLAError", "NLAArgumentError", "load_library", "unified_rectrxm_mixed_", "matmul_mixed_", "device_status",
-    "residual_", "trsm", "trmm",
+    "residual_", "trsm", "trmm", "unified_rectrxm_host_", "unified_rectrxm_mixed_host_",
 ]
 
 

@@ -205,35 +205,59 @@ int64_t split_point(int64_t n) {
 // ---------------------------------------------------------------------------
 // Recursion (unified_rec, src/rectrxm.jl:101-198).
 // ---------------------------------------------------------------------------
+// The first half (A11, B1) is processed first in these four cases
+// (src/rectrxm.jl:104-124); otherwise the second half (A22, B2) is.
+bool rec_forward(const RecPlan& c) {
+  const bool S = c.func == 'S', L = c.side == 'L';
+  return (L && c.uplo == 'L' && S) || (!L && c.uplo == 'U' && S) || (L && c.uplo == 'U' && !S) ||
+         (!L && c.uplo == 'L' && !S);
+}
+
+// Whether the update between the halves reads A21 (else A12).
+bool rec_update_reads_a21(const RecPlan& c) {
+  return rec_forward(c) != (c.side == 'R') != (c.func == 'M');
+}
+
+// The update between the two halves of one recursion node on the n x n
+// diagonal block A and its rows (side 'L') or columns ('R') of B.  A solve
+// writes the half processed second from the one solved first; a multiply
+// adds into the half processed first from the other.
+int rec_update(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
+  const int64_t mid = split_point(n), rem = n - mid;
+  const int d = c.dtype;
+  const Mat A21 = sub(A, mid, 0, d), A12 = sub(A, 0, mid, d);
+  const Mat B1 = B, B2 = c.side == 'L' ? sub(B, mid, 0, d) : sub(B, 0, mid, d);
+  const bool S = c.func == 'S', L = c.side == 'L';
+  const int64_t m = c.m;
+  if (rec_forward(c)) {
+    if (L) {
+      if (S) return launch_update(c, rem, m, mid, -1.0, A21, B1, B2);  // B2 -= A21*B1
+      return launch_update(c, mid, m, rem, 1.0, A12, B2, B1);          // B1 += A12*B2
+    }
+    if (S) return launch_update(c, m, rem, mid, -1.0, B1, A12, B2);  // B2 -= B1*A12
+    return launch_update(c, m, mid, rem, 1.0, B2, A21, B1);          // B1 += B2*A21
+  }
+  if (L) {
+    if (S) return launch_update(c, mid, m, rem, -1.0, A12, B2, B1);  // B1 -= A12*B2
+    return launch_update(c, rem, m, mid, 1.0, A21, B1, B2);          // B2 += A21*B1
+  }
+  if (S) return launch_update(c, m, mid, rem, -1.0, B2, A21, B1);  // B1 -= B2*A21
+  return launch_update(c, m, rem, mid, 1.0, B1, A12, B2);          // B2 += B1*A12
+}
+
 int recurse(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
   if (n <= c.threshold) return launch_leaf(c.func, c.side, c.uplo, c.dtype, n, c.m, A, B, c.s, c.unit);
   const int64_t mid = split_point(n), rem = n - mid;
   const int d = c.dtype;
-  const Mat A11 = A, A22 = sub(A, mid, mid, d), A21 = sub(A, mid, 0, d), A12 = sub(A, 0, mid, d);
+  const Mat A11 = A, A22 = sub(A, mid, mid, d);
   const Mat B1 = B, B2 = c.side == 'L' ? sub(B, mid, 0, d) : sub(B, 0, mid, d);
-  const bool S = c.func == 'S', L = c.side == 'L';
-  const bool forward = (L && c.uplo == 'L' && S) || (!L && c.uplo == 'U' && S) || (L && c.uplo == 'U' && !S) ||
-                       (!L && c.uplo == 'L' && !S);
-  const int64_t m = c.m;
-  if (forward) {
+  if (rec_forward(c)) {
     NLA_TRY(recurse(c, A11, mid, B1));
-    if (L) {
-      if (S) NLA_TRY(launch_update(c, rem, m, mid, -1.0, A21, B1, B2));  // B2 -= A21*B1
-      else NLA_TRY(launch_update(c, mid, m, rem, 1.0, A12, B2, B1));     // B1 += A12*B2
-    } else {
-      if (S) NLA_TRY(launch_update(c, m, rem, mid, -1.0, B1, A12, B2));  // B2 -= B1*A12
-      else NLA_TRY(launch_update(c, m, mid, rem, 1.0, B2, A21, B1));     // B1 += B2*A21
-    }
+    NLA_TRY(rec_update(c, A, n, B));
     return recurse(c, A22, rem, B2);
   }
   NLA_TRY(recurse(c, A22, rem, B2));
-  if (L) {
-    if (S) NLA_TRY(launch_update(c, mid, m, rem, -1.0, A12, B2, B1));  // B1 -= A12*B2
-    else NLA_TRY(launch_update(c, rem, m, mid, 1.0, A21, B1, B2));     // B2 += A21*B1
-  } else {
-    if (S) NLA_TRY(launch_update(c, m, mid, rem, -1.0, B2, A21, B1));  // B1 -= B2*A21
-    else NLA_TRY(launch_update(c, m, rem, mid, 1.0, B1, A12, B2));     // B2 += B1*A12
-  }
+  NLA_TRY(rec_update(c, A, n, B));
   return recurse(c, A11, mid, B1);
 }
 
@@ -250,31 +274,37 @@ int64_t default_cutoff(char func, int dtype) {
   return env_cutoff("NLA_TRXM_CUTOFF_M", 128);
 }
 
-int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
-              const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, cudaStream_t s,
-              bool unit) {
+int trxm_plan(char side, char uplo, char trans, char func, int dtype, int64_t n, int64_t m, const void* A,
+              int64_t lda, const void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, cudaStream_t s, bool unit,
+              RecPlan* c, int* a_trans) {
   NLA_TRY(check_flags(side, uplo, trans, func, dtype));
   if (n < 0 || m < 0) return fail(NLA_ERR_ARG, "n and m must be non-negative");
   NLA_TRY(check_matrix("A", A, n, n, lda));
   NLA_TRY(check_matrix("B", B, side == 'L' ? n : m, side == 'L' ? m : n, ldb));
-  if (n == 0 || m == 0) return NLA_OK;
-  Mat Am{const_cast<void*>(A), lda, 0};
-  Mat Bm{B, ldb, 0};
+  *a_trans = 0;
   if (trans == 'T' || trans == 'C') {  // src/rectrxm.jl:56-59
-    Am.t = 1;
+    *a_trans = 1;
     uplo = uplo == 'L' ? 'U' : 'L';
   }
+  *c = RecPlan{func, side, uplo, dtype, m, 0, s, GEMM_PLAIN, 1, false};
+  c->unit = unit;
+  const int64_t cut = func == 'S' ? (cutoff_s > 0 ? cutoff_s : default_cutoff('S', dtype))
+                                  : (cutoff_m > 0 ? cutoff_m : default_cutoff('M', dtype));
+  c->threshold = cut > 1024 ? 1024 : cut;
+  return NLA_OK;
+}
+
+int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
+              const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, cudaStream_t s,
+              bool unit) {
+  RecPlan c{};
+  int at = 0;
+  NLA_TRY(trxm_plan(side, uplo, trans, func, dtype, n, m, A, lda, B, ldb, cutoff_s, cutoff_m, s, unit, &c, &at));
+  if (n == 0 || m == 0) return NLA_OK;
+  const Mat Am{const_cast<void*>(A), lda, at};
+  const Mat Bm{B, ldb, 0};
   const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
-  RecPlan c{func, side, uplo, dtype, m, 0, s, GEMM_PLAIN, 1, false};
-  c.unit = unit;
-  if (func == 'S') {
-    c.threshold = cutoff_s > 0 ? cutoff_s : default_cutoff('S', dtype);
-    if (c.threshold > 1024) c.threshold = 1024;
-    NLA_TRY(launch_scale(dtype, rows, cols, alpha, Bm, s));  // src/rectrxm.jl:64
-  } else {
-    c.threshold = cutoff_m > 0 ? cutoff_m : default_cutoff('M', dtype);
-    if (c.threshold > 1024) c.threshold = 1024;
-  }
+  if (func == 'S') NLA_TRY(launch_scale(dtype, rows, cols, alpha, Bm, s));  // src/rectrxm.jl:64
   NLA_TRY(recurse(c, Am, n, Bm));
   if (func == 'M') NLA_TRY(launch_scale(dtype, rows, cols, alpha, Bm, s));  // src/rectrxm.jl:72
   return NLA_OK;

@@ -175,10 +175,26 @@ struct RecPlan {
   bool unit = false;  // unit diagonal (plain path only)
 };
 int recurse(const RecPlan& c, const Mat& A, int64_t n, const Mat& B);
-// The plain recursion behind nla_trxm / nla_trxm_ex / nla_trxm_diag.
+// One node of the recursion: which half goes first, which off-diagonal block
+// the update between the halves reads, and that update.
+bool rec_forward(const RecPlan& c);
+bool rec_update_reads_a21(const RecPlan& c);
+int rec_update(const RecPlan& c, const Mat& A, int64_t n, const Mat& B);
+// The plain recursion behind nla_trxm / nla_trxm_ex / nla_trxm_diag, and its
+// argument checks and plan (a_trans: A is used transposed).
+int trxm_plan(char side, char uplo, char trans, char func, int dtype, int64_t n, int64_t m, const void* A,
+              int64_t lda, const void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, cudaStream_t s, bool unit,
+              RecPlan* c, int* a_trans);
 int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
               const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, cudaStream_t s,
               bool unit = false);
+// The mixed-precision recursion behind nla_trxm_mixed, and its checks and plan
+// (which also sizes the update workspace on stream s).
+int mixed_plan(char side, char uplo, char trans, char func, int64_t n, int64_t m, const void* A, int64_t lda,
+               const void* B, int64_t ldb, const nla_mixed_opts* o, cudaStream_t s, RecPlan* c, int* a_trans,
+               nla_mixed_opts* out);
+int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, int64_t n, int64_t m,
+                    const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* o, cudaStream_t s);
 int64_t split_point(int64_t n);
 int check_flags(char side, char uplo, char trans, char func, int dtype);
 int check_matrix(const char* name, const void* p, int64_t rows, int64_t cols, int64_t ld);

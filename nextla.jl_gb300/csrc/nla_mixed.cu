@@ -182,9 +182,9 @@ int split_residual(const Mat& Am, const Staged& As, char side, int64_t n, int64_
   return launch_exact_gemm(As, *Xs, -1.0, Rm, true, s, &term);
 }
 
-int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, int64_t n, int64_t m,
-                    const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* o,
-                    cudaStream_t s) {
+int mixed_plan(char side, char uplo, char trans, char func, int64_t n, int64_t m, const void* A, int64_t lda,
+               const void* B, int64_t ldb, const nla_mixed_opts* o, cudaStream_t s, RecPlan* c, int* a_trans,
+               nla_mixed_opts* out) {
   NLA_TRY(check_flags(side, uplo, trans, func, NLA_F64));
   if (n < 0 || m < 0) return fail(NLA_ERR_ARG, "n and m must be non-negative");
   NLA_TRY(check_matrix("A", A, n, n, lda));
@@ -200,25 +200,36 @@ int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, i
   if (opts.sweeps < 0 || opts.sweeps > 8) return fail(NLA_ERR_ARG, "sweeps must be in 0..8");
   if (opts.residual != NLA_RESIDUAL_FP64 && opts.residual != NLA_RESIDUAL_SPLIT)
     return fail(NLA_ERR_ARG, "unknown residual mode");
-  if (n == 0 || m == 0) return NLA_OK;
-
-  Mat Am{const_cast<double*>(A), lda, 0};
-  Mat Bm{B, ldb, 0};
+  *out = opts;
+  *a_trans = 0;
   if (trans == 'T' || trans == 'C') {  // src/rectrxm.jl:56-59
-    Am.t = 1;
+    *a_trans = 1;
     uplo = uplo == 'L' ? 'U' : 'L';
   }
-  RecPlan mixed{func, side, uplo, NLA_F64, m, opts.cutoff > 0 ? (opts.cutoff > 1024 ? 1024 : opts.cutoff)
-                                                               : default_mixed_cutoff(),
-                s, GEMM_MIXED, opts.split_terms, opts.lowp == NLA_LOWP_BF16};
-
+  *c = RecPlan{func, side, uplo, NLA_F64, m, opts.cutoff > 0 ? (opts.cutoff > 1024 ? 1024 : opts.cutoff)
+                                                             : default_mixed_cutoff(),
+               s, GEMM_MIXED, opts.split_terms, opts.lowp == NLA_LOWP_BF16};
+  if (n == 0 || m == 0) return NLA_OK;
   // Size the staging workspace once for the largest update (the top split).
-  {
-    const int64_t mid = split_point(n), rem = n - mid;
-    const int64_t big = mid > rem ? mid : rem;
-    void* ws = nullptr;
-    if (n > mixed.threshold) NLA_TRY(workspace_get(s, sliced_workspace_bytes(big, m, big, opts.split_terms), &ws));
-  }
+  const int64_t mid = split_point(n), rem = n - mid;
+  const int64_t big = mid > rem ? mid : rem;
+  void* ws = nullptr;
+  if (n > c->threshold) NLA_TRY(workspace_get(s, sliced_workspace_bytes(big, m, big, opts.split_terms), &ws));
+  return NLA_OK;
+}
+
+int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, int64_t n, int64_t m,
+                    const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* o,
+                    cudaStream_t s) {
+  RecPlan mixed{};
+  nla_mixed_opts opts{};
+  int at = 0;
+  NLA_TRY(mixed_plan(side, uplo, trans, func, n, m, A, lda, B, ldb, o, s, &mixed, &at, &opts));
+  if (n == 0 || m == 0) return NLA_OK;
+  uplo = mixed.uplo;
+  const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
+  const Mat Am{const_cast<double*>(A), lda, at};
+  const Mat Bm{B, ldb, 0};
 
   if (func == 'M') {
     NLA_TRY(recurse(mixed, Am, n, Bm));

@@ -21,7 +21,7 @@ module NextLA_GB300
 using CUDA
 using LinearAlgebra
 
-export unified_rectrxm!, unified_rectrxm_julia!, unified_rectrxm_mixed!, trsm, trmm
+export unified_rectrxm!, unified_rectrxm_julia!, unified_rectrxm_mixed!, unified_rectrxm_mixed_host!, trsm, trmm
 
 const libnla = get(ENV, "NEXTLA_GB300_LIB", joinpath(@__DIR__, "..", "libnextla_gb300.so"))
 
@@ -219,6 +219,33 @@ function unified_rectrxm_mixed!(side::Char, uplo::Char, transpose::Char, alpha::
                  Ref{MixedOpts}, Ptr{Cvoid}),
                 side, uplo, transpose, Float64(alpha), func, n, m, pointer(A), stride(A, 2), pointer(B), stride(B, 2),
                 opts, stream_handle()))
+    return B
+end
+
+"""
+    unified_rectrxm_mixed_host!(side, uplo, transpose, alpha, func, A, B; split_terms=7, sweeps=0)
+
+The mixed form on host `Matrix{Float64}` arrays (`nla_trxm_mixed_host`): the
+copies of A's triangle and B in and of the result out overlap the solve, and
+the result overwrites `B`. Pin `A` and `B` (`CUDA.Mem.pin`) for the overlap.
+Returns once `B` holds the result.
+"""
+function unified_rectrxm_mixed_host!(side::Char, uplo::Char, transpose::Char, alpha::Number, func::Char,
+                                     A::Matrix{Float64}, B::Matrix{Float64};
+                                     lowp::Symbol=:bf16, split_terms::Integer=7, sweeps::Integer=0,
+                                     residual::Symbol=:split, cutoff::Integer=0, host_levels::Integer=0)
+    opts = Ref(MixedOpts(lowp == :bf16 ? 0 : 1, split_terms, sweeps, residual == :split ? 1 : 0, cutoff, C_NULL))
+    n = size(A, 1)
+    m = side == 'L' ? size(B, 2) : size(B, 1)
+    dA = CuMatrix{Float64}(undef, size(A))
+    dB = CuMatrix{Float64}(undef, size(B))
+    check(ccall((:nla_trxm_mixed_host, libnla), Cint,
+                (Cchar, Cchar, Cchar, Cdouble, Cchar, Int64, Int64, Ptr{Cdouble}, Int64, Ptr{Cdouble}, Int64,
+                 Ptr{Cdouble}, Int64, CuPtr{Cdouble}, Int64, CuPtr{Cdouble}, Int64, Ref{MixedOpts}, Cint, Ptr{Cvoid}),
+                side, uplo, transpose, Float64(alpha), func, n, m, pointer(A), max(stride(A, 2), 1), pointer(B),
+                max(stride(B, 2), 1), pointer(B), max(stride(B, 2), 1), pointer(dA), max(stride(dA, 2), 1),
+                pointer(dB), max(stride(dB, 2), 1), opts, host_levels, stream_handle()))
+    CUDA.synchronize()
     return B
 end
 

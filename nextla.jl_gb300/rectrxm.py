@@ -443,3 +443,92 @@ def device_status(X=None):
     """Synchronise the stream and raise if a bounded device-side wait gave up."""
     L = _lib.load()
     _lib.check(L.nla_device_status(_stream(X) if X is not None else None))
+
+
+# ---------------------------------------------------------------------------
+# Host-buffer forms: CuArray(A), CuArray(B), unified_rectrxm!, copyto! as one
+# call, with the copies pipelined against the recursion.
+# ---------------------------------------------------------------------------
+
+def _host_mat(X, name):
+    """(pointer, leading dimension) of a column-major 2-D CPU tensor view."""
+    if X.dim() != 2 or X.is_cuda:
+        raise ValueError("%s must be a 2-D CPU tensor" % name)
+    r, c = X.shape
+    s0, s1 = X.stride()
+    if (s0 == 1 or r <= 1) and (c <= 1 or s1 >= max(r, 1)):
+        return X.data_ptr(), (s1 if c > 1 else max(r, 1))
+    raise ValueError("%s must be a column-major view (strides %s)" % (name, (s0, s1)))
+
+
+def _host_call(side, uplo, transpose, func, A, B, X, A_dev, B_dev, dtype):
+    import torch
+
+    _check_flags(side, uplo, transpose, func)
+    if A.dtype != dtype or B.dtype != dtype:
+        raise ValueError("A and B must be %s" % dtype)
+    n = A.shape[0]
+    if tuple(A.shape) != (n, n):
+        raise ValueError("A must be square, got %s" % (tuple(A.shape),))
+    if (side == "L" and B.shape[0] != n) or (side == "R" and B.shape[1] != n):
+        raise ValueError("B of shape %s does not conform with A of size %d for side %r" % (tuple(B.shape), n, side))
+    X = B if X is None else X
+    if tuple(X.shape) != tuple(B.shape) or X.dtype != dtype:
+        raise ValueError("X must have B's shape and element type")
+    dev = A_dev.device if A_dev is not None else (B_dev.device if B_dev is not None else torch.device("cuda"))
+    if A_dev is None:
+        A_dev = torch.empty_strided((n, n), (1, max(n, 1)), dtype=dtype, device=dev)
+    if B_dev is None:
+        B_dev = torch.empty_strided(tuple(B.shape), (1, max(B.shape[0], 1)), dtype=dtype, device=dev)
+    a, lda = _host_mat(A, "A")
+    b, ldb = _host_mat(B, "B")
+    x, ldx = _host_mat(X, "X")
+    ad, ldad, tad = _mat(A_dev)
+    bd, ldbd, tbd = _mat(B_dev)
+    if tad or tbd or tuple(A_dev.shape) != (n, n) or tuple(B_dev.shape) != tuple(B.shape):
+        raise ValueError("A_dev and B_dev must be column-major device arrays of A's and B's shapes")
+    m = B.shape[1] if side == "L" else B.shape[0]
+    return n, m, (a, lda, b, ldb, x, ldx, ad, ldad, bd, ldbd), X, torch.cuda.current_stream(dev)
+
+
+def unified_rectrxm_host_(side, uplo, transpose, alpha, func, A, B, *, X=None, A_dev=None, B_dev=None,
+                          host_levels=0, synchronize=True):
+    """unified_rectrxm! (src/rectrxm.jl:43-76) on host (CPU) tensors A and B,
+    column-major and preferably pinned: the result goes to X (default: B, in
+    place).  A_dev / B_dev are optional device arrays of A's and B's shapes
+    (allocated when not given).  The copies in and out are pipelined with the
+    native recursion over its top ``host_levels`` levels (0: library
+    default).  With ``synchronize`` the call returns once X holds the result."""
+    n, m, ptrs, X, stream = _host_call(side, uplo, transpose, func, A, B, X, A_dev, B_dev, A.dtype)
+    code = _dtype_code(A)
+    a, lda, b, ldb, x, ldx, ad, ldad, bd, ldbd = ptrs
+    L = _lib.load()
+    _lib.check(L.nla_trxm_host(_lib.ch(side), _lib.ch(uplo), _lib.ch(transpose), float(alpha), _lib.ch(func), code,
+                               n, m, a, lda, b, ldb, x, ldx, ad, ldad, bd, ldbd, int(host_levels),
+                               stream.cuda_stream))
+    if synchronize:
+        stream.synchronize()
+    return X
+
+
+def unified_rectrxm_mixed_host_(side, uplo, transpose, alpha, func, A, B, *, X=None, A_dev=None, B_dev=None,
+                                lowp="bf16", split_terms=7, sweeps=0, cutoff=0, residual="split", host_levels=0,
+                                synchronize=True):
+    """The mixed-precision unified_rectrxm! on Float64 host tensors (see
+    ``unified_rectrxm_host_`` for the buffers and ``unified_rectrxm_mixed_``
+    for the options; here the defaults are the exact 7-slice updates without
+    refinement)."""
+    import ctypes
+
+    import torch
+
+    n, m, ptrs, X, stream = _host_call(side, uplo, transpose, func, A, B, X, A_dev, B_dev, torch.float64)
+    a, lda, b, ldb, x, ldx, ad, ldad, bd, ldbd = ptrs
+    opts = _lib.MixedOpts(_LOWP[lowp], int(split_terms), int(sweeps), _RESIDUAL[residual], int(cutoff), None)
+    L = _lib.load()
+    _lib.check(L.nla_trxm_mixed_host(_lib.ch(side), _lib.ch(uplo), _lib.ch(transpose), float(alpha), _lib.ch(func),
+                                     n, m, a, lda, b, ldb, x, ldx, ad, ldad, bd, ldbd, ctypes.byref(opts),
+                                     int(host_levels), stream.cuda_stream))
+    if synchronize:
+        stream.synchronize()
+    return X

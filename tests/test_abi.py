@@ -90,3 +90,23 @@ def test_trxm_diag_rejects_bad_diag(lib):
     rc = lib.nla_trxm_diag(b"L", b"L", b"N", b"X", 1.0, b"S", 2, 4, 4, ctypes.c_void_p(16), 4,
                            ctypes.c_void_p(16), 4, None)
     assert rc == -1
+
+
+def test_host_entries_reject_bad_arguments(lib):
+    """The host-buffer entry points check flags and buffers before any device
+    work: a bad flag, a missing result buffer or a short leading dimension is
+    NLA_ERR_ARG."""
+    import ctypes
+
+    p = ctypes.c_void_p(16)
+    # bad side
+    assert lib.nla_trxm_host(b"X", b"L", b"N", 1.0, b"S", 2, 4, 4, p, 4, p, 4, p, 4, p, 4, p, 4, 0, None) == -1
+    # no X_host
+    assert lib.nla_trxm_host(b"L", b"L", b"N", 1.0, b"S", 2, 4, 4, p, 4, p, 4, None, 4, p, 4, p, 4, 0, None) == -1
+    # A_dev leading dimension below n
+    assert lib.nla_trxm_host(b"L", b"L", b"N", 1.0, b"S", 2, 4, 4, p, 4, p, 4, p, 4, p, 3, p, 4, 0, None) == -1
+    assert lib.nla_trxm_mixed_host(b"L", b"L", b"Q", 1.0, b"S", 4, 4, p, 4, p, 4, p, 4, p, 4, p, 4, None, 0,
+                                   None) == -1
+    assert lib.nla_trxm_mixed_host(b"L", b"L", b"N", 1.0, b"S", 4, 4, p, 4, p, 4, p, 4, p, 4, None, 4, None, 0,
+                                   None) == -1
+    assert b"B_dev" in lib.nla_last_error()
