@@ -82,6 +82,7 @@ def parse():
                     help="run single launches of one kernel on a moderate case (for ncu captures)")
     ap.add_argument("--case-size", type=int, default=4096)
     ap.add_argument("--case-reps", type=int, default=2)
+    ap.add_argument("--case-shape", default="", help="M,N,K of the exact/fast update case (default: s,s,s)")
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--m", type=int, default=16384)
     ap.add_argument("--cpu-sample", type=int, default=0,
@@ -537,7 +538,8 @@ def run_kernel_case(args):
     """Single launches of one kernel on an s x s case (s = --case-size),
     sized so that operands exceed L2 but the device holds a few GB at most:
       exact  one exact slice-product update, C (s x s) -= A (s x s) B (s x s),
-             7 BF16 slices per operand;
+             7 BF16 slices per operand (--case-shape M,N,K for C (M x N) -=
+             A (M x K) B (K x N));
       fast   the same with 3 BF16 slices (FP32 accumulation);
       leaf   one FP64 diagonal-block solve of order 128 with 8 s right-hand
              sides;
@@ -565,7 +567,8 @@ def run_kernel_case(args):
     times = []
     for _ in range(args.case_reps):
         if args.kernel_case in ("exact", "fast"):
-            A, B, C = cm(s, s), cm(s, s), cm(s, s)
+            M, N, K = (int(x) for x in args.case_shape.split(",")) if args.case_shape else (s, s, s)
+            A, B, C = cm(M, K), cm(K, N), cm(M, N)
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
             pkg.matmul_mixed_(C, A, B, -1.0, split_terms=7 if args.kernel_case == "exact" else 3)
@@ -584,7 +587,8 @@ def run_kernel_case(args):
             pkg.GEMM_SUB_(C, A, B)
         pkg.device_status()
         times.append((time.perf_counter() - t0) * 1e3)
-    print(json.dumps({"kernel_case": args.kernel_case, "size": s, "host_ms": times}), flush=True)
+    print(json.dumps({"kernel_case": args.kernel_case, "size": s, "shape": args.case_shape or None,
+                      "host_ms": times}), flush=True)
     return 0
 
 

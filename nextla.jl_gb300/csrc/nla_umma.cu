@@ -331,15 +331,52 @@ __device__ __forceinline__ int exact_row_lb(const ExactParams& p, int i) {
 
 // Adds one exact FP32 chunk sum (64 TMEM columns of this thread's lane at ta)
 // into the int64 fixed point, shifted by sh (rounded half up when sh < 0).
+// The chunk sums are integers below 2^24 in magnitude, so each converts to an
+// int32 v exactly.  When every lane of the warp has sh >= 0, v * 2^sh is built
+// from 32-bit shifts: low word v << sh (0 once sh >= 32), high word the
+// funnel shift of (sign(v) : v) by min(sh, 32), shifted on by sh - 32.  When
+// every lane has -24 <= sh < 0 the rounded shift stays in 32 bits.  Both give
+// the same bits as the 64-bit expression of the general case.
+__device__ __forceinline__ uint32_t shl_clamped(uint32_t a, uint32_t s) {
+  uint32_t d;
+  asm("shl.b32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(s));  // shifts of 32 or more give 0
+  return d;
+}
+
 __device__ __forceinline__ void exact_drain(long long (&acc)[64], uint32_t ta, int sh) {
+  if (__all_sync(0xffffffffu, sh >= 0)) {
+    const uint32_t s_lo = (uint32_t)sh, s_hi = (uint32_t)max(sh - 32, 0);
 #pragma unroll
-  for (int j0 = 0; j0 < 64; j0 += 16) {
-    uint32_t r[16];
-    umma::tmem_ld16(ta + (uint32_t)j0, r);
+    for (int j0 = 0; j0 < 64; j0 += 16) {
+      uint32_t r[16];
+      umma::tmem_ld16(ta + (uint32_t)j0, r);
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      const long long v = (long long)__float2int_rn(__uint_as_float(r[j]));
-      acc[j0 + j] += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
+      for (int j = 0; j < 16; ++j) {
+        const int v = __float2int_rn(__uint_as_float(r[j]));
+        const uint32_t lo = shl_clamped((uint32_t)v, s_lo);
+        const uint32_t hi = __funnelshift_lc((uint32_t)v, (uint32_t)(v >> 31), s_lo) << s_hi;
+        acc[j0 + j] += (long long)(((unsigned long long)hi << 32) | lo);
+      }
+    }
+  } else if (__all_sync(0xffffffffu, sh < 0 && sh >= -24)) {
+    const int n = -sh, bias = 1 << (n - 1);
+#pragma unroll
+    for (int j0 = 0; j0 < 64; j0 += 16) {
+      uint32_t r[16];
+      umma::tmem_ld16(ta + (uint32_t)j0, r);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) acc[j0 + j] += (long long)((__float2int_rn(__uint_as_float(r[j])) + bias) >> n);
+    }
+  } else {
+#pragma unroll
+    for (int j0 = 0; j0 < 64; j0 += 16) {
+      uint32_t r[16];
+      umma::tmem_ld16(ta + (uint32_t)j0, r);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const long long v = (long long)__float2int_rn(__uint_as_float(r[j]));
+        acc[j0 + j] += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
+      }
     }
   }
 }
