@@ -37,12 +37,12 @@ __global__ void __launch_bounds__(LEAF_THREADS) leaf_solve_wide_kernel(LeafArgs 
   solve_block_wide<T, CW>(g, c0, ncols, smem_raw, typename Elem<T>::compute(1));
 }
 
-template <int HALVES>
-__global__ void __launch_bounds__(LEAF_THREADS * HALVES, 1) leaf_solve_cols_kernel(LeafArgs g) {
+template <int HALVES, int CW>
+__global__ void __launch_bounds__(CW * HALVES, 1) leaf_solve_cols_kernel(LeafArgs g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int64_t c0 = (int64_t)blockIdx.x * LEAF_THREADS;
-  const int ncols = (int)(g.m - c0 < LEAF_THREADS ? g.m - c0 : LEAF_THREADS);
-  solve_cols_f64<HALVES>(g, c0, ncols, smem_raw, 1.0);
+  const int64_t c0 = (int64_t)blockIdx.x * CW;
+  const int ncols = (int)(g.m - c0 < CW ? g.m - c0 : CW);
+  solve_cols_f64<HALVES, CW>(g, c0, ncols, smem_raw, 1.0);
 }
 
 // Canonical lower-left multiply: X := L X for CW columns.
@@ -165,24 +165,46 @@ int leaf_cols_mode() {
   return mode;
 }
 
-template <int HALVES>
+template <int HALVES, int CW>
 int launch_leaf_cols(const LeafArgs& g, cudaStream_t s) {
-  const size_t smem = leaf_cols_smem_elems(g.n, HALVES) * sizeof(double);
-  const int64_t grid = (g.m + LEAF_THREADS - 1) / LEAF_THREADS;
+  const size_t smem = leaf_cols_smem_elems(g.n, HALVES, CW) * sizeof(double);
+  const int64_t grid = (g.m + CW - 1) / CW;
   if (g.n > COLS_MAX_N || smem > 200 * 1024) return fail(NLA_ERR_UNSUPPORTED, "leaf: shared memory plan too large");
   if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "leaf: too many right-hand sides");
   static std::once_flag once;
   static cudaError_t st = cudaSuccess;
   std::call_once(once, [] {
-    st = cudaFuncSetAttribute(leaf_solve_cols_kernel<HALVES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    st = cudaFuncSetAttribute(leaf_solve_cols_kernel<HALVES, CW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               200 * 1024);
   });
   if (st != cudaSuccess) return cuda_status(st, "cudaFuncSetAttribute(leaf_solve_cols_kernel)");
   TraceScope trace(NLA_K_LEAF_SOLVE, s, (double)g.n * g.n * (double)g.m,
                    8.0 * ((double)g.n * (g.n + 1) / 2 + 2.0 * (double)g.n * g.m));
-  leaf_solve_cols_kernel<HALVES><<<(unsigned)grid, LEAF_THREADS * HALVES, smem, s>>>(g);
+  leaf_solve_cols_kernel<HALVES, CW><<<(unsigned)grid, CW * HALVES, smem, s>>>(g);
   NLA_CHECK_LAUNCH("leaf_solve_cols_kernel");
   return NLA_OK;
+}
+
+// Right-hand sides per CTA of the two-threads-per-column leaf: the fewest of
+// 128, 112, 96 and 64 that keep every CTA in one wave of one CTA per SM
+// (NLA_LEAF_CW forces one of them).
+int leaf_cols_width(int64_t m) {
+  const char* v = getenv("NLA_LEAF_CW");  // read per launch, so tests can pin each width
+  const int forced = v ? atoi(v) : 0;
+  if (forced == 128 || forced == 112 || forced == 96 || forced == 64) return forced;
+  const int64_t sms = num_sms();
+  for (int cw : {64, 96, 112})
+    if ((m + cw - 1) / cw <= sms) return cw;
+  return 128;
+}
+
+int launch_leaf_cols2(const LeafArgs& g, cudaStream_t s) {
+  switch (leaf_cols_width(g.m)) {
+    case 64: return launch_leaf_cols<2, 64>(g, s);
+    case 96: return launch_leaf_cols<2, 96>(g, s);
+    case 112: return launch_leaf_cols<2, 112>(g, s);
+    default: return launch_leaf_cols<2, 128>(g, s);
+  }
 }
 
 // Wide solve blocks: the widest of 128/64/32 right-hand sides whose block
@@ -242,7 +264,7 @@ int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m
     // the GPU: one right-hand side per thread, or two threads per right-hand
     // side (NLA_LEAF_COLS=0 selects the panel-parallel kernels instead).
     if (dtype == NLA_F64 && n <= COLS_MAX_N && m >= 8 * LEAF_THREADS && leaf_cols_mode() != 0)
-      return leaf_cols_mode() == 1 ? launch_leaf_cols<1>(g, s) : launch_leaf_cols<2>(g, s);
+      return leaf_cols_mode() == 1 ? launch_leaf_cols<1, LEAF_THREADS>(g, s) : launch_leaf_cols2(g, s);
     const int cw = wide_cols(n, m, dtype == NLA_F64 ? 8 : 4);
     if (cw) {
       switch (dtype) {

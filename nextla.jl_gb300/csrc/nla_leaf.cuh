@@ -345,10 +345,12 @@ __device__ __forceinline__ void solve_block_wide(const LeafArgs& g, int64_t c0, 
 }
 
 // Float64 solve with one right-hand side per thread, for n <= COLS_MAX_N and
-// LEAF_THREADS columns per CTA.  GB300 issues FP64 at two fused multiply-adds
-// per clock per SM: a warp instruction holds its sub-partition's FP64 unit for
-// 64 clocks.  The fastest schedule therefore keeps one warp per
-// sub-partition issuing independent FMAs and has no serial single-warp phase.
+// CW columns per CTA.  GB300 issues FP64 at two fused multiply-adds per clock
+// per SM, and measured time is proportional to the FP64 warp instructions an
+// SM issues, whichever sub-partitions issue them (8 warps of independent FMA
+// chains take 8/7 of the time of 7).  So a solve over m columns is fastest
+// with the fewest columns per CTA that still fit one CTA per SM: 112 for
+// m = 16384 (147 CTAs) instead of 128 (128 CTAs, 24 SMs idle).
 //
 // The kernel works left-looking over 32-row panels.  Each thread keeps its
 // panel's 32 values in registers, y, and does two steps:
@@ -366,16 +368,15 @@ constexpr int LOAD_BATCH = 16;  // loads in flight per thread (one CTA per SM)
 // split the already-solved rows of each panel's update, so that every SM
 // sub-partition has two warps issuing FMAs in that phase; half 1 hands its
 // partial sums over through shared memory and half 0 solves the triangle.
-__host__ __device__ constexpr size_t leaf_cols_smem_elems(int n, int halves) {
-  return (size_t)n * LEAF_THREADS + (size_t)PANEL * COLS_MAX_N + (size_t)n +
-         (halves > 1 ? (size_t)PANEL * LEAF_THREADS : 0);
+__host__ __device__ constexpr size_t leaf_cols_smem_elems(int n, int halves, int cw = LEAF_THREADS) {
+  return (size_t)n * cw + (size_t)PANEL * COLS_MAX_N + (size_t)n + (halves > 1 ? (size_t)PANEL * cw : 0);
 }
 
-template <int HALVES>
+template <int HALVES, int CW>
 __device__ __forceinline__ void solve_cols_f64(const LeafArgs& g, int64_t c0, int ncols, unsigned char* smem_raw,
                                                double alpha) {
-  constexpr int CW = LEAF_THREADS;            // right-hand sides per CTA
-  constexpr int NT = LEAF_THREADS * HALVES;   // threads per CTA
+  static_assert(CW % 16 == 0 && CW <= LEAF_THREADS, "right-hand sides per CTA");
+  constexpr int NT = CW * HALVES;  // threads per CTA
   const int n = g.n;
   double* X = reinterpret_cast<double*>(smem_raw);  // n x CW
   double* L = X + (size_t)n * CW;                   // PANEL x COLS_MAX_N: rows p0.., columns 0..

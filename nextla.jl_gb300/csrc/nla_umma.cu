@@ -343,15 +343,24 @@ __device__ __forceinline__ uint32_t shl_clamped(uint32_t a, uint32_t s) {
   return d;
 }
 
+#ifndef NLA_DRAIN_COLS
+#define NLA_DRAIN_COLS 16
+#endif
+constexpr int DRAIN_COLS = NLA_DRAIN_COLS;  // TMEM columns per load-and-wait
+__device__ __forceinline__ void drain_load(uint32_t ta, uint32_t* r) {
+  if constexpr (DRAIN_COLS == 32) umma::tmem_ld32(ta, r);
+  else umma::tmem_ld16(ta, r);
+}
+
 __device__ __forceinline__ void exact_drain(long long (&acc)[64], uint32_t ta, int sh) {
   if (__all_sync(0xffffffffu, sh >= 0)) {
     const uint32_t s_lo = (uint32_t)sh, s_hi = (uint32_t)max(sh - 32, 0);
 #pragma unroll
-    for (int j0 = 0; j0 < 64; j0 += 16) {
-      uint32_t r[16];
-      umma::tmem_ld16(ta + (uint32_t)j0, r);
+    for (int j0 = 0; j0 < 64; j0 += DRAIN_COLS) {
+      uint32_t r[DRAIN_COLS];
+      drain_load(ta + (uint32_t)j0, r);
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
+      for (int j = 0; j < DRAIN_COLS; ++j) {
         const int v = __float2int_rn(__uint_as_float(r[j]));
         const uint32_t lo = shl_clamped((uint32_t)v, s_lo);
         const uint32_t hi = __funnelshift_lc((uint32_t)v, (uint32_t)(v >> 31), s_lo) << s_hi;

@@ -240,6 +240,31 @@ def test_f64_leaf_one_rhs_per_thread_exact(pkg, cuda):
         np.testing.assert_array_equal(to_host(Bd), X.astype(np.float64))
 
 
+@pytest.mark.parametrize("cw", [64, 96, 112, 128])
+def test_f64_leaf_columns_per_cta(pkg, oracle, workloads, cuda, cw, monkeypatch):
+    """Every width of the one-right-hand-side-per-thread leaf (NLA_LEAF_CW
+    pins it; by default the fewest columns per CTA that fit one wave): exact
+    integer solves bit for bit, and a random system with a partial last CTA
+    against BLAS at the Float64 bound."""
+    import torch
+
+    monkeypatch.setenv("NLA_LEAF_CW", str(cw))
+    rng = np.random.default_rng(cw)
+    for n in (37, 128):
+        L = np.tril(rng.integers(-3, 4, (n, n)), -1).astype(np.int64)
+        L[np.diag_indices(n)] = 2 ** rng.integers(0, 3, n)
+        X = rng.integers(-8, 9, (n, 1100)).astype(np.int64)
+        Ad = to_dev(L.astype(np.float64), np.float64, cuda)
+        Bd = to_dev((L @ X).astype(np.float64), np.float64, cuda)
+        pkg.unified_rectrxm_("L", "L", "N", 1.0, "S", Ad, Bd, native=True)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(to_host(Bd), X.astype(np.float64))
+    for side, trans in itertools.product("LR", "NT"):
+        A, B = workloads.problem(128, 1237, side, "U", seed=cw)
+        X = _run(pkg, cuda, side, "U", trans, -1.5, "S", A, B, np.float64, True)
+        assert oracle.rel_err(X, oracle.blas_rectrxm(side, "U", trans, -1.5, "S", A, B)) < 1e-14, (cw, side, trans)
+
+
 @pytest.mark.parametrize("func", ["S", "M"])
 def test_trsm_trmm_wrappers_with_diag(pkg, oracle, workloads, cuda, func):
     """trsm()/trmm() (src/trsm.jl:186-204, src/trmm.jl:430-448) through the
