@@ -964,17 +964,13 @@ __device__ __forceinline__ long long fixed_of(double x, int ex) {
 // When nrm is not null, nrm[row] accumulates sum_k sum_p |s_p| 2^(-beta p),
 // which bounds every partial sum of slice products along that row (in units
 // of the row's scale 2^e) for a partner whose elements are below 1/2.
-template <typename T, typename Sl, int NS>
-__global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int64_t ld, int t, int64_t rows,
-                                                    int64_t cols, int tri, const int* __restrict__ e,
-                                                    Sl* __restrict__ out, int64_t rows_pad, int64_t cols_pad,
-                                                    float* __restrict__ nrm) {
-  constexpr int BETA = std::is_same<Sl, __nv_bfloat16>::value ? 8 : 11;
-  __shared__ double tile[32][65];
-  const int64_t i0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 64;
-  // All eight loads of a thread are issued before any is used (the kernel is
-  // bound by memory-level parallelism, not by its integer work).
-  double v[8];
+// Loads of one 32 x 64 tile (rows i0.., K k0..) of a rows x cols view: eight
+// per thread, all in flight before any is used (the staging kernels are bound
+// by memory-level parallelism, not by their integer work).  Zeros outside
+// the view and outside the staged triangle.
+template <typename T>
+__device__ __forceinline__ void load_tile(const T* __restrict__ X, int64_t ld, int t, int64_t rows, int64_t cols,
+                                          int tri, int64_t i0, int64_t k0, double (&v)[8]) {
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     const int idx = threadIdx.x + 256 * j;
@@ -983,6 +979,9 @@ __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int
     const int64_t gi = i0 + i, gk = k0 + k;
     v[j] = (gi < rows && gk < cols && in_tri(tri, gi, gk)) ? to_double(X[mat_off(gi, gk, ld, t)]) : 0.0;
   }
+}
+
+__device__ __forceinline__ void store_tile(double (*tile)[65], int t, const double (&v)[8]) {
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     const int idx = threadIdx.x + 256 * j;
@@ -990,19 +989,38 @@ __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int
     if (!t) { i = idx & 31; k = idx >> 5; } else { k = idx & 63; i = idx >> 6; }
     tile[i][k] = v[j];
   }
-  __syncthreads();
-  (void)rows_pad;
+}
+
+// Split the 32 x 64 tile in `tile` (rows i0.., K k0..) into NS K-major slices
+// of type Sl.  Layout: the slices of one 128-row tile are adjacent, row
+// (t * NS + sl) * 128 + r holding row t * 128 + r of slice sl, so that one
+// TMA box of 256 rows brings slices sl and sl + 1 of a tile.  The slices are
+// the integers s_p of
+//   x = 2^ex[row] * sum_p s_p 2^(-beta p),  beta = 8 (BF16) or 11 (FP16),
+// with |s_p| <= 2^(beta-1).  NS = 0 stages the element itself (a Float16
+// operand of the plain path).  The slice count and width are compile-time
+// constants, so every shift is an immediate; each thread produces two
+// adjacent K values and writes them with one 32-bit store per slice.  Warp w
+// handles rows w, w + 8, w + 16 and w + 24; mag[r] returns, for the r-th of
+// them, sum_k sum_p |s_p| 2^(-beta p) over the tile (on every lane).
+template <typename Sl, int NS>
+__device__ __forceinline__ void split_tile(const double (*tile)[65], int64_t i0, int64_t k0, int64_t rows,
+                                           const int* ex_rows, Sl* __restrict__ out, int64_t cols_pad,
+                                           float (&mag)[4]) {
+  constexpr int BETA = std::is_same<Sl, __nv_bfloat16>::value ? 8 : 11;
   constexpr int NSL = NS == 0 ? 1 : NS;
   // One row per warp and pass (idx >> 5 is warp-uniform), two K values per lane.
-  for (int idx = threadIdx.x; idx < 32 * 32; idx += 256) {
+#pragma unroll
+  for (int pass = 0; pass < 4; ++pass) {
+    const int idx = threadIdx.x + 256 * pass;
     const int i = idx >> 5, k = (idx & 31) * 2;
     const int64_t gi = i0 + i, gk = k0 + k;
     uint32_t* o = reinterpret_cast<uint32_t*>(out + ((gi >> 7) * NSL * 128 + (gi & 127)) * cols_pad + gk);
+    mag[pass] = 0.0f;
     if constexpr (NS == 0) {
       *o = pack2<Sl>((Sl)(float)tile[i][k], (Sl)(float)tile[i][k + 1]);
-      continue;
     } else {
-      const int ex = gi < rows ? e[gi] : SENTINEL_EXP;
+      const int ex = gi < rows ? ex_rows[i] : SENTINEL_EXP;
       // Balanced digits by bias: with Z = Y + sum_p 2^(beta-1) 2^(sigma_p)
       // + 2^(sigma_last - 1) and sigma_p = 62 - beta (p + 1), the digit
       // s_p = ((Z >> sigma_p) mod 2^beta) - 2^(beta-1) (the top digit keeps
@@ -1015,7 +1033,7 @@ __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int
         return b;
       }();
       const long long z0 = fixed_of(tile[i][k], ex) + BIAS, z1 = fixed_of(tile[i][k + 1], ex) + BIAS;
-      float mag = 0.0f;
+      float m = 0.0f;
 #pragma unroll
       for (int sl = 0; sl < NS; ++sl) {
         const int sigma = 62 - BETA * (sl + 1);
@@ -1029,13 +1047,134 @@ __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int
         const float f1 = __int_as_float(0x4B400000 + d1) - 12582912.0f;
         o[sl * (128 * cols_pad / 2)] = pack_slices<Sl>(f0, f1);
         // 2^(-beta (sl + 1)) built from its exponent bits (exact).
-        mag += (fabsf(f0) + fabsf(f1)) * __int_as_float((127 - BETA * (sl + 1)) << 23);
+        m += (fabsf(f0) + fabsf(f1)) * __int_as_float((127 - BETA * (sl + 1)) << 23);
       }
-      if (nrm) {
-        for (int off = 16; off > 0; off >>= 1) mag += __shfl_xor_sync(0xffffffffu, mag, off);
-        if ((threadIdx.x & 31) == 0 && gi < rows && mag > 0.0f) atomicAdd(&nrm[gi], mag);
-      }
+      for (int off = 16; off > 0; off >>= 1) m += __shfl_xor_sync(0xffffffffu, m, off);
+      mag[pass] = m;
     }
+  }
+}
+
+// Split a rows x cols view into NS K-major slices of type Sl (rows padded to
+// rows_pad, K padded to cols_pad, zeros in the padding and outside the staged
+// triangle), one 32 x 64 tile per CTA, with the row exponents e[] from
+// row_exp_kernel.  When nrm is not null, nrm[row] accumulates
+// sum_k sum_p |s_p| 2^(-beta p), which bounds every partial sum of slice
+// products along that row (in units of the row's scale 2^e) for a partner
+// whose elements are below 1/2.
+template <typename T, typename Sl, int NS>
+__global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int64_t ld, int t, int64_t rows,
+                                                    int64_t cols, int tri, const int* __restrict__ e,
+                                                    Sl* __restrict__ out, int64_t rows_pad, int64_t cols_pad,
+                                                    float* __restrict__ nrm) {
+  __shared__ double tile[32][65];
+  const int64_t i0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 64;
+  (void)rows_pad;
+  double v[8];
+  load_tile(X, ld, t, rows, cols, tri, i0, k0, v);
+  store_tile(tile, t, v);
+  __syncthreads();
+  float mag[4];
+  split_tile<Sl, NS>(tile, i0, k0, rows, e ? e + i0 : nullptr, out, cols_pad, mag);
+  if (NS != 0 && nrm && (threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int pass = 0; pass < 4; ++pass) {
+      const int64_t gi = i0 + (threadIdx.x >> 5) + 8 * pass;
+      if (gi < rows && mag[pass] > 0.0f) atomicAdd(&nrm[gi], mag[pass]);
+    }
+  }
+}
+
+// One operand of a fused staging launch.
+struct StageJob {
+  const double* X;
+  int64_t ld;
+  int t;
+  int64_t rows, cols;
+  int tri;
+  int* e;
+  void* out;
+  int64_t cols_pad;
+  float* nrm;
+  int blocks;  // 32-row blocks: rows_pad / 32
+};
+
+// Both operands of one update staged by one launch, for short K: a CTA takes
+// 32 rows of one operand, finds their exponents over the whole K range (the
+// same maximum row_exp_kernel takes), then splits them tile by tile as
+// split_kernel does (the second pass reads from L2), and writes e[] and
+// nrm[] itself, so no memsets, no atomics and one launch replace the eight
+// stream operations of two separately staged operands.
+template <typename Sl, int NS>
+__global__ void __launch_bounds__(256, 3) stage_pair_kernel(const StageJob a, const StageJob b) {
+  __shared__ double tile[2][32][65];
+  __shared__ int sred[8][32];
+  __shared__ int sexp[32];
+  const bool first = (int)blockIdx.x < a.blocks;
+  const StageJob j = first ? a : b;
+  const int64_t i0 = (int64_t)(first ? blockIdx.x : blockIdx.x - a.blocks) * 32;
+  const int64_t ktiles = j.cols_pad / 64;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  // Pass 1: row exponents.  With t = 0 a thread's eight values lie in row
+  // `lane`; with t = 1 in rows (threadIdx.x >> 6) + 4 q, q = 0..7.
+  int m[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) m[q] = SENTINEL_EXP;
+  for (int64_t kt = 0; kt < ktiles; ++kt) {
+    double v[8];
+    load_tile(j.X, j.ld, j.t, j.rows, j.cols, j.tri, i0, kt * 64, v);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int ex = exp_of(v[q]);  // zeros (and the padding) give SENTINEL_EXP
+      if (j.t) m[q] = max(m[q], ex);
+      else m[0] = max(m[0], ex);
+    }
+  }
+  if (!j.t) {
+    sred[warp][lane] = m[0];
+  } else {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int r = __reduce_max_sync(0xffffffffu, m[q]);
+      if (lane == 0) sred[warp][q] = r;  // rows (warp >> 1) + 4 q
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int r = threadIdx.x;
+    int mx = SENTINEL_EXP;
+    if (!j.t) {
+#pragma unroll
+      for (int w = 0; w < 8; ++w) mx = max(mx, sred[w][r]);
+    } else {
+      const int g = r & 3, q = r >> 2;  // row r = g + 4 q, read by warps 2g and 2g + 1
+      mx = max(sred[2 * g][q], sred[2 * g + 1][q]);
+    }
+    sexp[r] = mx;
+    if (i0 + r < j.rows) j.e[i0 + r] = mx;
+    else j.e[i0 + r] = SENTINEL_EXP;
+  }
+  __syncthreads();
+
+  // Pass 2: the split, two tile buffers so that one barrier per tile orders
+  // both the tile's writes before its reads and the previous reads before
+  // the next writes.
+  float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  Sl* out = static_cast<Sl*>(j.out);
+  for (int64_t kt = 0; kt < ktiles; ++kt) {
+    double v[8];
+    load_tile(j.X, j.ld, j.t, j.rows, j.cols, j.tri, i0, kt * 64, v);
+    store_tile(tile[kt & 1], j.t, v);
+    __syncthreads();
+    float mag[4];
+    split_tile<Sl, NS>(tile[kt & 1], i0, kt * 64, j.rows, sexp, out, j.cols_pad, mag);
+#pragma unroll
+    for (int pass = 0; pass < 4; ++pass) acc[pass] += mag[pass];
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int pass = 0; pass < 4; ++pass) j.nrm[i0 + warp + 8 * pass] = i0 + warp + 8 * pass < j.rows ? acc[pass] : 0.0f;
   }
 }
 
@@ -1217,12 +1356,8 @@ size_t staged_bytes(int64_t rows, int64_t K, int S) {
   return b;
 }
 
-int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bool bf16, int tri, void* buf,
-                  Staged* out, cudaStream_t s) {
-  const bool copy = in_dtype == NLA_F16;
-  const int beta = bf16 ? 8 : 11;
-  if (copy) S = 1;
-  if (S < 1 || 62 - beta * S < 1) return fail(NLA_ERR_ARG, "too many slices for the slice width");
+// The layout of a staged operand in `buf` (see staged_bytes).
+void staged_layout(void* buf, int64_t rows, int64_t K, int S, bool bf16, bool copy, int tri, Staged* out) {
   const int64_t Rp = pad_to(rows, BM), Kp = pad_to(K, BK);
   uint8_t* w = static_cast<uint8_t*>(buf);
   out->slices = w;
@@ -1237,6 +1372,16 @@ int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bo
   out->bf16 = copy ? false : bf16;
   out->tri = tri;
   out->scaled = !copy;
+}
+
+int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bool bf16, int tri, void* buf,
+                  Staged* out, cudaStream_t s) {
+  const bool copy = in_dtype == NLA_F16;
+  const int beta = bf16 ? 8 : 11;
+  if (copy) S = 1;
+  if (S < 1 || 62 - beta * S < 1) return fail(NLA_ERR_ARG, "too many slices for the slice width");
+  const int64_t Rp = pad_to(rows, BM), Kp = pad_to(K, BK);
+  staged_layout(buf, rows, K, S, bf16, copy, tri, out);
   TraceScope trace(NLA_K_SPLIT, s, 0.0,
                    (double)rows * (double)K * (double)dtype_size(in_dtype) * (copy ? 1 : 2) + (double)S * Rp * Kp * 2);
   const dim3 gs((unsigned)(Rp / 32), (unsigned)(Kp / 64));
@@ -1274,6 +1419,59 @@ int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bo
   return NLA_OK;
 }
 
+// Fused staging of both operands of one Float64 update (stage_pair_kernel)
+// for K up to FUSED_STAGE_MAX_K; NLA_STAGE_FUSED=0 turns it off (read per
+// update, so that tests can compare both paths in one process).
+constexpr int64_t FUSED_STAGE_MAX_K = 256;  // measured: slower than the separate kernels from K = 512
+bool stage_fused_enabled() {
+  const char* v = getenv("NLA_STAGE_FUSED");
+  return !(v && v[0] == '0');
+}
+
+int stage_pair(const Mat& A, int64_t M, const Mat& Bt, int64_t N, int64_t K, int S, bool bf16, void* bufA,
+               void* bufB, Staged* As, Staged* Bs, cudaStream_t s) {
+  staged_layout(bufA, M, K, S, bf16, false, 0, As);
+  staged_layout(bufB, N, K, S, bf16, false, 0, Bs);
+  auto job = [](const Mat& X, const Staged& st) {
+    StageJob j{};
+    j.X = static_cast<const double*>(X.p);
+    j.ld = X.ld;
+    j.t = X.t;
+    j.rows = st.rows;
+    j.cols = st.K;
+    j.tri = 0;
+    j.e = st.e;
+    j.out = st.slices;
+    j.cols_pad = st.K_pad;
+    j.nrm = st.nrm;
+    j.blocks = (int)(st.rows_pad / 32);
+    return j;
+  };
+  const StageJob ja = job(A, *As), jb = job(Bt, *Bs);
+  const int64_t grid = (int64_t)ja.blocks + jb.blocks;
+  if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "operand too large");
+  TraceScope trace(NLA_K_SPLIT, s, 0.0,
+                   (double)(M + N) * (double)K * 16.0 + (double)S * (As->rows_pad + Bs->rows_pad) * As->K_pad * 2);
+  if (bf16) {
+    switch (S) {
+      case 1: stage_pair_kernel<__nv_bfloat16, 1><<<(unsigned)grid, 256, 0, s>>>(ja, jb); break;
+      case 2: stage_pair_kernel<__nv_bfloat16, 2><<<(unsigned)grid, 256, 0, s>>>(ja, jb); break;
+      case 3: stage_pair_kernel<__nv_bfloat16, 3><<<(unsigned)grid, 256, 0, s>>>(ja, jb); break;
+      case EXACT_SLICES: stage_pair_kernel<__nv_bfloat16, EXACT_SLICES><<<(unsigned)grid, 256, 0, s>>>(ja, jb); break;
+      default: return fail(NLA_ERR_ARG, "BF16 slices: 1, 2, 3 or 7 terms");
+    }
+  } else {
+    switch (S) {
+      case 1: stage_pair_kernel<__half, 1><<<(unsigned)grid, 256, 0, s>>>(ja, jb); break;
+      case 2: stage_pair_kernel<__half, 2><<<(unsigned)grid, 256, 0, s>>>(ja, jb); break;
+      case 3: stage_pair_kernel<__half, 3><<<(unsigned)grid, 256, 0, s>>>(ja, jb); break;
+      default: return fail(NLA_ERR_ARG, "FP16 slices: 1, 2 or 3 terms");
+    }
+  }
+  NLA_CHECK_LAUNCH("stage_pair_kernel");
+  return NLA_OK;
+}
+
 size_t sliced_workspace_bytes(int64_t M, int64_t N, int64_t K, int S) {
   return staged_bytes(M, K, S) + staged_bytes(N, K, S) + 1024;
 }
@@ -1298,8 +1496,12 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
       return fail(NLA_ERR_WORKSPACE, "workspace too small for the exact update");
     }
     Staged As, Bs;
-    NLA_TRY(stage_operand(A, M, K, NLA_F64, S, true, 0, base, &As, s));
-    NLA_TRY(stage_operand(transposed(B), N, K, NLA_F64, S, true, 0, static_cast<uint8_t*>(base) + sa, &Bs, s));
+    if (K <= FUSED_STAGE_MAX_K && stage_fused_enabled()) {
+      NLA_TRY(stage_pair(A, M, transposed(B), N, K, S, true, base, static_cast<uint8_t*>(base) + sa, &As, &Bs, s));
+    } else {
+      NLA_TRY(stage_operand(A, M, K, NLA_F64, S, true, 0, base, &As, s));
+      NLA_TRY(stage_operand(transposed(B), N, K, NLA_F64, S, true, 0, static_cast<uint8_t*>(base) + sa, &Bs, s));
+    }
     return launch_exact_gemm(As, Bs, alpha, C, false, s);
   }
   if (S < 1 || S > 3) return fail(NLA_ERR_ARG, "split terms must be 1, 2, 3 or 7");
@@ -1314,10 +1516,15 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
     return fail(NLA_ERR_WORKSPACE, "workspace too small for the tensor-core update");
   }
   Staged As, Bs;
-  NLA_TRY(stage_operand(A, M, K, in_dtype, S, bf16, 0, base, &As, s));
   // N x K view: row j is column j of op(B)
-  NLA_TRY(stage_operand(transposed(B), N, K, in_dtype, S, bf16, 0, static_cast<uint8_t*>(base) + staged_bytes(M, K, S),
-                        &Bs, s));
+  if (!copy && K <= FUSED_STAGE_MAX_K && stage_fused_enabled()) {
+    NLA_TRY(stage_pair(A, M, transposed(B), N, K, S, bf16, base, static_cast<uint8_t*>(base) + staged_bytes(M, K, S),
+                       &As, &Bs, s));
+  } else {
+    NLA_TRY(stage_operand(A, M, K, in_dtype, S, bf16, 0, base, &As, s));
+    NLA_TRY(stage_operand(transposed(B), N, K, in_dtype, S, bf16, 0,
+                          static_cast<uint8_t*>(base) + staged_bytes(M, K, S), &Bs, s));
+  }
 
   const bool use_bf16 = As.bf16;
   CUtensorMap mA, mB;

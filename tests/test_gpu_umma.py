@@ -134,3 +134,40 @@ def test_exact_update_bit_exact_on_integers(pkg, cuda):
     pkg.matmul_mixed_(C, A, B, 1.0, split_terms=7)
     pkg.device_status(C)
     assert torch.equal(C, ref)
+
+
+@pytest.mark.parametrize("terms", [7, 3])
+def test_fused_staging_matches_separate(pkg, cuda, terms, monkeypatch):
+    """Updates with K <= 256 stage both operands in one launch
+    (stage_pair_kernel).  Its slices and row exponents equal those of the
+    separate exponent scan and split; the row bounds differ at most in the
+    order of a float sum.  So the updates agree bit for bit on the fast path,
+    and on the exact path to the last bit (the fixed point's scale can shift
+    when a row bound sits at a power of two).  Both operand layouts, ragged
+    sizes, K from one 64-wide tile to 256 (and 1024, staged separately both
+    times), a zero row and a zero column."""
+    import torch
+
+    g = torch.Generator(device=cuda).manual_seed(17)
+    shapes = [(129, 64, 300), (257, 100, 64), (200, 256, 130), (131, 1024, 70)]
+    for (N, R, M), t1, t2 in itertools.product(shapes, [False, True], [False, True]):
+        A = torch.randn(R if t1 else N, N if t1 else R, device=cuda, generator=g, dtype=torch.float64)
+        B = torch.randn(M if t2 else R, R if t2 else M, device=cuda, generator=g, dtype=torch.float64)
+        A = _col_major(A)
+        B = _col_major(B)
+        opA, opB = (A.T if t1 else A), (B.T if t2 else B)
+        opA[3].zero_()
+        opB[:, 5].zero_()
+        C0 = _col_major(torch.randn(N, M, device=cuda, generator=g, dtype=torch.float64))
+        out = []
+        for fused in ("1", "0"):
+            monkeypatch.setenv("NLA_STAGE_FUSED", fused)
+            C = C0.clone().T.contiguous().T
+            pkg.matmul_mixed_(C, opA, opB, -1.0, split_terms=terms)
+            pkg.device_status(C)
+            out.append(C)
+        if terms == 3:
+            assert torch.equal(out[0], out[1]), (N, R, M, t1, t2)
+        else:
+            scale = (opA.abs() @ opB.abs()).clamp_min(1e-300)
+            assert ((out[0] - out[1]).abs() / scale).max().item() < 1e-15, (N, R, M, t1, t2)
