@@ -292,6 +292,7 @@ struct ExactParams {
   double alpha;
   const int* ea;
   const int* eb;
+  int merged;  // coupled kernel: short-K group table (pairs of one weight share an accumulator)
 };
 
 // K range of the staged triangle that meets rows [r0, r0 + span).
@@ -656,22 +657,61 @@ constexpr int CP_DYN_SMEM = CP_STAGES * CP_STAGE_BYTES + 1024 + 256;
 constexpr int CP_GROUPS = 16;
 static_assert(CP_DYN_SMEM + 16 <= 232448, "coupled exact kernel shared memory above the per-block limit");
 
-// Group g -> (p, q, coupled): q-major, p = 0, 2, 4, ... (a coupled group
-// also takes p + 1, while p + 1 <= 6 - q).  Packed as p | q << 4 | coupled << 8.
-__constant__ uint16_t c_cp_groups[CP_GROUPS] = {
-    0x100, 0x102, 0x104, 0x006,   // q = 0: (0,1) (2,3) (4,5) (6)
-    0x110, 0x112, 0x114,          // q = 1: (0,1) (2,3) (4,5)
-    0x120, 0x122, 0x024,          // q = 2: (0,1) (2,3) (4)
-    0x130, 0x132,                 // q = 3: (0,1) (2,3)
-    0x140, 0x042,                 // q = 4: (0,1) (2)
-    0x150,                        // q = 5: (0,1)
-    0x060};                       // q = 6: (0)
+// Group tables.  A group is drained as one or two accumulators (d0, d1) of
+// weights w0, w1; it is filled by segments, each one K loop of one slice
+// pair (p, q) into d0 or d1, or of the coupled pairs (p, q) -> d0 and
+// (p + 1, q) -> d1 that share the B_q tile.  A segment's init bits mark the
+// first write into each accumulator (its MMAs start with enable_input_d 0).
+//   segment: p | q << 4 | coupled << 8 | dst << 9 | init0 << 10 | init1 << 11
+//   group:   first segment | segment count << 8 | w0 << 12 | w1 << 16 (15: no d1)
+constexpr uint16_t cp_seg(int p, int q, int two, int dst, int i0, int i1) {
+  return (uint16_t)(p | q << 4 | two << 8 | dst << 9 | i0 << 10 | i1 << 11);
+}
+constexpr uint32_t cp_grp(int first, int count, int w0, int w1) {
+  return (uint32_t)(first | count << 8 | w0 << 12 | w1 << 16);
+}
+constexpr int CP_MERGED_MAX_K = 256;  // 4 pairs x 256 products of at most 2^14: 2^24
+constexpr int CP_GROUPS_MERGED = 5;
+__constant__ uint16_t c_cp_segs[CP_GROUPS + 19] = {
+    // Default: 16 groups of one segment, q-major, p = 0, 2, 4, ... (a
+    // coupled segment also takes p + 1 while p + 1 <= 6 - q).
+    cp_seg(0, 0, 1, 0, 1, 1), cp_seg(2, 0, 1, 0, 1, 1), cp_seg(4, 0, 1, 0, 1, 1), cp_seg(6, 0, 0, 0, 1, 0),
+    cp_seg(0, 1, 1, 0, 1, 1), cp_seg(2, 1, 1, 0, 1, 1), cp_seg(4, 1, 1, 0, 1, 1),
+    cp_seg(0, 2, 1, 0, 1, 1), cp_seg(2, 2, 1, 0, 1, 1), cp_seg(4, 2, 0, 0, 1, 0),
+    cp_seg(0, 3, 1, 0, 1, 1), cp_seg(2, 3, 1, 0, 1, 1),
+    cp_seg(0, 4, 1, 0, 1, 1), cp_seg(2, 4, 0, 0, 1, 0),
+    cp_seg(0, 5, 1, 0, 1, 1),
+    cp_seg(0, 6, 0, 0, 1, 0),
+    // Short K (at most CP_MERGED_MAX_K): the pairs of one weight share an
+    // accumulator, at most 4 pairs each, so 5 groups (9 drains) replace 16
+    // groups (28 drains) with the same 28 pair products.
+    cp_seg(0, 0, 1, 0, 1, 1), cp_seg(0, 1, 0, 1, 0, 0),                              // w 0 | 1
+    cp_seg(0, 2, 1, 0, 1, 1), cp_seg(1, 1, 1, 0, 0, 0), cp_seg(2, 0, 1, 0, 0, 0),
+    cp_seg(0, 3, 0, 1, 0, 0),                                                         // w 2 | 3
+    cp_seg(0, 4, 1, 0, 1, 1), cp_seg(1, 3, 1, 0, 0, 0), cp_seg(2, 2, 1, 0, 0, 0),   // w 4 | 5
+    cp_seg(3, 1, 1, 0, 1, 1), cp_seg(4, 0, 1, 0, 0, 0), cp_seg(0, 5, 0, 1, 0, 0),   // w 4 | 5
+    cp_seg(0, 6, 0, 0, 1, 0), cp_seg(1, 5, 0, 0, 0, 0), cp_seg(2, 4, 0, 0, 0, 0), cp_seg(3, 3, 0, 0, 0, 0),
+    cp_seg(4, 2, 0, 1, 0, 1), cp_seg(5, 1, 0, 1, 0, 0), cp_seg(6, 0, 0, 1, 0, 0)};  // w 6 | 6
+__constant__ uint32_t c_cp_grps[CP_GROUPS + CP_GROUPS_MERGED] = {
+    cp_grp(0, 1, 0, 1),   cp_grp(1, 1, 2, 3),   cp_grp(2, 1, 4, 5),   cp_grp(3, 1, 6, 15),
+    cp_grp(4, 1, 1, 2),   cp_grp(5, 1, 3, 4),   cp_grp(6, 1, 5, 6),
+    cp_grp(7, 1, 2, 3),   cp_grp(8, 1, 4, 5),   cp_grp(9, 1, 6, 15),
+    cp_grp(10, 1, 3, 4),  cp_grp(11, 1, 5, 6),
+    cp_grp(12, 1, 4, 5),  cp_grp(13, 1, 6, 15),
+    cp_grp(14, 1, 5, 6),
+    cp_grp(15, 1, 6, 15),
+    cp_grp(16, 2, 0, 1),  cp_grp(18, 4, 2, 3),  cp_grp(22, 3, 4, 5),  cp_grp(25, 3, 4, 5),
+    cp_grp(28, 7, 6, 6)};
 
-__device__ __forceinline__ void cp_group(int g, int& pa, int& qb, bool& two) {
-  const int v = c_cp_groups[g];
-  pa = v & 15;
-  qb = (v >> 4) & 15;
-  two = (v >> 8) & 1;
+struct CpSeg {
+  int p, q;
+  bool two, init0, init1;
+  int dst;
+};
+__device__ __forceinline__ CpSeg cp_seg_at(int i) {
+  const int v = c_cp_segs[i];
+  return CpSeg{v & 15, (v >> 4) & 15, ((v >> 8) & 1) != 0, ((v >> 10) & 1) != 0, ((v >> 11) & 1) != 0,
+               (v >> 9) & 1};
 }
 
 __global__ void __launch_bounds__(EX_THREADS, 1)
@@ -722,6 +762,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   const uint32_t tmem = *tmem_slot;
   bool ok = true;
 
+  const int g0 = p.merged ? CP_GROUPS : 0, g1 = p.merged ? CP_GROUPS + CP_GROUPS_MERGED : CP_GROUPS;
   if (warp == 0 || warp == 2) {
     const bool is_a = warp == 0;
     if (lane == 0) {
@@ -729,27 +770,29 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
       for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
         const int c0 = max(kb0, cc * EX_CHUNK), c1 = min(kb1, (cc + 1) * EX_CHUNK);
         if (c0 >= c1) continue;
-        for (int g = 0; g < CP_GROUPS && ok; ++g) {
-          int pa, qb;
-          bool two;
-          cp_group(g, pa, qb, two);
-          for (int kb = c0; kb < c1; ++kb, ++it) {
-            const int s = it % CP_STAGES;
-            const uint32_t round = (uint32_t)(it / CP_STAGES);
-            if (!umma::mbar_wait(umma::smem_u32(&empty[s]), (round & 1u) ^ 1u, &s_abort, &g_device_error, 31)) {
-              ok = false;
-              break;
-            }
-            const uint32_t fb = umma::smem_u32(&full[s]);
-            uint8_t* st = smem + s * CP_STAGE_BYTES;
-            // Staged rows: slice sl of the tile at row r0 starts at r0 * 7 + sl * 128,
-            // so A_p and A_p+1 are one 256-row box.
-            if (is_a) {
-              umma::mbar_arrive_expect_tx(fb, (uint32_t)((two ? 2 : 1) * TILE_BYTES));
-              umma::tma_load_2d(umma::smem_u32(st), two ? &tmA2 : &tmA, fb, kb * BK, m0 * EX_SLICES + pa * BM);
-            } else {
-              umma::mbar_arrive_expect_tx(fb, (uint32_t)TILE_BYTES);
-              umma::tma_load_2d(umma::smem_u32(st + 2 * TILE_BYTES), &tmB, fb, kb * BK, n0 * EX_SLICES + qb * BN);
+        for (int g = g0; g < g1 && ok; ++g) {
+          const uint32_t gv = c_cp_grps[g];
+          const int s0 = gv & 255, ns = (gv >> 8) & 15;
+          for (int si = s0; si < s0 + ns && ok; ++si) {
+            const CpSeg sg = cp_seg_at(si);
+            for (int kb = c0; kb < c1; ++kb, ++it) {
+              const int s = it % CP_STAGES;
+              const uint32_t round = (uint32_t)(it / CP_STAGES);
+              if (!umma::mbar_wait(umma::smem_u32(&empty[s]), (round & 1u) ^ 1u, &s_abort, &g_device_error, 31)) {
+                ok = false;
+                break;
+              }
+              const uint32_t fb = umma::smem_u32(&full[s]);
+              uint8_t* st = smem + s * CP_STAGE_BYTES;
+              // Staged rows: slice sl of the tile at row r0 starts at r0 * 7 + sl * 128,
+              // so A_p and A_p+1 are one 256-row box.
+              if (is_a) {
+                umma::mbar_arrive_expect_tx(fb, (uint32_t)((sg.two ? 2 : 1) * TILE_BYTES));
+                umma::tma_load_2d(umma::smem_u32(st), sg.two ? &tmA2 : &tmA, fb, kb * BK, m0 * EX_SLICES + sg.p * BM);
+              } else {
+                umma::mbar_arrive_expect_tx(fb, (uint32_t)TILE_BYTES);
+                umma::tma_load_2d(umma::smem_u32(st + 2 * TILE_BYTES), &tmB, fb, kb * BK, n0 * EX_SLICES + sg.q * BN);
+              }
             }
           }
         }
@@ -762,10 +805,9 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
       for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
         const int c0 = max(kb0, cc * EX_CHUNK), c1 = min(kb1, (cc + 1) * EX_CHUNK);
         if (c0 >= c1) continue;
-        for (int g = 0; g < CP_GROUPS && ok; ++g, ++ch) {
-          int pa, qb;
-          bool two;
-          cp_group(g, pa, qb, two);
+        for (int g = g0; g < g1 && ok; ++g, ++ch) {
+          const uint32_t gv = c_cp_grps[g];
+          const int s0 = gv & 255, ns = (gv >> 8) & 15;
           const int b = ch & 1;
           if (!umma::mbar_wait(umma::smem_u32(&cempty[b]), ((uint32_t)(ch >> 1) & 1u) ^ 1u, &s_abort,
                                &g_device_error, 32)) {
@@ -774,27 +816,35 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
           }
           umma::fence_after_sync();
           const uint32_t d0 = tmem + (uint32_t)(b * 2 * BN), d1 = d0 + (uint32_t)BN;
-          for (int kb = c0; kb < c1; ++kb, ++it) {
-            const int s = it % CP_STAGES;
-            if (!umma::mbar_wait(umma::smem_u32(&full[s]), (uint32_t)(it / CP_STAGES) & 1u, &s_abort,
-                                 &g_device_error, 33)) {
-              ok = false;
-              break;
-            }
-            umma::fence_after_sync();
-            const uint32_t a0 = umma::smem_u32(smem + s * CP_STAGE_BYTES);
-            const uint32_t a1 = a0 + TILE_BYTES, b0 = a0 + 2 * TILE_BYTES;
-#pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk)
-              umma::mma_f16(d0, umma::desc_kmajor_sw128(a0 + kk * 32), umma::desc_kmajor_sw128(b0 + kk * 32), idesc,
-                            (kb > c0 || kk > 0) ? 1u : 0u);
-            if (two) {
+          for (int si = s0; si < s0 + ns && ok; ++si) {
+            const CpSeg sg = cp_seg_at(si);
+            // The first MMA of a segment starts an accumulator the segment
+            // initialises and adds to one an earlier segment started.
+            const uint32_t first0 = sg.two ? (sg.init0 ? 0u : 1u) : (sg.dst ? (sg.init1 ? 0u : 1u) : (sg.init0 ? 0u : 1u));
+            const uint32_t first1 = sg.init1 ? 0u : 1u;
+            const uint32_t dA = sg.two ? d0 : (sg.dst ? d1 : d0);
+            for (int kb = c0; kb < c1; ++kb, ++it) {
+              const int s = it % CP_STAGES;
+              if (!umma::mbar_wait(umma::smem_u32(&full[s]), (uint32_t)(it / CP_STAGES) & 1u, &s_abort,
+                                   &g_device_error, 33)) {
+                ok = false;
+                break;
+              }
+              umma::fence_after_sync();
+              const uint32_t a0 = umma::smem_u32(smem + s * CP_STAGE_BYTES);
+              const uint32_t a1 = a0 + TILE_BYTES, b0 = a0 + 2 * TILE_BYTES;
 #pragma unroll
               for (int kk = 0; kk < BK / 16; ++kk)
-                umma::mma_f16(d1, umma::desc_kmajor_sw128(a1 + kk * 32), umma::desc_kmajor_sw128(b0 + kk * 32),
-                              idesc, (kb > c0 || kk > 0) ? 1u : 0u);
+                umma::mma_f16(dA, umma::desc_kmajor_sw128(a0 + kk * 32), umma::desc_kmajor_sw128(b0 + kk * 32), idesc,
+                              (kb > c0 || kk > 0) ? 1u : first0);
+              if (sg.two) {
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; ++kk)
+                  umma::mma_f16(d1, umma::desc_kmajor_sw128(a1 + kk * 32), umma::desc_kmajor_sw128(b0 + kk * 32),
+                                idesc, (kb > c0 || kk > 0) ? 1u : first1);
+              }
+              umma::mma_commit(umma::smem_u32(&empty[s]));
             }
-            umma::mma_commit(umma::smem_u32(&empty[s]));
           }
           if (ok) umma::mma_commit(umma::smem_u32(&cfull[b]));
         }
@@ -813,18 +863,17 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     int ch = 0;
     for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
       if (max(kb0, cc * EX_CHUNK) >= min(kb1, (cc + 1) * EX_CHUNK)) continue;
-      for (int g = 0; g < CP_GROUPS && ok; ++g, ++ch) {
-        int pa, qb;
-        bool two;
-        cp_group(g, pa, qb, two);
+      for (int g = g0; g < g1 && ok; ++g, ++ch) {
+        const uint32_t gv = c_cp_grps[g];
+        const int w0 = (gv >> 12) & 15, w1 = (gv >> 16) & 15;
         const int b = ch & 1;
         ok = __all_sync(0xffffffffu, umma::mbar_wait(umma::smem_u32(&cfull[b]), (uint32_t)(ch >> 1) & 1u, &s_abort,
                                                      &g_device_error, 35));
         if (!ok) break;
         umma::fence_after_sync();
         const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * 2 * BN + h * 64);
-        exact_drain(acc, ta, Lb - 8 * (pa + qb + 2));
-        if (two) exact_drain(acc, ta + (uint32_t)BN, Lb - 8 * (pa + 1 + qb + 2));
+        exact_drain(acc, ta, Lb - 8 * (w0 + 2));
+        if (w1 != 15) exact_drain(acc, ta + (uint32_t)BN, Lb - 8 * (w1 + 2));
         umma::fence_before_sync();
         __syncwarp();
         if (lane == 0) umma::mbar_arrive(umma::smem_u32(&cempty[b]));
@@ -1280,7 +1329,16 @@ bool exact_coupled() {
   return on;
 }
 
-int launch_exact_coupled(const ExactParams& p, const Staged& A, const Staged& B, cudaStream_t s) {
+// Short-K group table of the coupled kernel (NLA_EXACT_MERGED=0 turns it
+// off; read per launch, so that tests can compare both tables).
+bool exact_merged_enabled() {
+  const char* v = getenv("NLA_EXACT_MERGED");
+  return !(v && v[0] == '0');
+}
+
+int launch_exact_coupled(const ExactParams& params, const Staged& A, const Staged& B, cudaStream_t s) {
+  ExactParams p = params;
+  p.merged = A.K_pad <= CP_MERGED_MAX_K && exact_merged_enabled() ? 1 : 0;
   CUtensorMap mA, mA2, mB;
   NLA_TRY(make_map(&mA, A.slices, true, (uint64_t)A.K_pad, (uint64_t)(EX_SLICES * A.rows_pad)));
   NLA_TRY(make_map(&mA2, A.slices, true, (uint64_t)A.K_pad, (uint64_t)(EX_SLICES * A.rows_pad), 2 * BM));

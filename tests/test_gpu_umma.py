@@ -171,3 +171,40 @@ def test_fused_staging_matches_separate(pkg, cuda, terms, monkeypatch):
         else:
             scale = (opA.abs() @ opB.abs()).clamp_min(1e-300)
             assert ((out[0] - out[1]).abs() / scale).max().item() < 1e-15, (N, R, M, t1, t2)
+
+
+def test_exact_short_k_group_table(pkg, cuda, monkeypatch):
+    """Updates with K <= 256 use the coupled kernel's short-K table: the pairs
+    of one weight share a TMEM accumulator (at most 4 pairs x 256 products
+    of at most 2^14 stay exact in FP32).  Integers come out bit for bit;
+    random data is FP64-accurate and agrees with the 16-group table to the
+    last bit of the fixed point (the tables round the low-weight chunks at
+    different points)."""
+    import torch
+
+    g = torch.Generator(device=cuda).manual_seed(23)
+    for N, R, M in [(200, 256, 130), (130, 64, 300), (129, 100, 129)]:
+        A = _col_major(torch.randint(-3000, 3001, (N, R), device=cuda, generator=g).double())
+        B = _col_major(torch.randint(-3000, 3001, (R, M), device=cuda, generator=g).double())
+        C = _col_major(torch.randint(-10, 11, (N, M), device=cuda, generator=g).double())
+        ref = C + A @ B
+        pkg.matmul_mixed_(C, A, B, 1.0, split_terms=7)
+        pkg.device_status(C)
+        assert torch.equal(C, ref), (N, R, M)
+    for (N, R, M), t1 in itertools.product([(256, 256, 200), (300, 128, 140), (140, 64, 256)], [False, True]):
+        A = torch.randn(R if t1 else N, N if t1 else R, device=cuda, generator=g, dtype=torch.float64)
+        A = _col_major(A * torch.exp(torch.randn(A.shape[0], 1, device=cuda, generator=g, dtype=torch.float64)))
+        B = _col_major(torch.randn(R, M, device=cuda, generator=g, dtype=torch.float64))
+        opA = A.T if t1 else A
+        C0 = _col_major(torch.randn(N, M, device=cuda, generator=g, dtype=torch.float64))
+        out = []
+        for merged in ("1", "0"):
+            monkeypatch.setenv("NLA_EXACT_MERGED", merged)
+            C = C0.clone().T.contiguous().T
+            pkg.matmul_mixed_(C, opA, B, -1.0, split_terms=7)
+            pkg.device_status(C)
+            out.append(C)
+        scale = opA.abs() @ B.abs()
+        err = ((out[0] - (C0 - opA @ B)).abs() / scale).max().item()
+        assert err < 1e-14, (N, R, M, t1, err)
+        assert ((out[0] - out[1]).abs() / scale).max().item() < 1e-15, (N, R, M, t1)
