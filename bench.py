@@ -761,7 +761,7 @@ def main():
     e2e_s = statistics.median(e2e_times)
     e2e_value = world * flops / e2e_s / 1e12
     host_levels = args.host_levels if args.host_levels > 0 else int(os.environ.get("NLA_HOST_LEVELS", "3"))
-    host_cutoff = args.cutoff if args.cutoff > 0 else (128 if args.variant == "mixed" else 256)
+    host_cutoff = args.cutoff if args.cutoff > 0 else (64 if args.variant == "mixed" else 256)
     # The host-buffer result against the device-resident solve of the timed loop.
     e2e_same = bool(torch.equal(X_pin, B.T.cpu()))
     # The same with copy-in, solve and copy-out one after another, and one

@@ -131,7 +131,7 @@ NLA_API int nla_scale(int dtype, int64_t rows, int64_t cols, double alpha, void*
  * tcgen05 tensor cores.  Each update operand is split into `split_terms`
  * BF16 (lowp NLA_LOWP_BF16) or FP16 (NLA_LOWP_F16) slices with one
  * power-of-two scale per row / column, slice products accumulate in FP32, and
- * the diagonal blocks (size `cutoff`, default 128) are solved or multiplied in
+ * the diagonal blocks (size `cutoff`, default 64) are solved or multiplied in
  * FP64.  Solves then run `sweeps` refinement sweeps: R = alpha*B - op(A) X with
  * an FP64-accurate residual product (`residual`), op(A) D = R with the same
  * mixed solver, X += D.  If corr_out is not

@@ -154,8 +154,10 @@ struct ResidualTerm {
 // operands staged with 7 BF16 slices.  With trans_out the product is added
 // to C^T (C is N x M).  With res, the epilogue instead forms a residual
 // (alpha is then -1 implicitly), rounding once.
+// fixed_buf (A.rows_pad x N int64, or null) lets a plain update leave its
+// fixed-point sums there for a separate finishing pass over C.
 int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat& C, bool trans_out,
-                      cudaStream_t s, const ResidualTerm* res = nullptr);
+                      cudaStream_t s, const ResidualTerm* res = nullptr, long long* fixed_buf = nullptr);
 constexpr int EXACT_SLICES = 7;
 int workspace_get(cudaStream_t s, size_t bytes, void** out);
 int device_status(cudaStream_t s);

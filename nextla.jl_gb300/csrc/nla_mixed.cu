@@ -147,13 +147,18 @@ unsigned grid_for(int64_t total) {
   return (unsigned)(blocks < cap ? (blocks > 0 ? blocks : 1) : cap);
 }
 
+// FP64 diagonal blocks of the mixed recursion: 64 rows.  The FP64 leaf is
+// bound by GB300's FP64 pipe (2 FMA per clock per SM), so halving it from 128
+// moves half of its work onto the tensor cores as one more level of short
+// exact updates; with the fused staging, the short-K group table and the
+// finishing pass those cost less than the leaf time they save.
 int default_mixed_cutoff() {
   const char* v = std::getenv("NLA_MIXED_CUTOFF");
   if (v && *v) {
     long x = std::atol(v);
     if (x > 0) return (int)(x > 1024 ? 1024 : x);
   }
-  return 128;
+  return 64;
 }
 
 }  // namespace

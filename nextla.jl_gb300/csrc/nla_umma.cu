@@ -293,6 +293,10 @@ struct ExactParams {
   const int* ea;
   const int* eb;
   int merged;  // coupled kernel: short-K group table (pairs of one weight share an accumulator)
+  // When set, the kernel writes its fixed-point sums to P (element (i, j) at
+  // P[i + j * ldp]) and exact_finish_kernel applies them to C.
+  long long* P;
+  int64_t ldp;
 };
 
 // K range of the staged triangle that meets rows [r0, r0 + span).
@@ -387,6 +391,58 @@ __device__ __forceinline__ void exact_drain(long long (&acc)[64], uint32_t ta, i
         const long long v = (long long)__float2int_rn(__uint_as_float(r[j]));
         acc[j0 + j] += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
       }
+    }
+  }
+}
+
+// The fixed-point sums of output row i and the 64 columns from c0, written
+// to P as they are: 64 independent stores, no loads and no FP64 work, so
+// the CTA ends (and the next tile starts on its SM) as soon as they are
+// issued.  exact_finish_kernel applies them to C.
+__device__ __forceinline__ void exact_store_fixed(const ExactParams& p, const long long (&acc)[64], int i, int c0) {
+  if (i >= p.M) return;
+  long long* P = p.P + i;
+#pragma unroll
+  for (int j = 0; j < 64; ++j)
+    if (c0 + j < p.N) P[(int64_t)(c0 + j) * p.ldp] = acc[j];
+}
+
+// C += alpha * P for the fixed-point sums an exact kernel left in P: the
+// same arithmetic as exact_store, over all M x N elements at full occupancy
+// (a drain warp doing it in the exact kernel spent about 40 us per 128 x 128
+// tile on the latency of its loads and its FP64 conversions, with the
+// tensor cores of its SM idle).
+constexpr int FINISH_COLS = 16;  // columns per CTA of exact_finish_kernel
+__global__ void __launch_bounds__(256) exact_finish_kernel(const ExactParams p) {
+  // Thread: one row; CTA: 256 rows x FINISH_COLS columns (coalesced along
+  // the rows, eight columns of loads in flight per thread).
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= p.M) return;
+  const int ei = p.ea[i];
+  const bool row_nan = ei == NONFINITE_EXP;
+  const int er = max(ei, -4000) - exact_row_lb(p, i);
+  const int64_t cbase = (int64_t)blockIdx.y * FINISH_COLS;
+#pragma unroll
+  for (int c0 = 0; c0 < FINISH_COLS; c0 += 8) {
+    long long v[8];
+    double cv[8];
+    int ej[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int64_t col = cbase + c0 + c;
+      const bool in = col < p.N;
+      v[c] = in ? p.P[(int64_t)i + col * p.ldp] : 0;
+      cv[c] = in ? static_cast<const double*>(p.C)[(int64_t)i + col * p.ldc] : 0.0;
+      ej[c] = in ? p.eb[col] : 0;
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int64_t col = cbase + c0 + c;
+      if (col >= p.N) continue;
+      double out = __longlong_as_double(0x7ff8000000000000ll);
+      if (!row_nan && ej[c] != NONFINITE_EXP)
+        out = fma(p.alpha, scale_pow2(__ll2double_rn(v[c]), er + max(ej[c], -4000)), cv[c]);
+      static_cast<double*>(p.C)[(int64_t)i + col * p.ldc] = out;
     }
   }
 }
@@ -626,7 +682,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
         if (lane == 0) umma::mbar_arrive(umma::smem_u32(&cempty[b]));
       }
     }
-    if (ok) exact_store(p, acc, i, n0 + h * 64, Lb);
+    if (ok) {
+      if (p.P) exact_store_fixed(p, acc, i, n0 + h * 64);
+      else exact_store(p, acc, i, n0 + h * 64, Lb);
+    }
   }
 
   umma::fence_before_sync();
@@ -879,7 +938,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
         if (lane == 0) umma::mbar_arrive(umma::smem_u32(&cempty[b]));
       }
     }
-    if (ok) exact_store(p, acc, i, n0 + h * 64, Lb);
+    if (ok) {
+      if (p.P) exact_store_fixed(p, acc, i, n0 + h * 64);
+      else exact_store(p, acc, i, n0 + h * 64, Lb);
+    }
   }
 
   umma::fence_before_sync();
@@ -1329,6 +1391,13 @@ bool exact_coupled() {
   return on;
 }
 
+// Fixed-point sums applied to C by exact_finish_kernel (NLA_EXACT_FINISH=0
+// applies them in the exact kernel's epilogue instead; read per launch).
+bool exact_finish_enabled() {
+  const char* v = getenv("NLA_EXACT_FINISH");
+  return !(v && v[0] == '0');
+}
+
 // Short-K group table of the coupled kernel (NLA_EXACT_MERGED=0 turns it
 // off; read per launch, so that tests can compare both tables).
 bool exact_merged_enabled() {
@@ -1530,8 +1599,11 @@ int stage_pair(const Mat& A, int64_t M, const Mat& Bt, int64_t N, int64_t K, int
   return NLA_OK;
 }
 
+// Exact updates also hold their fixed-point sums, rows padded to 128.
+size_t fixed_sums_bytes(int64_t M, int64_t N) { return (size_t)pad_to(M, BM) * (size_t)N * sizeof(long long); }
+
 size_t sliced_workspace_bytes(int64_t M, int64_t N, int64_t K, int S) {
-  return staged_bytes(M, K, S) + staged_bytes(N, K, S) + 1024;
+  return staged_bytes(M, K, S) + staged_bytes(N, K, S) + 1024 + (S == EXACT_SLICES ? fixed_sums_bytes(M, N) : 0);
 }
 
 // One tensor-core update.  in_dtype is NLA_F64 (split into S slices of BF16
@@ -1546,13 +1618,19 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
     // Exact slice products (FP64-accurate update).
     if (!bf16) return fail(NLA_ERR_ARG, "exact updates use BF16 slices");
     if (out_dtype != NLA_F64) return fail(NLA_ERR_DTYPE, "exact updates produce Float64");
-    const size_t sa = staged_bytes(M, K, S), need = sa + staged_bytes(N, K, S) + 1024;
+    const size_t sa = staged_bytes(M, K, S), sb = staged_bytes(N, K, S), need = sa + sb + 1024;
     void* base = ws;
     if (base == nullptr) {
-      NLA_TRY(workspace_get(s, need, &base));
+      NLA_TRY(workspace_get(s, need + fixed_sums_bytes(M, N), &base));
+      ws_bytes = need + fixed_sums_bytes(M, N);
     } else if (ws_bytes < need) {
       return fail(NLA_ERR_WORKSPACE, "workspace too small for the exact update");
     }
+    // The fixed-point sums follow the staged operands when the workspace has
+    // room for them (a caller's fixed workspace may not).
+    long long* fixed = ws_bytes >= need + fixed_sums_bytes(M, N)
+                           ? reinterpret_cast<long long*>(static_cast<uint8_t*>(base) + ((sa + sb + 1023) & ~(size_t)1023))
+                           : nullptr;
     Staged As, Bs;
     if (K <= FUSED_STAGE_MAX_K && stage_fused_enabled()) {
       NLA_TRY(stage_pair(A, M, transposed(B), N, K, S, true, base, static_cast<uint8_t*>(base) + sa, &As, &Bs, s));
@@ -1560,7 +1638,7 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
       NLA_TRY(stage_operand(A, M, K, NLA_F64, S, true, 0, base, &As, s));
       NLA_TRY(stage_operand(transposed(B), N, K, NLA_F64, S, true, 0, static_cast<uint8_t*>(base) + sa, &Bs, s));
     }
-    return launch_exact_gemm(As, Bs, alpha, C, false, s);
+    return launch_exact_gemm(As, Bs, alpha, C, false, s, nullptr, fixed);
   }
   if (S < 1 || S > 3) return fail(NLA_ERR_ARG, "split terms must be 1, 2, 3 or 7");
   const int beta = bf16 ? 8 : 11;
@@ -1651,7 +1729,7 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
 // C (M x N, FP64) += alpha * A * B^T from two operands staged with
 // EX_SLICES BF16 slices (A: M rows, B: N rows, same K).
 int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat& C, bool trans_out,
-                      cudaStream_t s, const ResidualTerm* res) {
+                      cudaStream_t s, const ResidualTerm* res, long long* fixed_buf) {
   const int64_t M = A.rows, N = B.rows, K = A.K;
   if (M <= 0 || N <= 0 || K <= 0) return NLA_OK;
   if (B.K != K || A.S != EX_SLICES || B.S != EX_SLICES || !A.bf16 || !B.bf16 || !A.scaled || !B.scaled)
@@ -1693,13 +1771,29 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
   const double tri_frac = (A.tri != 0 || B.tri != 0) ? 0.5 : 1.0;
   TraceScope trace(NLA_K_GEMM_UMMA, s, 2.0 * (double)M * N * (double)K * p.npairs * tri_frac,
                    (double)EX_SLICES * (A.rows_pad + B.rows_pad) * A.K_pad * 2 + 16.0 * (double)M * N);
-  if (exact_cluster_shape() == 11 && exact_coupled()) return launch_exact_coupled(p, A, B, s);
-  switch (exact_cluster_shape()) {
-    case 21: return launch_exact_shape<2, 1>(p, A, B, s);
-    case 12: return launch_exact_shape<1, 2>(p, A, B, s);
-    case 22: return launch_exact_shape<2, 2>(p, A, B, s);
-    default: return launch_exact_shape<1, 1>(p, A, B, s);
+  // Plain updates leave their fixed-point sums in fixed_buf (A.rows_pad x N)
+  // for exact_finish_kernel; residuals and transposed outputs are applied by
+  // the exact kernel itself.
+  if (fixed_buf && !res && !trans_out && exact_finish_enabled() && (N + FINISH_COLS - 1) / FINISH_COLS <= 65535) {
+    p.P = fixed_buf;
+    p.ldp = A.rows_pad;
   }
+  int rc;
+  if (exact_cluster_shape() == 11 && exact_coupled()) {
+    rc = launch_exact_coupled(p, A, B, s);
+  } else {
+    switch (exact_cluster_shape()) {
+      case 21: rc = launch_exact_shape<2, 1>(p, A, B, s); break;
+      case 12: rc = launch_exact_shape<1, 2>(p, A, B, s); break;
+      case 22: rc = launch_exact_shape<2, 2>(p, A, B, s); break;
+      default: rc = launch_exact_shape<1, 1>(p, A, B, s); break;
+    }
+  }
+  if (rc != NLA_OK || !p.P) return rc;
+  const int64_t gy = (N + FINISH_COLS - 1) / FINISH_COLS;
+  exact_finish_kernel<<<dim3((unsigned)((M + 255) / 256), (unsigned)gy), 256, 0, s>>>(p);
+  NLA_CHECK_LAUNCH("exact_finish_kernel");
+  return NLA_OK;
 }
 
 // Reads and clears the device error word after synchronising the stream.

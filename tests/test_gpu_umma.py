@@ -208,3 +208,31 @@ def test_exact_short_k_group_table(pkg, cuda, monkeypatch):
         err = ((out[0] - (C0 - opA @ B)).abs() / scale).max().item()
         assert err < 1e-14, (N, R, M, t1, err)
         assert ((out[0] - out[1]).abs() / scale).max().item() < 1e-15, (N, R, M, t1)
+
+
+def test_exact_finish_pass_matches_epilogue(pkg, cuda, monkeypatch):
+    """Plain exact updates leave their fixed-point sums in the workspace and
+    exact_finish_kernel applies them to C; NLA_EXACT_FINISH=0 applies them in
+    the exact kernel's epilogue.  Same arithmetic, so the results agree bit
+    for bit: ragged shapes, both operand layouts, alpha other than +-1, a
+    non-finite row of A and a non-finite column of B (NaN out)."""
+    import torch
+
+    g = torch.Generator(device=cuda).manual_seed(29)
+    for (N, R, M), t1 in itertools.product([(257, 300, 130), (128, 1500, 77), (64, 64, 1000)], [False, True]):
+        A = torch.randn(R if t1 else N, N if t1 else R, device=cuda, generator=g, dtype=torch.float64)
+        B = _col_major(torch.randn(R, M, device=cuda, generator=g, dtype=torch.float64))
+        A = _col_major(A)
+        opA = A.T if t1 else A
+        opA[1, 2] = float("inf")
+        B[3, 4] = float("nan")
+        C0 = _col_major(torch.randn(N, M, device=cuda, generator=g, dtype=torch.float64))
+        out = []
+        for fin in ("1", "0"):
+            monkeypatch.setenv("NLA_EXACT_FINISH", fin)
+            C = C0.clone().T.contiguous().T
+            pkg.matmul_mixed_(C, opA, B, 0.75, split_terms=7)
+            pkg.device_status(C)
+            out.append(C)
+        assert torch.isnan(out[0][1]).all() and torch.isnan(out[0][:, 4]).all()
+        assert torch.equal(out[0].nan_to_num(7.0), out[1].nan_to_num(7.0)), (N, R, M, t1)
