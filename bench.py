@@ -84,7 +84,8 @@ def parse():
                     help="run single launches of one kernel on a moderate case (for ncu captures)")
     ap.add_argument("--case-size", type=int, default=4096)
     ap.add_argument("--case-reps", type=int, default=2)
-    ap.add_argument("--case-shape", default="", help="M,N,K of the exact/fast update case (default: s,s,s)")
+    ap.add_argument("--case-shape", default="",
+                    help="M,N,K of the exact/fast update case (default: s,s,s); n,m of the leaf case")
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--m", type=int, default=16384)
     ap.add_argument("--cpu-sample", type=int, default=0,
@@ -546,7 +547,7 @@ def run_kernel_case(args):
              A (M x K) B (K x N));
       fast   the same with 3 BF16 slices (FP32 accumulation);
       leaf   one FP64 diagonal-block solve of order 128 with 8 s right-hand
-             sides;
+             sides (--case-shape n,m for order n with m right-hand sides);
       dfma   one FP64 update on CUDA cores, s x s x s;
       feed   the tensor-core feed probes (nla_measure_tensor_feed)."""
     import torch
@@ -577,10 +578,10 @@ def run_kernel_case(args):
             t0 = time.perf_counter()
             pkg.matmul_mixed_(C, A, B, -1.0, split_terms=7 if args.kernel_case == "exact" else 3)
         elif args.kernel_case == "leaf":
-            n = 128
+            n, mr = (int(x) for x in args.case_shape.split(",")) if args.case_shape else (128, 8 * s)
             A = cm(n, n).tril_() + 4 * torch.eye(n, device=dev, dtype=torch.float64)
             A = A.T.contiguous().T
-            B = cm(n, 8 * s)
+            B = cm(n, mr)
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
             pkg.LeftLowerTRSM_(A, B)

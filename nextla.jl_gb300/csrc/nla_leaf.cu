@@ -191,7 +191,7 @@ int launch_leaf_cols(const LeafArgs& g, cudaStream_t s) {
 int leaf_cols_width(int64_t m) {
   const char* v = getenv("NLA_LEAF_CW");  // read per launch, so tests can pin each width
   const int forced = v ? atoi(v) : 0;
-  if (forced == 128 || forced == 112 || forced == 96 || forced == 64) return forced;
+  if (forced == 128 || forced == 112 || forced == 96 || forced == 64 || forced == 56) return forced;
   const int64_t sms = num_sms();
   for (int cw : {64, 96, 112})
     if ((m + cw - 1) / cw <= sms) return cw;
@@ -200,6 +200,7 @@ int leaf_cols_width(int64_t m) {
 
 int launch_leaf_cols2(const LeafArgs& g, cudaStream_t s) {
   switch (leaf_cols_width(g.m)) {
+    case 56: return launch_leaf_cols<2, 56>(g, s);
     case 64: return launch_leaf_cols<2, 64>(g, s);
     case 96: return launch_leaf_cols<2, 96>(g, s);
     case 112: return launch_leaf_cols<2, 112>(g, s);

@@ -375,7 +375,7 @@ __host__ __device__ constexpr size_t leaf_cols_smem_elems(int n, int halves, int
 template <int HALVES, int CW>
 __device__ __forceinline__ void solve_cols_f64(const LeafArgs& g, int64_t c0, int ncols, unsigned char* smem_raw,
                                                double alpha) {
-  static_assert(CW % 16 == 0 && CW <= LEAF_THREADS, "right-hand sides per CTA");
+  static_assert(CW % 8 == 0 && CW <= LEAF_THREADS, "right-hand sides per CTA");
   constexpr int NT = CW * HALVES;  // threads per CTA
   const int n = g.n;
   double* X = reinterpret_cast<double*>(smem_raw);  // n x CW

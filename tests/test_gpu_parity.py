@@ -240,7 +240,7 @@ def test_f64_leaf_one_rhs_per_thread_exact(pkg, cuda):
         np.testing.assert_array_equal(to_host(Bd), X.astype(np.float64))
 
 
-@pytest.mark.parametrize("cw", [64, 96, 112, 128])
+@pytest.mark.parametrize("cw", [56, 64, 96, 112, 128])
 def test_f64_leaf_columns_per_cta(pkg, oracle, workloads, cuda, cw, monkeypatch):
     """Every width of the one-right-hand-side-per-thread leaf (NLA_LEAF_CW
     pins it; by default the fewest columns per CTA that fit one wave): exact
