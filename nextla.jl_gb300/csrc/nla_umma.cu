@@ -707,7 +707,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
 // 24 KiB of tile loads instead of 32: the TMA feed, not the tensor core,
 // bounds these kernels (about 100-120 GB/s per SM).
 // Each group's two accumulators (weights p + q and p + 1 + q) take half of a
-// 256-column TMEM buffer; two buffers fill the 512 columns.
+// 256-column TMEM buffer; two buffers fill the 512 columns.  Updates with
+// K <= 256 use a second table (below) in which the pairs of one weight share
+// an accumulator.  Plain updates store the tile's fixed-point sums for
+// exact_finish_kernel; residuals apply them here (exact_store).
 // Warps: 0 loads A, 1 issues the MMAs, 2 loads B, 3-10 drain.
 // ---------------------------------------------------------------------------
 constexpr int CP_STAGES = 4;
