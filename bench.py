@@ -77,6 +77,8 @@ def parse():
                     help="error table: every mixed configuration, or the default exact one only")
     ap.add_argument("--config3", action="store_true",
                     help="mixed TRMM R/U/T n=12288 (3-term BF16) and Float16 TRSM n=8192 m=4096, vs FP64")
+    ap.add_argument("--callers", action="store_true",
+                    help="the package's own callers (LU's trsm, LAUUM's trmm updates) on the GPU path")
     ap.add_argument("--sweep-plain", action="store_true",
                     help="plain F32/F64 TRSM and TRMM over the 8 side/uplo/trans forms, alpha 0.5 (config 1)")
     ap.add_argument("--sizes", default="4096,8192,16384")
@@ -391,6 +393,90 @@ def run_error_table(args):
     return 0
 
 
+def run_callers(args):
+    """The package's own callers on the GPU path, Float64, n = --n:
+      getrf2_trsm   the recursive LU's triangular solve (src/lu.jl:277) at
+                    the top split n1 = n/2: unit lower 8192 x 8192 with 8192
+                    right-hand sides at n = 16384, on views of one array;
+      lauum_trmm    every off-diagonal TRMM update of the blocked LAUUM
+                    (src/lauum.jl:110 and :162), block size 512.
+    One JSON line each: device time, flop rate (n1^2 (n - n1) and
+    sum_i i b^2) and the relative error against scipy/numpy in FP64 on the
+    host (the LU solve is checked on 64 sampled columns)."""
+    import numpy as np
+    import torch
+    from scipy.linalg import solve_triangular
+
+    import __graft_entry__ as graft
+
+    pkg = graft.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    n = args.n
+    rng = np.random.default_rng(5)
+
+    def timed(fn):
+        fn()  # warm-up
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1)
+
+    n1 = n // 2
+    A_h = rng.standard_normal((n, n))
+    A_h[:n1, :n1] = np.tril(A_h[:n1, :n1], -1) / np.sqrt(n1) + np.triu(A_h[:n1, :n1])
+    A0 = torch.from_numpy(np.ascontiguousarray(A_h.T)).to(dev).T
+    Ad = torch.empty_like(A0.T).T
+
+    cols = np.arange(n1, n, max(1, (n - n1) // 64))
+    L11 = np.tril(A_h[:n1, :n1], -1) + np.eye(n1)
+    want = solve_triangular(L11, A_h[:n1, cols], lower=True, unit_diagonal=True)
+    flops = float(n1) * n1 * (n - n1)
+    copy_ms = timed(lambda: Ad.copy_(A0))
+    for mixed in (False, True):
+        def lu_step():
+            Ad.copy_(A0)
+            pkg.getrf2_trsm_(Ad, n1, mixed=mixed)
+
+        ms = timed(lu_step) - copy_ms  # Ad holds the solved step afterwards
+        got = Ad[:n1, torch.from_numpy(cols).to(dev)].cpu().numpy()
+        print(json.dumps({"caller": "getrf2_trsm", "ref": "src/lu.jl:277", "n": n, "n1": n1, "dtype": "f64",
+                          "form": "exact tensor-core updates" if mixed else "plain FP64", "ms": ms,
+                          "tflops": flops / ms / 1e9,
+                          "rel_err": float(np.linalg.norm(got - want) / np.linalg.norm(want))}), flush=True)
+    del Ad, A0
+    ib = 512
+    for uplo in "UL":
+        T = np.triu(rng.standard_normal((n, n))) if uplo == "U" else np.tril(rng.standard_normal((n, n)))
+        T0 = torch.from_numpy(np.ascontiguousarray(T.T)).to(dev).T
+        Td = torch.empty_like(T0.T).T
+
+        i = (n // ib // 2) * ib  # one panel checked against numpy
+        blk = T[i:i + ib, i:i + ib]
+        want = T[:i, i:i + ib] @ blk.T if uplo == "U" else blk.T @ T[i:i + ib, :i]
+        flops = float(sum(i * ib * ib for i in range(ib, n, ib)))
+        copy_ms = timed(lambda: Td.copy_(T0))
+        for mixed in (False, True):
+            def lauum_updates():
+                Td.copy_(T0)
+                for k in range(ib, n, ib):
+                    pkg.lauum_offdiag_trmm_(uplo, Td, k, min(ib, n - k), mixed=mixed)
+
+            ms = timed(lauum_updates) - copy_ms  # Td holds the updated panels afterwards
+            got = (Td[:i, i:i + ib] if uplo == "U" else Td[i:i + ib, :i]).cpu().numpy()
+            print(json.dumps({"caller": "lauum_trmm_" + uplo, "ref": "src/lauum.jl:110" if uplo == "U" else
+                              "src/lauum.jl:162", "n": n, "block": ib, "dtype": "f64",
+                              "form": "exact tensor-core updates" if mixed else "plain FP64", "ms": ms,
+                              "tflops": flops / ms / 1e9,
+                              "rel_err_one_panel": float(np.linalg.norm(got - want) / np.linalg.norm(want))}),
+                  flush=True)
+        del Td, T0
+    return 0
+
+
 def run_sweep_plain(args):
     """Dtype-preserving TRSM and TRMM in Float32 and Float64 over all 8
     side/uplo/trans forms (trans N, T), alpha = 0.5, B n x n uniform[-1, 1],
@@ -618,6 +704,8 @@ def main():
         return run_kernel_case(args)
     if args.sweep_plain:
         return run_sweep_plain(args)
+    if args.callers:
+        return run_callers(args)
     if args.config3:
         return run_config3(args)
     if args.workload == "batched":

@@ -159,6 +159,18 @@ NLA_API int nla_trxm_mixed(char side, char uplo, char trans, double alpha, char 
                            void* stream);
 
 /*
+ * nla_trxm_mixed with a unit-diagonal option, as nla_trxm_diag is to
+ * nla_trxm: diag 'U' takes the diagonal of A as ones and never reads it (the
+ * recursive LU's solve with its unit lower factor, BLAS.trsm!('L', 'L', 'N',
+ * 'U') at src/lu.jl:277, whose diagonal holds U's).  Unit-diagonal solves
+ * take no refinement sweeps (NLA_ERR_UNSUPPORTED): use the exact 7-term
+ * updates, whose solves need none.
+ */
+NLA_API int nla_trxm_mixed_diag(char side, char uplo, char trans, char diag, double alpha, char func, int64_t n,
+                                int64_t m, const double* A, int64_t lda, double* B, int64_t ldb,
+                                const nla_mixed_opts* opts, void* stream);
+
+/*
  * Host-buffer forms of nla_trxm and nla_trxm_mixed: what a Julia caller does
  * with host arrays around unified_rectrxm! (CuArray(A), CuArray(B), the call,
  * copyto!(B, dB); src/rectrxm.jl:43-76), as one call.

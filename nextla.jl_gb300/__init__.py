@@ -12,6 +12,7 @@ identifier, so callers load it by path with :func:`load_package` in
 from . import _lib
 from ._lib import NLAArgumentError, NLAError
 from .rectrxm import (GEMM_ADD_, GEMM_SUB_, LeftLowerTRMM_, LeftLowerTRSM_, LeftUpperTRMM_, LeftUpperTRSM_,
+                      getrf2_trsm_, lauum_offdiag_trmm_,
                       RightLowerTRMM_, RightLowerTRSM_, RightUpperTRMM_, RightUpperTRSM_, device_status,
                       matmul_, matmul_mixed_, residual_, scale_, split_point, trmm, trsm, unified_rec,
                       unified_rectrxm_, unified_rectrxm_host_, unified_rectrxm_mixed_,
@@ -22,7 +23,8 @@ __all__ = [
     "LeftLowerTRSM_", "LeftUpperTRSM_", "RightLowerTRSM_", "RightUpperTRSM_",
     "LeftLowerTRMM_", "LeftUpperTRMM_", "RightLowerTRMM_", "RightUpperTRMM_",
     "NLAError", "NLAArgumentError", "load_library", "unified_rectrxm_mixed_", "matmul_mixed_", "device_status",
-    "residual_", "trsm", "trmm", "unified_rectrxm_host_", "unified_rectrxm_mixed_host_",
+    "residual_", "trsm", "trmm", "unified_rectrxm_host_", "unified_rectrxm_mixed_host_", "getrf2_trsm_",
+    "lauum_offdiag_trmm_",
 ]
 
 

@@ -83,6 +83,8 @@ SIGNATURES.update({
 SIGNATURES["nla_trxm_diag"] = ([_c, _c, _c, _c, _d, _c, _i32, _i64, _i64, _p, _i64, _p, _i64, _p], _i32)
 SIGNATURES["nla_measure_pipes"] = ([ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d), _p], _i32)
 SIGNATURES["nla_measure_tensor_feed"] = ([ctypes.POINTER(_d)] * 5 + [_p], _i32)
+SIGNATURES["nla_trxm_mixed_diag"] = ([_c, _c, _c, _c, _d, _c, _i64, _i64, _p, _i64, _p, _i64, ctypes.POINTER(MixedOpts),
+                                      _p], _i32)
 SIGNATURES["nla_trxm_host"] = ([_c, _c, _c, _d, _c, _i32, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p,
                                  _i64, _i32, _p], _i32)
 SIGNATURES["nla_trxm_mixed_host"] = ([_c, _c, _c, _d, _c, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p,

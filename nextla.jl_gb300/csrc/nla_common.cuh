@@ -196,7 +196,8 @@ int mixed_plan(char side, char uplo, char trans, char func, int64_t n, int64_t m
                const void* B, int64_t ldb, const nla_mixed_opts* o, cudaStream_t s, RecPlan* c, int* a_trans,
                nla_mixed_opts* out);
 int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, int64_t n, int64_t m,
-                    const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* o, cudaStream_t s);
+                    const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* o, cudaStream_t s,
+                    bool unit = false);
 int64_t split_point(int64_t n);
 int check_flags(char side, char uplo, char trans, char func, int dtype);
 int check_matrix(const char* name, const void* p, int64_t rows, int64_t cols, int64_t ld);

@@ -225,11 +225,16 @@ int mixed_plan(char side, char uplo, char trans, char func, int64_t n, int64_t m
 
 int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, int64_t n, int64_t m,
                     const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* o,
-                    cudaStream_t s) {
+                    cudaStream_t s, bool unit) {
   RecPlan mixed{};
   nla_mixed_opts opts{};
   int at = 0;
   NLA_TRY(mixed_plan(side, uplo, trans, func, n, m, A, lda, B, ldb, o, s, &mixed, &at, &opts));
+  // A unit diagonal reaches only the FP64 diagonal blocks (the updates never
+  // read the diagonal); the refinement's residual would need it too.
+  if (unit && func == 'S' && opts.sweeps > 0)
+    return fail(NLA_ERR_UNSUPPORTED, "unit-diagonal mixed solves take no refinement sweeps");
+  mixed.unit = unit;
   if (n == 0 || m == 0) return NLA_OK;
   uplo = mixed.uplo;
   const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
@@ -380,6 +385,15 @@ int nla_trxm_mixed(char side, char uplo, char trans, double alpha, char func, in
                    const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* opts, void* stream) {
   clear_error();
   return trxm_mixed_impl(side, uplo, trans, alpha, func, n, m, A, lda, B, ldb, opts, (cudaStream_t)stream);
+}
+
+int nla_trxm_mixed_diag(char side, char uplo, char trans, char diag, double alpha, char func, int64_t n, int64_t m,
+                        const double* A, int64_t lda, double* B, int64_t ldb, const nla_mixed_opts* opts,
+                        void* stream) {
+  clear_error();
+  if (diag != 'N' && diag != 'U') return fail(NLA_ERR_ARG, std::string("diag must be 'N' or 'U', got '") + diag + "'");
+  return trxm_mixed_impl(side, uplo, trans, alpha, func, n, m, A, lda, B, ldb, opts, (cudaStream_t)stream,
+                         diag == 'U');
 }
 
 int nla_gemm_update_mixed(int trans1, int trans2, int64_t N, int64_t R, int64_t M, double alpha, const double* in1,

@@ -267,7 +267,7 @@ def unified_rec(func, side, uplo, A, n, B, threshold=256):
     return B
 
 
-def _trxm_diag(func, side, uplo, transa, diag, A, B, alpha):
+def _trxm_diag(func, side, uplo, transa, diag, A, B, alpha, mixed=False):
     _check_flags(side, uplo, transa, func)
     if diag not in ("N", "U"):
         raise ValueError("diag must be 'N' or 'U', got %r" % (diag,))
@@ -282,27 +282,80 @@ def _trxm_diag(func, side, uplo, transa, diag, A, B, alpha):
         tr = "N" if transa in ("T", "C") else "T"
         up = "U" if uplo == "L" else "L"
     m = B.shape[1] if side == "L" else B.shape[0]
+    if mixed:
+        import ctypes
+
+        if _dtype_code(B) != _lib.NLA_F64:
+            raise ValueError("the mixed form takes Float64 operands")
+        opts = _lib.MixedOpts(_lib.NLA_LOWP_BF16, 7, 0, _lib.NLA_RESIDUAL_SPLIT, 0, None)
+        _lib.check(_lib.load().nla_trxm_mixed_diag(_lib.ch(side), _lib.ch(up), _lib.ch(tr), _lib.ch(diag),
+                                                   float(alpha), _lib.ch(func), n, m, a, lda, b, ldb,
+                                                   ctypes.byref(opts), _stream(B)))
+        return B
     _lib.check(_lib.load().nla_trxm_diag(_lib.ch(side), _lib.ch(up), _lib.ch(tr), _lib.ch(diag), float(alpha),
                                          _lib.ch(func), _dtype_code(B), n, m, a, lda, b, ldb, _stream(B)))
     return B
 
 
-def trsm(side, uplo, transa, diag, A, B, alpha=1.0):
+def trsm(side, uplo, transa, diag, A, B, alpha=1.0, *, mixed=False):
     """trsm(side, uplo, transa, diag, A, B, alpha) (src/trsm.jl:186-204):
     solves op(A) X = alpha B (side 'L') or X op(A) = alpha B ('R') in place in
     B and returns B.  The reference scales B and calls one base-case kernel,
     ignoring transa and diag (so it is limited to n <= 1024 and op(A) = A);
     here the call runs the whole recursion (nla_trxm_diag), honours transa
-    and applies diag 'U' (unit diagonal, never read)."""
-    return _trxm_diag("S", side, uplo, transa, diag, A, B, alpha)
+    and applies diag 'U' (unit diagonal, never read).  With ``mixed=True``
+    (Float64 only) the updates run on the tensor cores with exact 7-slice
+    products (nla_trxm_mixed_diag)."""
+    return _trxm_diag("S", side, uplo, transa, diag, A, B, alpha, mixed)
 
 
-def trmm(side, uplo, transa, diag, A, B, alpha=1.0):
+def trmm(side, uplo, transa, diag, A, B, alpha=1.0, *, mixed=False):
     """trmm(side, uplo, transa, diag, A, B, alpha) (src/trmm.jl:430-448):
     B := alpha op(A) B (side 'L') or alpha B op(A) ('R'), in place, through
     the recursion; transa and diag 'U' are applied (the reference ignores
-    both)."""
-    return _trxm_diag("M", side, uplo, transa, diag, A, B, alpha)
+    both).  ``mixed`` as for trsm."""
+    return _trxm_diag("M", side, uplo, transa, diag, A, B, alpha, mixed)
+
+
+# ---------------------------------------------------------------------------
+# The package's own callers of a triangular solve / multiply, on the GPU path.
+# ---------------------------------------------------------------------------
+
+def getrf2_trsm_(A, n1, *, mixed=False):
+    """The triangular solve of the recursive LU, getrf2! (src/lu.jl:277):
+    A[1:n1, n1+1:end] := L11^-1 A[1:n1, n1+1:end], with L11 the unit lower
+    triangle of A[1:n1, 1:n1] (BLAS.trsm!('L', 'L', 'N', 'U', 1, ...)).  Both
+    operands are views of the one device array A; the diagonal of A[1:n1,
+    1:n1] (which holds U's) is never read.  ``mixed=True`` (Float64) runs
+    the exact tensor-core form.  Returns A."""
+    n1 = int(n1)
+    if n1 <= 0 or n1 >= A.shape[1]:
+        return A
+    trsm("L", "L", "N", "U", A[:n1, :n1], A[:n1, n1:], 1.0, mixed=mixed)
+    return A
+
+
+def lauum_offdiag_trmm_(uplo, A, i, b, *, mixed=False):
+    """The off-diagonal update of the blocked LAUUM (compute_upper!,
+    src/lauum.jl:110; compute_lower!, src/lauum.jl:162) on the TRMM path,
+    for the diagonal block at 0-based offset i of size b:
+      uplo 'U': A[0:i, i:i+b] := A[0:i, i:i+b] * U^T,  U = triu(A[i:i+b, i:i+b]);
+      uplo 'L': A[i:i+b, 0:i] := L^T * A[i:i+b, 0:i],  L = tril(A[i:i+b, i:i+b]).
+    The reference forms these with a generic product of the whole block (the
+    same result when the block's other triangle is zero, as LAUUM's input
+    has it); here only the triangle is read.  ``mixed`` as for
+    getrf2_trsm_.  Returns A."""
+    if uplo not in ("U", "L"):
+        raise ValueError("uplo must be 'U' or 'L', got %r" % (uplo,))
+    i, b = int(i), int(b)
+    if i <= 0 or b <= 0:
+        return A
+    blk = A[i:i + b, i:i + b]
+    if uplo == "U":
+        trmm("R", "U", "T", "N", blk, A[:i, i:i + b], 1.0, mixed=mixed)
+    else:
+        trmm("L", "L", "T", "N", blk, A[i:i + b, :i], 1.0, mixed=mixed)
+    return A
 
 
 def unified_rectrxm_(side, uplo, transpose, alpha, func, A, B, *, native=False, thresholds=None):

@@ -110,3 +110,13 @@ def test_host_entries_reject_bad_arguments(lib):
     assert lib.nla_trxm_mixed_host(b"L", b"L", b"N", 1.0, b"S", 4, 4, p, 4, p, 4, p, 4, p, 4, None, 4, None, 0,
                                    None) == -1
     assert b"B_dev" in lib.nla_last_error()
+
+
+def test_trxm_mixed_diag_rejects_bad_diag(lib):
+    """nla_trxm_mixed_diag validates diag before any device work."""
+    import ctypes
+
+    rc = lib.nla_trxm_mixed_diag(b"L", b"L", b"N", b"Q", 1.0, b"S", 4, 4, ctypes.c_void_p(16), 4,
+                                 ctypes.c_void_p(16), 4, None, None)
+    assert rc == -1
+    assert b"diag" in lib.nla_last_error()
