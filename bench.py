@@ -935,7 +935,7 @@ def main():
             "metric": "trsm_tflops", "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
-            "config": {"workload": "trsm_LLN_f64_n%d_m%d_%s" % (n, m, args.variant), "n": n, "m": m, "side": "L",
+            "config": {"workload": "trsm_LLN_f64_n%d_m%d" % (n, m), "n": n, "m": m, "side": "L",
                        "uplo": "L", "trans": "N", "alpha": 1.0, "variant": args.variant,
                        "mixed": ({"lowp": args.lowp, "split_terms": args.terms, "sweeps": args.sweeps,
                                   "residual": args.residual, "cutoff": args.cutoff or "default"}
