@@ -21,7 +21,8 @@ module NextLA_GB300
 using CUDA
 using LinearAlgebra
 
-export unified_rectrxm!, unified_rectrxm_julia!, unified_rectrxm_mixed!, unified_rectrxm_mixed_host!, trsm, trmm
+export unified_rectrxm!, unified_rectrxm_julia!, unified_rectrxm_mixed!, unified_rectrxm_mixed_host!, trsm, trmm,
+       getrf2_trsm!
 
 const libnla = get(ENV, "NEXTLA_GB300_LIB", joinpath(@__DIR__, "..", "libnextla_gb300.so"))
 
@@ -247,6 +248,52 @@ function unified_rectrxm_mixed_host!(side::Char, uplo::Char, transpose::Char, al
                 pointer(dB), max(stride(dB, 2), 1), opts, host_levels, stream_handle()))
     CUDA.synchronize()
     return B
+end
+
+"""
+    trxm_mixed_diag!(func, side, uplo, transa, diag, A, B, alpha)
+
+Float64 trsm/trmm with exact tensor-core updates (`nla_trxm_mixed_diag`):
+diag 'U' takes A's diagonal as ones and never reads it.
+"""
+function trxm_mixed_diag!(func::Char, side::Char, uplo::Char, transa::Char, diag::Char,
+                          A::AbstractMatrix{Float64}, B::AbstractMatrix{Float64}, alpha)
+    n = size(A, 1)
+    m = side == 'L' ? size(B, 2) : size(B, 1)
+    pA, lda, tA = operand(A)
+    pB, ldb, tB = operand(B)
+    tB && throw(ArgumentError("B must be column-major"))
+    tr, up = transa, uplo
+    if tA
+        tr = transa in ('T', 'C') ? 'N' : 'T'
+        up = uplo == 'L' ? 'U' : 'L'
+    end
+    opts = Ref(MixedOpts(0, 7, 0, 1, 0, C_NULL))
+    check(ccall((:nla_trxm_mixed_diag, libnla), Cint,
+                (Cchar, Cchar, Cchar, Cchar, Cdouble, Cchar, Int64, Int64, CuPtr{Cvoid}, Int64, CuPtr{Cvoid}, Int64,
+                 Ref{MixedOpts}, Ptr{Cvoid}),
+                side, up, tr, diag, Float64(alpha), func, n, m, pA, lda, pB, ldb, opts, stream_handle()))
+    return B
+end
+
+"""
+    getrf2_trsm!(A, n1; mixed=false)
+
+The triangular solve of the recursive LU (getrf2!, src/lu.jl:277) on the GPU:
+A[1:n1, n1+1:end] := L11 \ A[1:n1, n1+1:end] with L11 the unit lower triangle
+of A[1:n1, 1:n1], on views of the one CuMatrix.  `mixed=true` (Float64) uses
+the exact tensor-core updates.
+"""
+function getrf2_trsm!(A::CuMatrix{T}, n1::Integer; mixed::Bool=false) where {T}
+    (n1 <= 0 || n1 >= size(A, 2)) && return A
+    L11 = view(A, 1:n1, 1:n1)
+    A12 = view(A, 1:n1, n1+1:size(A, 2))
+    if mixed
+        trxm_mixed_diag!('S', 'L', 'L', 'N', 'U', L11, A12, one(T))
+    else
+        trsm('L', 'L', 'N', 'U', L11, A12, one(T))
+    end
+    return A
 end
 
 end # module
