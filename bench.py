@@ -201,9 +201,33 @@ def cpu_baseline(A, B, sample_cols, threads):
     return float(n) * n * sample_cols / dt / 1e12, dt
 
 
+def rank_env():
+    """(world size, rank, local rank) from the torchrun environment."""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def max_over_ranks(ms, world, device):
+    """The slowest rank's time.  Every rank times its own replica between the
+    same barriers, and the job is done when the last one is."""
+    if world <= 1:
+        return ms
+    import torch
+
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_tflops(world, flops_per_rank, ms):
+    """Whole-job rate: every rank does flops_per_rank in the slowest rank's ms."""
+    return world * flops_per_rank / (ms / 1e3) / 1e12
+
+
 def run_reference(args):
-    """--impl reference: the reference algorithm (oracle port) on host cores."""
-    rank = int(os.environ.get("RANK", "0"))
+    """--impl reference: the reference algorithm (oracle port) on host cores.
+    Under torchrun, rank 0 alone runs and prints; the other ranks exit."""
+    _, rank, _ = rank_env()
     if rank != 0:
         return 0
     import numpy as np
@@ -718,9 +742,7 @@ def main():
 
     import __graft_entry__ as graft
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world, rank, local = rank_env()
     if world > 1:
         import torch.distributed as dist
 
@@ -786,13 +808,9 @@ def main():
     barrier()
     _lib.trace_enable(False)
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
     ms_per_step = ms / args.steps
-    value = world * args.steps * flops / (ms / 1e3) / 1e12
+    value = job_tflops(world, args.steps * flops, ms)
     trace = _lib.trace_summary()
 
     # Accuracy of the last solution on a sample of columns: backward error
@@ -851,8 +869,8 @@ def main():
 
     e2e_steps = 7  # the median of 7 is robust to the occasional slow host copy
     e2e_times = timed_steps(e2e_step, e2e_steps)
-    e2e_s = statistics.median(e2e_times)
-    e2e_value = world * flops / e2e_s / 1e12
+    e2e_s = max_over_ranks(statistics.median(e2e_times) * 1e3, world, dev) / 1e3
+    e2e_value = job_tflops(world, flops, e2e_s * 1e3)
     host_levels = args.host_levels if args.host_levels > 0 else int(os.environ.get("NLA_HOST_LEVELS", "3"))
     host_cutoff = args.cutoff if args.cutoff > 0 else (64 if args.variant == "mixed" else 256)
     # The host-buffer result against the device-resident solve of the timed loop.
