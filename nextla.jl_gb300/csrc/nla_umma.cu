@@ -270,7 +270,6 @@ constexpr int EX_STAGES = 6;  // 192 KiB of stages (seven measured no faster)
 constexpr int EX_STAGE_BYTES = 2 * TILE_BYTES;
 constexpr int EX_DYN_SMEM = EX_STAGES * EX_STAGE_BYTES + 1024 + 256;
 static_assert(EX_DYN_SMEM + 16 <= 232448, "exact kernel shared memory above the per-block limit");
-constexpr int EX_DEFAULT_CLUSTER = 11;  // cluster shape (CM x CN tiles) unless NLA_EXACT_CLUSTER says otherwise
 
 struct ExactParams {
   int M, N, K;
@@ -485,18 +484,11 @@ __device__ __forceinline__ void exact_store(const ExactParams& p, const long lon
   }
 }
 
-// CM x CN: the cluster shape in output tiles.  With a cluster, the CTAs of
-// one tile row share the A tile and those of one tile column the B tile: each
-// CTA loads 1/CN of its A tile and 1/CM of its B tile and multicasts them to
-// the CTAs that share it, so the L2 -> SM traffic per CTA falls from 32 KiB to
-// 16/CN + 16/CM KiB per stage.  A stage of CTA c is free again once every CTA
-// that writes into it (its tile row and tile column) has consumed it; their
-// tensor-core commits arrive on c's `empty` barrier, which counts CM + CN - 1.
-template <int CM, int CN>
+// Pair by pair: each stage holds one A slice tile and one B slice tile
+// (32 KiB), and every slice pair has its own accumulator drain.
 __global__ void __launch_bounds__(EX_THREADS, 1)
     umma_exact_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       const ExactParams p) {
-  constexpr int CS = CM * CN;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + EX_STAGES * EX_STAGE_BYTES);
@@ -508,37 +500,19 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   __shared__ volatile int s_abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int cm = 0, cn = 0, cid = (int)blockIdx.x;
-  if constexpr (CS > 1) {
-    const int r = (int)umma::cluster_ctarank();
-    cm = r % CM;
-    cn = r / CM;
-    cid = (int)blockIdx.x / CS;
-  }
-  // Clusters cover CM x CN output tiles and are rasterised in groups of 8
-  // tile rows for L2 reuse.
-  const int stm = (p.tiles_m + CM - 1) / CM, stn = (p.tiles_n + CN - 1) / CN;
-  constexpr int group = 8 / CM;
-  const int per_group = group * stn;
+  // Output tiles are rasterised in groups of 8 tile rows for L2 reuse.
+  const int cid = (int)blockIdx.x;
+  constexpr int group = 8;
+  const int per_group = group * p.tiles_n;
   const int g = cid / per_group;
   const int first_m = g * group;
-  const int gsize = min(stm - first_m, group);
+  const int gsize = min(p.tiles_m - first_m, group);
   const int local = cid % per_group;
-  const int sm0 = (first_m + local % gsize) * CM, sn0 = (local / gsize) * CN;
-  const int m0 = (sm0 + cm) * BM, n0 = (sn0 + cn) * BN;
-  // CTAs sharing this CTA's A tile (same cm) and B tile (same cn).
-  uint16_t row_mask = 0, col_mask = 0;
-#pragma unroll
-  for (int j = 0; j < CN; ++j) row_mask |= (uint16_t)(1u << (cm + CM * j));
-#pragma unroll
-  for (int j = 0; j < CM; ++j) col_mask |= (uint16_t)(1u << (j + CM * cn));
-  const uint16_t peer_mask = row_mask | col_mask;
+  const int m0 = (first_m + local % gsize) * BM, n0 = (local / gsize) * BN;
 
-  // K range: the union over the cluster's tiles, so that all its CTAs walk
-  // the same stage sequence (the extra K meets zeros of the staged triangle).
   int alo, ahi, blo, bhi;
-  tri_k_range(p.tri_a, sm0 * BM, CM * BM, p.K, alo, ahi);
-  tri_k_range(p.tri_b, sn0 * BN, CN * BN, p.K, blo, bhi);
+  tri_k_range(p.tri_a, m0, BM, p.K, alo, ahi);
+  tri_k_range(p.tri_b, n0, BN, p.K, blo, bhi);
   const int klo = max(alo, blo), khi = min(ahi, bhi);
   const int kb0 = klo / BK;
   const int kb1 = khi >= klo ? khi / BK + 1 : kb0;  // empty range when the triangles miss each other
@@ -547,7 +521,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     s_abort = 0;
     for (int s = 0; s < EX_STAGES; ++s) {
       umma::mbar_init(umma::smem_u32(&full[s]), 2);  // the A and the B producer
-      umma::mbar_init(umma::smem_u32(&empty[s]), CM + CN - 1);
+      umma::mbar_init(umma::smem_u32(&empty[s]), 1);
     }
     for (int b = 0; b < 2; ++b) {
       umma::mbar_init(umma::smem_u32(&cfull[b]), 1);
@@ -559,9 +533,6 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   if (warp == 1) umma::tmem_alloc(umma::smem_u32(tmem_slot), 256);
   umma::fence_before_sync();
   __syncthreads();
-  // Peers multicast into this CTA's stages and barriers only after all of
-  // the cluster's barriers are initialised.
-  if constexpr (CS > 1) umma::cluster_sync();
   umma::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
   bool ok = true;
@@ -588,31 +559,11 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
             const uint32_t fb = umma::smem_u32(&full[s]);
             umma::mbar_arrive_expect_tx(fb, (uint32_t)TILE_BYTES);
             uint8_t* st = smem + s * EX_STAGE_BYTES;
-            // Rows of a tile are 128 bytes: part j of a tile split in parts of
-            // R rows starts j * R * 128 bytes in (a multiple of the 1024-byte
-            // swizzle atom).
-            if (is_a) {
-              if constexpr (CN > 1)
-                umma::tma_load_2d_mc(umma::smem_u32(st + cn * (BM / CN) * 128), &tmA, fb, kb * BK,
-                                     m0 * EX_SLICES + p.pa[pr] * BM + cn * (BM / CN), row_mask);
-              else
-                umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, m0 * EX_SLICES + p.pa[pr] * BM);
-            } else {
-              if constexpr (CM > 1)
-                umma::tma_load_2d_mc(umma::smem_u32(st + TILE_BYTES + cm * (BN / CM) * 128), &tmB, fb, kb * BK,
-                                     n0 * EX_SLICES + p.pb[pr] * BN + cm * (BN / CM), col_mask);
-              else
-                umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), &tmB, fb, kb * BK, n0 * EX_SLICES + p.pb[pr] * BN);
-            }
+            if (is_a)
+              umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, m0 * EX_SLICES + p.pa[pr] * BM);
+            else
+              umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), &tmB, fb, kb * BK, n0 * EX_SLICES + p.pb[pr] * BN);
           }
-        }
-      }
-      if constexpr (CS > 1) {
-        // Wait for the last release of every stage used: every peer's commit
-        // that targets this CTA's barriers has landed before it exits.
-        for (int s = 0; s < EX_STAGES && s < it && ok; ++s) {
-          const uint32_t rounds = (uint32_t)((it - s + EX_STAGES - 1) / EX_STAGES);
-          ok = umma::mbar_wait(umma::smem_u32(&empty[s]), (rounds & 1u) ^ 1u, &s_abort, &g_device_error, 16);
         }
       }
     }
@@ -645,10 +596,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
             for (int kk = 0; kk < BK / 16; ++kk)
               umma::mma_f16(tmem + (uint32_t)(b * BN), umma::desc_kmajor_sw128(a0 + kk * 32),
                             umma::desc_kmajor_sw128(b0 + kk * 32), idesc, (kb > c0 || kk > 0) ? 1u : 0u);
-            if constexpr (CS > 1)
-              umma::mma_commit_mc(umma::smem_u32(&empty[s]), peer_mask);
-            else
-              umma::mma_commit(umma::smem_u32(&empty[s]));
+            umma::mma_commit(umma::smem_u32(&empty[s]));
           }
           if (ok) umma::mma_commit(umma::smem_u32(&cfull[b]));
         }
@@ -690,7 +638,6 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
 
   umma::fence_before_sync();
   __syncthreads();
-  if constexpr (CS > 1) umma::cluster_sync();
   if (warp == 1) {
     __syncwarp();
     umma::fence_after_sync();
@@ -1361,31 +1308,17 @@ int ensure_gemm_smem() {
   return status == cudaSuccess ? NLA_OK : cuda_status(status, "cudaFuncSetAttribute(umma_gemm_kernel)");
 }
 
-template <int CM, int CN>
 int ensure_exact_smem() {
   static std::once_flag once;
   static cudaError_t status = cudaSuccess;
   std::call_once(once, [] {
-    status = cudaFuncSetAttribute(umma_exact_kernel<CM, CN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  EX_DYN_SMEM);
+    status = cudaFuncSetAttribute(umma_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, EX_DYN_SMEM);
   });
   return status == cudaSuccess ? NLA_OK : cuda_status(status, "cudaFuncSetAttribute(umma_exact_kernel)");
 }
 
-// Cluster shape of the exact kernel, CM x CN output tiles: NLA_EXACT_CLUSTER
-// = "11", "21", "12" or "22" (read once).
-int exact_cluster_shape() {
-  static int shape = [] {
-    const char* v = getenv("NLA_EXACT_CLUSTER");
-    if (v && (!strcmp(v, "11") || !strcmp(v, "21") || !strcmp(v, "12") || !strcmp(v, "22"))) return atoi(v);
-    return EX_DEFAULT_CLUSTER;
-  }();
-  return shape;
-}
-
 // Exact-kernel variant (NLA_EXACT_KERNEL, read once): "coupled" (pairs
-// sharing a B tile, the default) or "pairs" (pair by pair, with the cluster
-// options).
+// sharing a B tile, the default) or "pairs" (pair by pair).
 bool exact_coupled() {
   static const bool on = [] {
     const char* e = getenv("NLA_EXACT_KERNEL");
@@ -1428,28 +1361,15 @@ int launch_exact_coupled(const ExactParams& params, const Staged& A, const Stage
   return NLA_OK;
 }
 
-template <int CM, int CN>
-int launch_exact_shape(const ExactParams& p, const Staged& A, const Staged& B, cudaStream_t s) {
+int launch_exact_pairs(const ExactParams& p, const Staged& A, const Staged& B, cudaStream_t s) {
   CUtensorMap mA, mB;
-  NLA_TRY(make_map(&mA, A.slices, true, (uint64_t)A.K_pad, (uint64_t)(EX_SLICES * A.rows_pad), BM / CN));
-  NLA_TRY(make_map(&mB, B.slices, true, (uint64_t)B.K_pad, (uint64_t)(EX_SLICES * B.rows_pad), BN / CM));
-  NLA_TRY((ensure_exact_smem<CM, CN>()));
-  const int64_t grid = (int64_t)CM * CN * ((p.tiles_m + CM - 1) / CM) * ((p.tiles_n + CN - 1) / CN);
+  NLA_TRY(make_map(&mA, A.slices, true, (uint64_t)A.K_pad, (uint64_t)(EX_SLICES * A.rows_pad)));
+  NLA_TRY(make_map(&mB, B.slices, true, (uint64_t)B.K_pad, (uint64_t)(EX_SLICES * B.rows_pad)));
+  NLA_TRY(ensure_exact_smem());
+  const int64_t grid = (int64_t)p.tiles_m * p.tiles_n;
   if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "too many output tiles");
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3(EX_THREADS);
-  cfg.dynamicSmemBytes = EX_DYN_SMEM;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = CM * CN;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = CM * CN > 1 ? 1 : 0;
-  const cudaError_t e = cudaLaunchKernelEx(&cfg, umma_exact_kernel<CM, CN>, mA, mB, p);
-  if (e != cudaSuccess) return cuda_status(e, "umma_exact_kernel launch");
+  umma_exact_kernel<<<(unsigned)grid, EX_THREADS, EX_DYN_SMEM, s>>>(mA, mB, p);
+  NLA_CHECK_LAUNCH("umma_exact_kernel");
   return NLA_OK;
 }
 
@@ -1781,17 +1701,7 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
     p.P = fixed_buf;
     p.ldp = A.rows_pad;
   }
-  int rc;
-  if (exact_cluster_shape() == 11 && exact_coupled()) {
-    rc = launch_exact_coupled(p, A, B, s);
-  } else {
-    switch (exact_cluster_shape()) {
-      case 21: rc = launch_exact_shape<2, 1>(p, A, B, s); break;
-      case 12: rc = launch_exact_shape<1, 2>(p, A, B, s); break;
-      case 22: rc = launch_exact_shape<2, 2>(p, A, B, s); break;
-      default: rc = launch_exact_shape<1, 1>(p, A, B, s); break;
-    }
-  }
+  const int rc = exact_coupled() ? launch_exact_coupled(p, A, B, s) : launch_exact_pairs(p, A, B, s);
   if (rc != NLA_OK || !p.P) return rc;
   const int64_t gy = (N + FINISH_COLS - 1) / FINISH_COLS;
   exact_finish_kernel<<<dim3((unsigned)((M + 255) / 256), (unsigned)gy), 256, 0, s>>>(p);
