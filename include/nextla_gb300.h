@@ -238,8 +238,10 @@ NLA_API int nla_trxm_residual(char side, char uplo, char trans, double alpha, in
  * NLA_ERR_WORKSPACE: with 3 slices, for example, about (N + M) * R <= 11e6
  * once N, M are rounded up to 128 and R to 64.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress); make that first
- * call before any stream capture.  All calls share the array: calls that
- * overlap on the GPU (concurrent streams or unordered host threads) race.
+ * call before any stream capture; the address is cached per device, so
+ * resetting the device after that first call is not supported.  All calls
+ * share the array: calls that overlap on the GPU (concurrent streams or
+ * unordered host threads) race.
  */
 #define NLA_NOALLOC_SCRATCH_BYTES (64ll << 20)
 NLA_API int nla_gemm_update_mixed_noalloc(int trans1, int trans2, int64_t N, int64_t R, int64_t M, double alpha,
@@ -254,17 +256,39 @@ NLA_API int nla_gemm_update_mixed_noalloc(int trans1, int trans2, int64_t N, int
 NLA_API int nla_device_status(void* stream);
 
 /*
+ * Give-up limit, in nanoseconds, of the waits between the roles of a
+ * tensor-core kernel on the current device (TMA producer, MMA issuer,
+ * accumulator drain); 0 restores the default of 2 s.  No counterpart in the
+ * reference, which has no bounded waits.  A wait past the limit makes the
+ * kernel stop, wait for its own in-flight loads and tensor-core work with the
+ * default limit, release its tensor memory and return; nla_device_status then
+ * reports NLA_ERR_TIMEOUT.  A limit below 1 ms makes nearly every wait that
+ * does not complete at once give up: that is how the tests drive this path.
+ * Takes effect for kernels launched after it returns.
+ */
+NLA_API int nla_set_wait_limit_ns(uint64_t ns);
+
+/*
  * Batched solve of independent, unevenly sized systems (no counterpart in the
  * reference, which solves one system per unified_rectrxm! call,
  * src/rectrxm.jl:43-76).  Every system i solves op(A_i) X_i = alpha B_i
  * (side 'L', the batch's uplo and trans) in place in B_i, with A_i n_i x n_i
  * (n_i <= 1024) at A_pool + a_off elements and B_i n_i x m_i at
  * B_pool + b_off elements, column-major with leading dimensions lda, ldb.
- * A plan uploads the descriptors and a cost-sorted list of work items (one
- * per system and block of right-hand sides); `cols_per_item` gives the block
- * width (8, 16 or 32) for each size bucket b (16*2^b <= n < 32*2^b, the last
- * bucket open above), or NULL for defaults.  The plan owns device memory
- * until destroyed; one plan must not be used from two streams at once.
+ * A plan runs the recursion of unified_rec (src/rectrxm.jl:101-198) for every
+ * system and block of right-hand sides (a group) on the host, down to leaves
+ * of at most `cutoff` rows, and uploads its pieces as a queue of nodes: leaf
+ * solves and update tiles (one per leaf the recursion's GEMM updates, with
+ * the K range of the half solved first).  The queue is ordered by a
+ * list-scheduling simulation over the persistent CTAs; nodes wait on
+ * per-group and per-leaf counters for the nodes they depend on, each wait
+ * bounded (nla_set_wait_limit_ns; nla_device_status reports one that gave
+ * up).  Per size bucket b (16*2^b <= n < 32*2^b, the last bucket open above)
+ * `tuning` gives the leaf order (16, 32 or 64) and the widest block of
+ * right-hand sides (16, 32, 64 or 128); NULL takes defaults.  With
+ * nla_batch_plan_create, `cols_per_item` gives only the block widths.  The
+ * plan owns device memory until destroyed; one plan must not be used from
+ * two streams at once.  nla_batch_plan_info reports the number of nodes.
  * Modes of nla_batch_solve:
  *   NLA_BATCH_GRAPH       one persistent kernel, captured once into a CUDA
  *                         graph (re-captured when alpha or the pools change)
@@ -278,12 +302,18 @@ typedef struct {
   int64_t b_off, ldb;
 } nla_batch_desc;
 #define NLA_BATCH_BUCKETS 6
+typedef struct {
+  int cutoff[NLA_BATCH_BUCKETS]; /* leaf order per size bucket: 16, 32 or 64 */
+  int cols[NLA_BATCH_BUCKETS];   /* widest block of right-hand sides: 16, 32, 64 or 128 */
+} nla_batch_tuning;
 #define NLA_BATCH_GRAPH 0
 #define NLA_BATCH_PERSISTENT 1
 #define NLA_BATCH_LOOP 2
 typedef struct nla_batch_plan_s* nla_batch_plan;
 NLA_API int nla_batch_plan_create(nla_batch_plan* plan, int dtype, char uplo, char trans, int64_t count,
                                   const nla_batch_desc* descs, const int* cols_per_item);
+NLA_API int nla_batch_plan_create_tuned(nla_batch_plan* plan, int dtype, char uplo, char trans, int64_t count,
+                                        const nla_batch_desc* descs, const nla_batch_tuning* tuning);
 NLA_API int nla_batch_plan_info(nla_batch_plan plan, int64_t* items, int64_t* grid, double* flops);
 NLA_API int nla_batch_solve(nla_batch_plan plan, double alpha, const void* A_pool, void* B_pool, int mode,
                             void* stream);
@@ -310,20 +340,6 @@ NLA_API int nla_batch_solve_mixed(nla_batch_plan plan, double alpha, const void*
 NLA_API int nla_measure_pipes(double* dfma_tflops, double* dmma_tflops, double* ffma_tflops, void* stream);
 
 /*
- * What feeds the tensor cores on the current GPU, one CTA per SM
- * (no counterpart in the reference):
- *   mma_tflops     128 x 128 x 16 BF16 tcgen05 MMAs from operands resident in
- *                  shared memory;
- *   tma_gbs_1/2    TMA tile loads into shared memory per SM (GB/s), issued by
- *                  one or two producer warps;
- *   pipe_tflops_1/2  TMA loads released by four MMAs per stage (the exact
- *                  kernels' main loop without their epilogue), one or two
- *                  producer warps.
- */
-NLA_API int nla_measure_tensor_feed(double* mma_tflops, double* tma_gbs_1, double* tma_gbs_2, double* pipe_tflops_1,
-                                    double* pipe_tflops_2, void* stream);
-
-/*
  * Kernel tracing (no counterpart in the reference, which has no tracing).
  * nla_trace_enable(1) clears earlier records and starts recording; every
  * library kernel launched afterwards is bracketed by CUDA events on its
@@ -341,7 +357,9 @@ NLA_API int nla_measure_tensor_feed(double* mma_tflops, double* tma_gbs_1, doubl
 #define NLA_K_SCALE 5      /* alpha scaling and element-wise passes */
 #define NLA_K_RESIDUAL 6   /* residual and correction passes of refinement */
 #define NLA_K_BATCHED 7    /* persistent batched solve */
-#define NLA_K_COUNT 8
+#define NLA_K_COPY_IN 8    /* host-to-device block copies of the host-buffer entry points (bytes, no flops) */
+#define NLA_K_COPY_OUT 9   /* device-to-host block copies of the host-buffer entry points */
+#define NLA_K_COUNT 10
 NLA_API int nla_trace_enable(int on);
 NLA_API int nla_trace_summary(int kernel_class, int64_t* launches, double* ms, double* flops, double* bytes);
 

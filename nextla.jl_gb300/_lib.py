@@ -55,6 +55,7 @@ SIGNATURES.update({
     "nla_gemm_update_mixed": ([_i32, _i32, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _p, _i64, _i32, _i32, _p],
                               _i32),
     "nla_device_status": ([_p], _i32),
+    "nla_set_wait_limit_ns": ([ctypes.c_uint64], _i32),
     "nla_trxm_residual": ([_c, _c, _c, _d, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _i32, _p], _i32),
     "nla_gemm_update_mixed_noalloc": ([_i32, _i32, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _p, _i64, _i32, _i32,
                                        _p], _i32),
@@ -68,12 +69,21 @@ class BatchDesc(ctypes.Structure):
                 ("b_off", ctypes.c_int64), ("ldb", ctypes.c_int64)]
 
 
+class BatchTuning(ctypes.Structure):
+    """nla_batch_tuning of include/nextla_gb300.h: per size bucket, the leaf
+    order of the recursion and the widest block of right-hand sides."""
+
+    _fields_ = [("cutoff", ctypes.c_int * 6), ("cols", ctypes.c_int * 6)]
+
+
 NLA_BATCH_BUCKETS = 6
 NLA_BATCH_GRAPH, NLA_BATCH_PERSISTENT, NLA_BATCH_LOOP = 0, 1, 2
 
 SIGNATURES.update({
     "nla_batch_plan_create": ([ctypes.POINTER(_p), _i32, _c, _c, _i64, ctypes.POINTER(BatchDesc),
                                ctypes.POINTER(_i32)], _i32),
+    "nla_batch_plan_create_tuned": ([ctypes.POINTER(_p), _i32, _c, _c, _i64, ctypes.POINTER(BatchDesc),
+                                     ctypes.POINTER(BatchTuning)], _i32),
     "nla_batch_plan_info": ([_p, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_d)], _i32),
     "nla_batch_solve": ([_p, _d, _p, _p, _i32, _p], _i32),
     "nla_batch_plan_destroy": ([_p], _i32),
@@ -82,7 +92,6 @@ SIGNATURES.update({
 
 SIGNATURES["nla_trxm_diag"] = ([_c, _c, _c, _c, _d, _c, _i32, _i64, _i64, _p, _i64, _p, _i64, _p], _i32)
 SIGNATURES["nla_measure_pipes"] = ([ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d), _p], _i32)
-SIGNATURES["nla_measure_tensor_feed"] = ([ctypes.POINTER(_d)] * 5 + [_p], _i32)
 SIGNATURES["nla_trxm_mixed_diag"] = ([_c, _c, _c, _c, _d, _c, _i64, _i64, _p, _i64, _p, _i64, ctypes.POINTER(MixedOpts),
                                       _p], _i32)
 SIGNATURES["nla_trxm_host"] = ([_c, _c, _c, _d, _c, _i32, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p,
@@ -98,17 +107,8 @@ def measure_pipes(stream=None) -> dict:
     return {"dfma": a.value, "dmma": b.value, "ffma": c.value}
 
 
-def measure_tensor_feed(stream=None) -> dict:
-    """nla_measure_tensor_feed: MMA-only TFLOP/s, TMA GB/s per SM with one and
-    two producer warps, and TMA-fed MMA TFLOP/s with one and two producers."""
-    v = [_d() for _ in range(5)]
-    check(load().nla_measure_tensor_feed(*[ctypes.byref(x) for x in v], stream))
-    keys = ["mma_tflops", "tma_gbs_per_sm_1_producer", "tma_gbs_per_sm_2_producers", "pipe_tflops_1_producer",
-            "pipe_tflops_2_producers"]
-    return {k: x.value for k, x in zip(keys, v)}
-
-
-KERNEL_CLASSES = ["leaf_solve", "leaf_mult", "gemm_simt", "gemm_umma", "split", "scale", "residual", "batched"]
+KERNEL_CLASSES = ["leaf_solve", "leaf_mult", "gemm_simt", "gemm_umma", "split", "scale", "residual", "batched",
+                  "copy_in", "copy_out"]
 
 _lib = None
 _lock = threading.Lock()

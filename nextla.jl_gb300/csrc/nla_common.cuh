@@ -161,6 +161,9 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
 constexpr int EXACT_SLICES = 7;
 int workspace_get(cudaStream_t s, size_t bytes, void** out);
 int device_status(cudaStream_t s);
+int set_wait_limit(uint64_t ns);
+uint64_t wait_limit_ns();  // the limit last set (default 2 s), for kernels that take it as a parameter
+int batch_device_error();  // the batched kernel's error word (read and cleared), or 0
 
 // The recursion of unified_rec (src/rectrxm.jl:101-198) with a choice of
 // update kernel.

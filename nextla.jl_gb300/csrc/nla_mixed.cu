@@ -427,4 +427,9 @@ int nla_device_status(void* stream) {
   return device_status((cudaStream_t)stream);
 }
 
+int nla_set_wait_limit_ns(uint64_t ns) {
+  clear_error();
+  return set_wait_limit(ns);
+}
+
 }  // extern "C"

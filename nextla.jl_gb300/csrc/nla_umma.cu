@@ -26,6 +26,7 @@
 
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <type_traits>
 #include <unordered_map>
@@ -92,9 +93,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)p.stages * p.stage_bytes);
-  uint64_t* full = bars;
-  uint64_t* empty = bars + p.stages;
-  uint64_t* accf = bars + 2 * p.stages;
+  uint64_t* fullA = bars;  // the A producer's (or, with one producer, both operands') loads of each stage
+  uint64_t* fullB = bars + p.stages;  // the B producer's loads
+  uint64_t* empty = bars + 2 * p.stages;
+  uint64_t* accf = bars + 3 * p.stages;
   uint64_t* drain = accf + 1;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   __shared__ volatile int s_abort;
@@ -115,7 +117,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   if (threadIdx.x == 0) {
     s_abort = 0;
     for (int s = 0; s < p.stages; ++s) {
-      umma::mbar_init(umma::smem_u32(&full[s]), p.producers);  // the A and the B producer
+      umma::mbar_init(umma::smem_u32(&fullA[s]), 1);
+      umma::mbar_init(umma::smem_u32(&fullB[s]), 1);
       umma::mbar_init(umma::smem_u32(&empty[s]), 1);
     }
     umma::mbar_init(umma::smem_u32(accf), 1);
@@ -134,15 +137,17 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     // Producers: warp 0 loads the A slices and the last warp the B slices
     // (p.producers = 2), or warp 0 loads both (1).  One issuing thread is
     // limited to about 110 GB/s of TMA tile loads per SM, two reach about
-    // 175 GB/s.  Each producer arrives on full[s] for its own bytes.
+    // 175 GB/s.  Each producer arrives on its own full barrier of a stage.
     const bool is_a = warp == 0;
     const bool both = p.producers == 1;
     if (lane == 0 && (is_a || !both)) {
-      for (int kb = 0; kb < p.num_kb; ++kb) {
+      uint64_t* own = is_a ? fullA : fullB;
+      int kb = 0;
+      for (; kb < p.num_kb; ++kb) {
         const int s = kb % p.stages;
         const uint32_t round = (uint32_t)(kb / p.stages);
         if (!umma::mbar_wait(umma::smem_u32(&empty[s]), (round & 1u) ^ 1u, &s_abort, &g_device_error, 1)) break;
-        const uint32_t fb = umma::smem_u32(&full[s]);
+        const uint32_t fb = umma::smem_u32(&own[s]);
         uint8_t* st = smem + (size_t)s * p.stage_bytes;
         umma::mbar_arrive_expect_tx(fb, (uint32_t)(((both ? p.sa + p.sb : is_a ? p.sa : p.sb)) * TILE_BYTES));
         if (is_a)
@@ -152,6 +157,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           for (int sl = 0; sl < p.sb; ++sl)
             umma::tma_load_2d(umma::smem_u32(st + (p.sa + sl) * TILE_BYTES), &tmB, fb, kb * BK, n0 * p.sb + sl * BN);
       }
+      umma::producer_quiesce(own, p.stages, kb, &s_abort, &g_device_error, 5);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -159,7 +165,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       for (int kb = 0; kb < p.num_kb; ++kb) {
         const int s = kb % p.stages;
         const uint32_t round = (uint32_t)(kb / p.stages);
-        if (!umma::mbar_wait(umma::smem_u32(&full[s]), round & 1u, &s_abort, &g_device_error, 2)) {
+        if (!umma::mbar_wait(umma::smem_u32(&fullA[s]), round & 1u, &s_abort, &g_device_error, 2) ||
+            (p.producers == 2 && !umma::mbar_wait(umma::smem_u32(&fullB[s]), round & 1u, &s_abort, &g_device_error, 2))) {
           ok = false;
           break;
         }
@@ -491,8 +498,9 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
                       const ExactParams p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + EX_STAGES * EX_STAGE_BYTES);
-  uint64_t* empty = full + EX_STAGES;
+  uint64_t* fullA = reinterpret_cast<uint64_t*>(smem + EX_STAGES * EX_STAGE_BYTES);  // A producer's loads
+  uint64_t* fullB = fullA + EX_STAGES;                                                // B producer's loads
+  uint64_t* empty = fullB + EX_STAGES;
   uint64_t* cfull = empty + EX_STAGES;
   uint64_t* cempty = cfull + 2;
   uint64_t* drain = cempty + 2;
@@ -520,7 +528,8 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   if (threadIdx.x == 0) {
     s_abort = 0;
     for (int s = 0; s < EX_STAGES; ++s) {
-      umma::mbar_init(umma::smem_u32(&full[s]), 2);  // the A and the B producer
+      umma::mbar_init(umma::smem_u32(&fullA[s]), 1);
+      umma::mbar_init(umma::smem_u32(&fullB[s]), 1);
       umma::mbar_init(umma::smem_u32(&empty[s]), 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -540,10 +549,11 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   if (warp == 0 || warp == 2) {
     // Two producers, one per operand: a thread issues TMA tile loads at a
     // limited rate (about 110 GB/s per SM measured with 16 KiB boxes), and two
-    // issuing warps reach about 175 GB/s.  Each arrives on full[s] for its
-    // own 16 KiB.
+    // issuing warps reach about 175 GB/s.  Each arrives on its own full
+    // barrier of a stage for its 16 KiB.
     const bool is_a = warp == 0;
     if (lane == 0) {
+      uint64_t* own = is_a ? fullA : fullB;
       int it = 0;
       for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
         const int c0 = max(kb0, cc * EX_CHUNK), c1 = min(kb1, (cc + 1) * EX_CHUNK);
@@ -556,7 +566,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
               ok = false;
               break;
             }
-            const uint32_t fb = umma::smem_u32(&full[s]);
+            const uint32_t fb = umma::smem_u32(&own[s]);
             umma::mbar_arrive_expect_tx(fb, (uint32_t)TILE_BYTES);
             uint8_t* st = smem + s * EX_STAGE_BYTES;
             if (is_a)
@@ -566,6 +576,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
           }
         }
       }
+      umma::producer_quiesce(own, EX_STAGES, it, &s_abort, &g_device_error, 16);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -585,7 +596,8 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
           for (int kb = c0; kb < c1; ++kb, ++it) {
             const int s = it % EX_STAGES;
             const uint32_t round = (uint32_t)(it / EX_STAGES);
-            if (!umma::mbar_wait(umma::smem_u32(&full[s]), round & 1u, &s_abort, &g_device_error, 13)) {
+            if (!umma::mbar_wait(umma::smem_u32(&fullA[s]), round & 1u, &s_abort, &g_device_error, 13) ||
+                !umma::mbar_wait(umma::smem_u32(&fullB[s]), round & 1u, &s_abort, &g_device_error, 13)) {
               ok = false;
               break;
             }
@@ -728,8 +740,9 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
                               const __grid_constant__ CUtensorMap tmB, const ExactParams p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + CP_STAGES * CP_STAGE_BYTES);
-  uint64_t* empty = full + CP_STAGES;
+  uint64_t* fullA = reinterpret_cast<uint64_t*>(smem + CP_STAGES * CP_STAGE_BYTES);  // A producer's loads
+  uint64_t* fullB = fullA + CP_STAGES;                                                // B producer's loads
+  uint64_t* empty = fullB + CP_STAGES;
   uint64_t* cfull = empty + CP_STAGES;
   uint64_t* cempty = cfull + 2;
   uint64_t* drain = cempty + 2;
@@ -754,7 +767,8 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   if (threadIdx.x == 0) {
     s_abort = 0;
     for (int s = 0; s < CP_STAGES; ++s) {
-      umma::mbar_init(umma::smem_u32(&full[s]), 2);  // the A and the B producer
+      umma::mbar_init(umma::smem_u32(&fullA[s]), 1);
+      umma::mbar_init(umma::smem_u32(&fullB[s]), 1);
       umma::mbar_init(umma::smem_u32(&empty[s]), 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -775,6 +789,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   if (warp == 0 || warp == 2) {
     const bool is_a = warp == 0;
     if (lane == 0) {
+      uint64_t* own = is_a ? fullA : fullB;
       int it = 0;
       for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
         const int c0 = max(kb0, cc * EX_CHUNK), c1 = min(kb1, (cc + 1) * EX_CHUNK);
@@ -791,7 +806,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
                 ok = false;
                 break;
               }
-              const uint32_t fb = umma::smem_u32(&full[s]);
+              const uint32_t fb = umma::smem_u32(&own[s]);
               uint8_t* st = smem + s * CP_STAGE_BYTES;
               // Staged rows: slice sl of the tile at row r0 starts at r0 * 7 + sl * 128,
               // so A_p and A_p+1 are one 256-row box.
@@ -806,6 +821,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
           }
         }
       }
+      umma::producer_quiesce(own, CP_STAGES, it, &s_abort, &g_device_error, 36);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -834,7 +850,9 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
             const uint32_t dA = sg.two ? d0 : (sg.dst ? d1 : d0);
             for (int kb = c0; kb < c1; ++kb, ++it) {
               const int s = it % CP_STAGES;
-              if (!umma::mbar_wait(umma::smem_u32(&full[s]), (uint32_t)(it / CP_STAGES) & 1u, &s_abort,
+              if (!umma::mbar_wait(umma::smem_u32(&fullA[s]), (uint32_t)(it / CP_STAGES) & 1u, &s_abort,
+                                   &g_device_error, 33) ||
+                  !umma::mbar_wait(umma::smem_u32(&fullB[s]), (uint32_t)(it / CP_STAGES) & 1u, &s_abort,
                                    &g_device_error, 33)) {
                 ok = false;
                 break;
@@ -1709,6 +1727,20 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
   return NLA_OK;
 }
 
+namespace {
+std::atomic<uint64_t> g_wait_limit_host{umma::WAIT_LIMIT_NS};
+}
+
+int set_wait_limit(uint64_t ns) {
+  const uint64_t v = ns == 0 ? umma::WAIT_LIMIT_NS : ns;
+  const cudaError_t e = cudaMemcpyToSymbol(umma::g_wait_limit_ns, &v, sizeof(v));
+  if (e != cudaSuccess) return cuda_status(e, "set wait limit");
+  g_wait_limit_host.store(v);
+  return NLA_OK;
+}
+
+uint64_t wait_limit_ns() { return g_wait_limit_host.load(); }
+
 // Reads and clears the device error word after synchronising the stream.
 int device_status(cudaStream_t s) {
   cudaError_t e = cudaStreamSynchronize(s);
@@ -1719,8 +1751,11 @@ int device_status(cudaStream_t s) {
   if (v != 0) {
     int zero = 0;
     cudaMemcpyToSymbol(g_device_error, &zero, sizeof(int));
-    return fail(NLA_ERR_TIMEOUT, "a bounded device-side wait gave up (site " + std::to_string(v) + ")");
   }
+  const int vb = batch_device_error();
+  if (v != 0) return fail(NLA_ERR_TIMEOUT, "a bounded device-side wait gave up (site " + std::to_string(v) + ")");
+  if (vb != 0)
+    return fail(NLA_ERR_TIMEOUT, "a batched dependency wait gave up (site " + std::to_string(vb) + ")");
   return NLA_OK;
 }
 

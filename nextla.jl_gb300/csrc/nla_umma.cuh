@@ -52,27 +52,52 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
+// Limit of the waits that honour aborts (the pipeline waits between the
+// roles of a CTA): WAIT_LIMIT_NS unless nla_set_wait_limit_ns changed it.
+// The waits that drain a CTA's own in-flight work before it exits always use
+// WAIT_LIMIT_NS.
+static __device__ uint64_t g_wait_limit_ns = WAIT_LIMIT_NS;
+
 // Wait for the phase with the given parity to complete.  Returns false (and
 // raises *abort and the device error word) if the wait runs past the limit
-// or another role of the CTA has aborted.
+// or another role of the CTA has aborted.  The timer is read every 256 polls,
+// or on every poll when the limit is below a millisecond.
 // With honor_abort false the wait ignores other roles' aborts (used to drain
-// in-flight tensor-core work before TMEM is released).
+// in-flight tensor-core work and TMA loads before the CTA exits).
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort, int* err,
                                           int where, bool honor_abort = true) {
+  if (mbar_try_wait(bar, parity)) return true;
+  // Only a wait that did not complete at once reads the limit.
+  const uint64_t limit = honor_abort ? g_wait_limit_ns : WAIT_LIMIT_NS;
+  const uint32_t mask = limit < 1000000ull ? 0u : 255u;
   uint64_t t0 = 0;
   for (uint32_t it = 0;; ++it) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 255u) == 0) {
+    if (it > 0 && mbar_try_wait(bar, parity)) return true;
+    if ((it & mask) == 0) {
       if (honor_abort && *abort) return false;
       const uint64_t now = globaltimer();
       if (it == 0) {
         t0 = now;
-      } else if (now - t0 > WAIT_LIMIT_NS) {
+      } else if (now - t0 > limit) {
         *abort = 1;
         atomicCAS(err, 0, where);
         return false;
       }
     }
+  }
+}
+
+// End of a TMA producer's loop: `issued` loads went to stage it % stages in
+// round it / stages, each completing one phase of that stage's barrier in
+// `own_full` (barriers this producer alone arrives on).  Waits, ignoring
+// aborts and with the fixed limit, for the last phase of every stage used, so
+// that none of its loads is still writing into this CTA's shared memory when
+// the CTA exits (after an abort the consumer may have stopped reading them).
+__device__ __forceinline__ void producer_quiesce(const uint64_t* own_full, int stages, int issued,
+                                                 volatile int* abort, int* err, int where) {
+  for (int s = 0; s < stages && s < issued; ++s) {
+    const uint32_t last_round = (uint32_t)((issued - 1 - s) / stages);
+    mbar_wait(smem_u32(&own_full[s]), last_round & 1u, abort, err, where, false);
   }
 }
 
