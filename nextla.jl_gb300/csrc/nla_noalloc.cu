@@ -17,7 +17,10 @@
 // previous call's contents: the staging kernels write every byte they read
 // (exponents and bounds are cleared with cudaMemsetAsync first), and calls
 // whose executions overlap on the GPU (different streams, or different host
-// threads without ordering) race on it.
+// threads without ordering) race on it.  The cached address belongs to the
+// device's context at the first call: resetting the device (cudaDeviceReset)
+// after that is not supported, as for the library's other per-device state
+// (the copy streams of the host-buffer entry points).
 #include <mutex>
 
 #include "nla_common.cuh"

@@ -39,7 +39,10 @@ def test_noalloc_matches_allocating_update(lib, cuda, lowp, terms):
     import torch
 
     g = torch.Generator(device=cuda).manual_seed(7 + terms)
-    for (N, R, M) in [(300, 257, 129), (640, 512, 384)]:  # two calls in a row, different shapes
+    # Calls in a row with different shapes; the last has R <= 256, which
+    # stages both operands in one fused kernel that writes every byte it reads
+    # from the array, right after a larger call has left its contents there.
+    for (N, R, M) in [(300, 257, 129), (640, 512, 384), (300, 200, 129)]:
         A = _col_major(torch.randn(N, R, generator=g, device=cuda, dtype=torch.float64))
         B = _col_major(torch.randn(R, M, generator=g, device=cuda, dtype=torch.float64))
         C0 = _col_major(torch.randn(N, M, generator=g, device=cuda, dtype=torch.float64))
