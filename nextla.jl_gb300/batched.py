@@ -30,11 +30,15 @@ class BatchPlan:
     """Plan for solving op(A_i) X_i = alpha B_i, i = 1..count (side 'L').
 
     ``systems`` is a sequence of (n, m, a_off, lda, b_off, ldb) with offsets
-    in elements into the A and B pools.  ``cols_per_item`` gives, per size
-    bucket, how many right-hand sides one work item solves (8, 16 or 32);
-    None uses the library defaults (see :mod:`tune` for tuned values)."""
+    in elements into the A and B pools.  The plan runs unified_rec's recursion
+    (src/rectrxm.jl:101-198) for each system on the host and uploads its
+    leaves and update tiles as a node queue.  Per size bucket, ``cutoff``
+    gives the leaf order (16, 32 or 64) and ``cols`` the widest block of
+    right-hand sides (16, 32, 64 or 128); ``cols_per_item`` is an older name
+    for ``cols``.  None takes the library defaults (see :mod:`tune` for tuned
+    values)."""
 
-    def __init__(self, dtype, uplo, trans, systems, cols_per_item=None):
+    def __init__(self, dtype, uplo, trans, systems, cols_per_item=None, *, cutoff=None, cols=None):
         import torch
 
         self.dtype = dtype
@@ -42,17 +46,23 @@ class BatchPlan:
         arr = (_lib.BatchDesc * max(len(systems), 1))()
         for i, s in enumerate(systems):
             arr[i] = _lib.BatchDesc(*[int(v) for v in s])
-        cw = None
-        if cols_per_item is not None:
-            cw = (ctypes.c_int * _lib.NLA_BATCH_BUCKETS)(*[int(c) for c in cols_per_item])
+        cols = cols if cols is not None else cols_per_item
         self._plan = ctypes.c_void_p()
         L = _lib.load()
-        _lib.check(L.nla_batch_plan_create(ctypes.byref(self._plan), code, _lib.ch(uplo), _lib.ch(trans),
-                                           len(systems), arr, cw))
+        if cutoff is None and cols is None:
+            _lib.check(L.nla_batch_plan_create(ctypes.byref(self._plan), code, _lib.ch(uplo), _lib.ch(trans),
+                                               len(systems), arr, None))
+        else:
+            t = _lib.BatchTuning()
+            for b in range(_lib.NLA_BATCH_BUCKETS):
+                t.cutoff[b] = int(cutoff[b]) if cutoff is not None else 64
+                t.cols[b] = int(cols[b]) if cols is not None else (64 if code == _lib.NLA_F64 else 128)
+            _lib.check(L.nla_batch_plan_create_tuned(ctypes.byref(self._plan), code, _lib.ch(uplo),
+                                                     _lib.ch(trans), len(systems), arr, ctypes.byref(t)))
         self.count = len(systems)
 
     def info(self):
-        """(work items, persistent CTAs, total n^2 m flops)."""
+        """(queued nodes, persistent CTAs, total n^2 m flops)."""
         items, grid, flops = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
         _lib.check(_lib.load().nla_batch_plan_info(self._plan, ctypes.byref(items), ctypes.byref(grid),
                                                    ctypes.byref(flops)))

@@ -1,43 +1,578 @@
 // Batched solve of many independent, unevenly sized triangular systems
-// op(A_i) X_i = alpha B_i (side L) in one persistent launch.
+// op(A_i) X_i = alpha B_i (side L) in one persistent launch, as a device
+// queue of recursion nodes.
 //
 // The reference solves one system per unified_rectrxm! call
-// (src/rectrxm.jl:43-76); a batch of thousands of small systems then costs
-// thousands of recursions and launches.  Here a plan turns the batch into
-// work items, one per (system, block of right-hand sides), sorted by cost
-// (largest first); a persistent kernel of one warp-group CTA per SM slot
-// pulls items from a device counter and solves each with the diagonal-block
-// solver of nla_leaf.cuh (systems are at most 1024, the base case's limit).
-// Items are independent, so no CTA ever waits on another.  The number of
-// right-hand sides per item is chosen per size bucket (tuned by the host
-// side and passed in).  The counter reset and the kernel are captured once
-// into a CUDA graph and replayed.
+// (src/rectrxm.jl:43-76), recursing in unified_rec (src/rectrxm.jl:101-198):
+// split at mid (:129-133), solve the half that goes first, update the other
+// half with one GEMM (:162-194), solve it.  Here the plan runs that recursion
+// on the host for every system (and block of right-hand sides, a "group"),
+// down to leaves of at most `cutoff` rows, and records its pieces as nodes:
+//   LEAF    solve one diagonal block of a group in place;
+//   UPDATE  one GEMM tile of the recursion: the rows of one leaf, minus the
+//           product of their A block over the K range of the half solved
+//           first with the solution of that half.
+// Nodes of one group depend on each other exactly as the recursion orders
+// them; nodes of different groups are independent.  The plan orders all
+// nodes by a list-scheduling simulation over the persistent CTAs (largest
+// critical path first), so the updates of one large system spread over many
+// CTAs while small systems fill the gaps, and uploads them once.
+//
+// One persistent kernel (CTAs = SMs x resident CTAs per SM) pulls nodes in
+// that order from a device counter.  Before a node runs, its CTA waits for
+// its dependencies on two kinds of counters, bounded by %globaltimer:
+//   solved[g]       leaves of group g solved so far (leaves finish in order:
+//                   a leaf's last update needs every earlier leaf);
+//   applied[leaf]   updates applied to a leaf's rows so far (the updates of
+//                   one leaf run in the recursion's order, outermost first,
+//                   and the leaf runs after all of them).
+// The queue order is a topological order of the dependencies and every CTA
+// that holds a node is resident, so the waits always end; a wait that runs
+// past the limit records an error word (read by nla_device_status) and the
+// kernel stops taking nodes.  The counter reset and the kernel are captured
+// into a CUDA graph once and replayed.
+//
+// Alpha is applied where a row of B is first read: by the outermost update
+// of each leaf, or by the leaf itself when no update reaches it (the first
+// leaf), as alpha * B rounded to the element type (src/rectrxm.jl:64).
 #include <algorithm>
 #include <mutex>
+#include <queue>
 #include <vector>
 
-#include "nla_leaf.cuh"
+#include "nla_common.cuh"
 
+namespace nla {
+namespace bat {
+
+constexpr int NT = 256;          // threads per CTA
+constexpr int MAX_ROWS = 64;     // largest leaf (and update-tile height)
+constexpr int ROW_GROUPS = 16;   // 16 row groups x 16 column groups of threads
+constexpr int RT = 4;            // rows per thread (strided by ROW_GROUPS)
+constexpr int PANEL = 16;        // triangle panel of a leaf
+constexpr int LEAF_PAD = 1;      // row padding of the staged diagonal block
+
+enum { NODE_LEAF = 0, NODE_UPDATE = 1 };
+enum { FLAG_ALPHA = 1 };
+
+struct Node {
+  int group;
+  int r0, rows;      // canonical rows of the target leaf
+  int k0, kw;        // UPDATE: canonical K range
+  int leaf;          // target leaf (index within the group)
+  int wait_solved;   // solved leaves of the group needed first
+  short wait_applied;  // updates applied to the target leaf needed first
+  unsigned char kind, flags;
+};
+static_assert(sizeof(Node) == 32, "node layout");
+
+struct Group {
+  int sys;
+  int c0, ncols;  // block of right-hand sides
+  int w;          // column template: 16, 32, 64 or 128
+  int leaf_base;  // first applied[] counter of the group
+  int n;
+};
+
+struct Args {
+  const nla_batch_desc* descs;
+  const Group* groups;
+  const Node* nodes;
+  int nnodes;
+  int* next;       // queue head
+  int* solved;     // per group
+  int* applied;    // per leaf
+  int* abort;      // set when a wait gave up: the CTAs stop taking nodes (reset per launch)
+  int* err;        // sticky error word: site of the first wait that gave up
+  const void* A;
+  void* B;
+  int tA, rev;
+  double alpha;
+  uint64_t limit_ns;
+};
+
+__device__ int g_batch_error = 0;
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void add_release(int* p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Waits until *p >= target; false if the limit passed (the error word and
+// the abort flag are then set) or another CTA has already aborted.
+__device__ bool wait_geq(const int* p, int target, const Args& a, int where) {
+  if (ld_acquire(p) >= target) return true;
+  const uint64_t t0 = globaltimer();
+  unsigned ns = 32;
+  for (;;) {
+    __nanosleep(ns);
+    if (ns < 1024) ns *= 2;
+    if (ld_acquire(p) >= target) return true;
+    if (*(volatile int*)a.abort) return false;
+    if (globaltimer() - t0 > a.limit_ns) {
+      atomicCAS(a.err, 0, where);
+      atomicExch(a.abort, 1);
+      return false;
+    }
+  }
+}
+
+// Loads of the B pool go through L2 (another CTA may have written the rows
+// since this SM last cached them); A is read-only.
+template <typename T> __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
+template <> __device__ __forceinline__ __half ldcg<__half>(const __half* p) {
+  return __ushort_as_half(__ldcg(reinterpret_cast<const unsigned short*>(p)));
+}
+__device__ __forceinline__ double to_c(double v) { return v; }
+__device__ __forceinline__ float to_c(float v) { return v; }
+__device__ __forceinline__ float to_c(__half v) { return __half2float(v); }
+
+// alpha * b formed in Float64 and rounded to the element type, as
+// B .= alpha .* B does (src/rectrxm.jl:64).
+template <typename T> __device__ __forceinline__ typename Elem<T>::compute scaled(T b, double alpha);
+template <> __device__ __forceinline__ double scaled<double>(double b, double alpha) { return alpha * b; }
+template <> __device__ __forceinline__ float scaled<float>(float b, double alpha) { return (float)(alpha * (double)b); }
+template <> __device__ __forceinline__ float scaled<__half>(__half b, double alpha) {
+  return __half2float(__double2half(alpha * (double)__half2float(b)));
+}
+
+// Element offsets in canonical coordinates: row i / column k of the lower
+// triangle applied from the left (rev maps i -> n - 1 - i; tA reads A's
+// transpose).
+__device__ __forceinline__ int64_t a_at(const nla_batch_desc& d, int tA, int rev, int i, int k) {
+  const int64_t r = rev ? d.n - 1 - i : i, c = rev ? d.n - 1 - k : k;
+  return d.a_off + (tA ? c + r * d.lda : r + c * d.lda);
+}
+__device__ __forceinline__ int64_t b_at(const nla_batch_desc& d, int rev, int i, int64_t col) {
+  const int64_t r = rev ? d.n - 1 - i : i;
+  return d.b_off + r + col * d.ldb;
+}
+
+// Shared-memory footprint (compute-type elements) of a node of width W.
+__host__ __device__ constexpr int kc_of(int esz) { return esz == 8 ? 16 : 32; }
+__host__ __device__ constexpr size_t update_elems(int W, int kc) {
+  return (size_t)kc * (MAX_ROWS + 4) + (size_t)kc * (W + 4);
+}
+__host__ __device__ constexpr size_t leaf_elems(int W) {
+  return (size_t)MAX_ROWS * (MAX_ROWS + LEAF_PAD) + (size_t)MAX_ROWS * (W + 4) + MAX_ROWS;
+}
+
+// ---------------------------------------------------------------------------
+// UPDATE: X[r0 + r, c] = base(r, c) - sum_k A[r0 + r, k0 + k] X[k0 + k, c] for
+// r < rows, c < ncols, base = alpha B (first touch) or B.  Thread (tr, tc)
+// owns rows tr + 16 i (i < 4) and columns tc * CT .. + CT.  K is walked in
+// chunks of KC staged in shared memory (A k-major, X k-major), the next
+// chunk's elements prefetched into registers during the current chunk.
+// ---------------------------------------------------------------------------
+template <typename T, int W>
+__device__ void run_update(const Args& a, const Node& nd, const Group& g, const nla_batch_desc& d, void* smem) {
+  using Tc = typename Elem<T>::compute;
+  constexpr int KC = kc_of(sizeof(Tc));
+  constexpr int CT = W / 16;
+  constexpr int AP = MAX_ROWS + 4, XP = W + 4;
+  constexpr int A_PER = MAX_ROWS * KC / NT, X_PER = KC * W / NT;
+  Tc* As = static_cast<Tc*>(smem);  // [KC][AP]
+  Tc* Xs = As + KC * AP;             // [KC][XP]
+  const T* A = static_cast<const T*>(a.A);
+  const T* B = static_cast<const T*>(a.B);
+  const int t = threadIdx.x, tr = t % ROW_GROUPS, tc = t / ROW_GROUPS;
+  const int rows = nd.rows, ncols = g.ncols;
+
+  Tc acc[RT][CT];
+#pragma unroll
+  for (int i = 0; i < RT; ++i)
+#pragma unroll
+    for (int c = 0; c < CT; ++c) acc[i][c] = Tc(0);
+
+  Tc pa[A_PER], px[X_PER];
+  auto fetch = [&](int k0) {
+    const int kw = min(KC, nd.k0 + nd.kw - k0);
+#pragma unroll
+    for (int u = 0; u < A_PER; ++u) {
+      const int idx = t + u * NT;
+      int r, k;
+      if (!a.tA) { r = idx % MAX_ROWS; k = idx / MAX_ROWS; }
+      else { k = idx % KC; r = idx / KC; }
+      pa[u] = r < rows && k < kw ? to_c(A[a_at(d, a.tA, a.rev, nd.r0 + r, k0 + k)]) : Tc(0);
+    }
+#pragma unroll
+    for (int u = 0; u < X_PER; ++u) {
+      const int idx = t + u * NT;
+      const int k = idx % KC, c = idx / KC;
+      px[u] = k < kw && c < ncols ? to_c(ldcg(B + b_at(d, a.rev, k0 + k, g.c0 + c))) : Tc(0);
+    }
+  };
+  auto stash = [&]() {
+#pragma unroll
+    for (int u = 0; u < A_PER; ++u) {
+      const int idx = t + u * NT;
+      int r, k;
+      if (!a.tA) { r = idx % MAX_ROWS; k = idx / MAX_ROWS; }
+      else { k = idx % KC; r = idx / KC; }
+      As[k * AP + r] = pa[u];
+    }
+#pragma unroll
+    for (int u = 0; u < X_PER; ++u) {
+      const int idx = t + u * NT;
+      Xs[(idx % KC) * XP + idx / KC] = px[u];
+    }
+  };
+
+  const int kend = nd.k0 + nd.kw;
+  fetch(nd.k0);
+  for (int k0 = nd.k0; k0 < kend; k0 += KC) {
+    __syncthreads();  // the previous chunk is no longer read
+    stash();
+    __syncthreads();
+    if (k0 + KC < kend) fetch(k0 + KC);
+    const int kw = min(KC, kend - k0);
+#pragma unroll 4
+    for (int k = 0; k < kw; ++k) {
+      Tc av[RT], xv[CT];
+#pragma unroll
+      for (int i = 0; i < RT; ++i) av[i] = As[k * AP + tr + ROW_GROUPS * i];
+#pragma unroll
+      for (int c = 0; c < CT; ++c) xv[c] = Xs[k * XP + tc * CT + c];
+#pragma unroll
+      for (int i = 0; i < RT; ++i)
+#pragma unroll
+        for (int c = 0; c < CT; ++c) acc[i][c] = fma(av[i], xv[c], acc[i][c]);
+    }
+  }
+  T* Bw = static_cast<T*>(a.B);
+  const bool first = nd.flags & FLAG_ALPHA;
+#pragma unroll
+  for (int i = 0; i < RT; ++i) {
+    const int r = tr + ROW_GROUPS * i;
+    if (r >= rows) continue;
+#pragma unroll
+    for (int c = 0; c < CT; ++c) {
+      const int col = tc * CT + c;
+      if (col >= ncols) continue;
+      const int64_t o = b_at(d, a.rev, nd.r0 + r, g.c0 + col);
+      const T b = ldcg(B + o);
+      const Tc base = first ? scaled<T>(b, a.alpha) : to_c(b);
+      Elem<T>::store(Bw + o, base - acc[i][c]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// LEAF: solve the diagonal block rows r0 .. r0 + rows (at most 64) in place.
+// The block of A (lower, with the diagonal's reciprocals) and of X are staged
+// in shared memory; 16-row panels are solved one right-hand side per thread
+// (the panel's values in registers), and each panel's rows below it are then
+// updated with the register-tiled product.
+// ---------------------------------------------------------------------------
+template <typename T, int W>
+__device__ void run_leaf(const Args& a, const Node& nd, const Group& g, const nla_batch_desc& d, void* smem) {
+  using Tc = typename Elem<T>::compute;
+  constexpr int LP = MAX_ROWS + LEAF_PAD, XP = W + 4, CT = W / 16;
+  Tc* Ls = static_cast<Tc*>(smem);    // [64][LP]: Ls[r][k], k < r, of the block
+  Tc* Xs = Ls + MAX_ROWS * LP;        // [64][XP]
+  Tc* inv = Xs + MAX_ROWS * XP;       // [64]
+  const T* A = static_cast<const T*>(a.A);
+  T* B = static_cast<T*>(a.B);
+  const int t = threadIdx.x, rows = nd.rows, ncols = g.ncols;
+  const bool first = nd.flags & FLAG_ALPHA;
+
+  // Stage the block of A (threads along the index contiguous in memory) and X.
+  for (int idx = t; idx < rows * rows; idx += NT) {
+    int r, k;
+    if (!a.tA) { r = idx % rows; k = idx / rows; }
+    else { k = idx % rows; r = idx / rows; }
+    if (k < r) Ls[r * LP + k] = to_c(A[a_at(d, a.tA, a.rev, nd.r0 + r, nd.r0 + k)]);
+    else if (k == r) inv[r] = Tc(1) / to_c(A[a_at(d, a.tA, a.rev, nd.r0 + r, nd.r0 + r)]);
+  }
+  for (int idx = t; idx < rows * W; idx += NT) {
+    const int r = idx % rows, c = idx / rows;
+    Tc v = Tc(0);
+    if (c < ncols) {
+      const T b = ldcg(B + b_at(d, a.rev, nd.r0 + r, g.c0 + c));
+      v = first ? scaled<T>(b, a.alpha) : to_c(b);
+    }
+    Xs[r * XP + c] = v;
+  }
+  __syncthreads();
+
+  const int tr = t % ROW_GROUPS, tc = t / ROW_GROUPS;
+  for (int p0 = 0; p0 < rows; p0 += PANEL) {
+    const int pw = min(PANEL, rows - p0);
+    // The panel's triangle: one right-hand side per thread.
+    if (t < W) {
+      Tc x[PANEL];
+#pragma unroll
+      for (int i = 0; i < PANEL; ++i) {
+        if (i < pw) {
+          Tc y = Xs[(p0 + i) * XP + t];
+#pragma unroll
+          for (int j = 0; j < i; ++j) y = fma(-Ls[(p0 + i) * LP + p0 + j], x[j], y);
+          y *= inv[p0 + i];
+          x[i] = y;
+          Xs[(p0 + i) * XP + t] = y;
+        }
+      }
+    }
+    __syncthreads();
+    // Rows below the panel: X[r, :] -= L[r, panel] X[panel, :].
+    const int rb = p0 + pw;
+    if (rb < rows) {
+      Tc acc[RT][CT];
+#pragma unroll
+      for (int i = 0; i < RT; ++i)
+#pragma unroll
+        for (int c = 0; c < CT; ++c) acc[i][c] = Tc(0);
+      for (int k = 0; k < pw; ++k) {
+        Tc xv[CT];
+#pragma unroll
+        for (int c = 0; c < CT; ++c) xv[c] = Xs[(p0 + k) * XP + tc * CT + c];
+#pragma unroll
+        for (int i = 0; i < RT; ++i) {
+          const int r = rb + tr + ROW_GROUPS * i;
+          const Tc av = r < rows ? Ls[r * LP + p0 + k] : Tc(0);
+#pragma unroll
+          for (int c = 0; c < CT; ++c) acc[i][c] = fma(av, xv[c], acc[i][c]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < RT; ++i) {
+        const int r = rb + tr + ROW_GROUPS * i;
+        if (r < rows) {
+#pragma unroll
+          for (int c = 0; c < CT; ++c) Xs[r * XP + tc * CT + c] -= acc[i][c];
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int idx = t; idx < rows * W; idx += NT) {
+    const int r = idx % rows, c = idx / rows;
+    if (c < ncols) Elem<T>::store(B + b_at(d, a.rev, nd.r0 + r, g.c0 + c), Xs[r * XP + c]);
+  }
+}
+
+template <typename T, int W>
+__device__ __forceinline__ void run_node(const Args& a, const Node& nd, const Group& g, const nla_batch_desc& d,
+                                         void* smem) {
+  if (nd.kind == NODE_LEAF) run_leaf<T, W>(a, nd, g, d, smem);
+  else run_update<T, W>(a, nd, g, d, smem);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT, 2) batched_node_kernel(Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_idx;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      int idx = atomicAdd(a.next, 1);
+      if (idx < a.nnodes) {
+        const Node nd = a.nodes[idx];
+        bool ok = *(volatile int*)a.abort == 0;
+        if (ok && nd.kind == NODE_UPDATE && nd.wait_solved > 0)
+          ok = wait_geq(a.solved + nd.group, nd.wait_solved, a, 1);
+        if (ok && nd.wait_applied > 0)
+          ok = wait_geq(a.applied + a.groups[nd.group].leaf_base + nd.leaf, nd.wait_applied, a, 2);
+        if (!ok) idx = a.nnodes;  // stop: a dependency did not arrive in time
+      }
+      s_idx = idx;
+    }
+    __syncthreads();
+    const int idx = s_idx;
+    if (idx >= a.nnodes) break;
+    const Node nd = a.nodes[idx];
+    const Group g = a.groups[nd.group];
+    const nla_batch_desc d = a.descs[g.sys];
+    // Float64 groups are at most 64 wide (the plan splits wider blocks): a
+    // 128-wide Float64 tile would not fit the register budget of two CTAs
+    // per SM, and the FP64 pipe is saturated at 64.
+    switch (g.w) {
+      case 16: run_node<T, 16>(a, nd, g, d, smem_raw); break;
+      case 32: run_node<T, 32>(a, nd, g, d, smem_raw); break;
+      case 64: run_node<T, 64>(a, nd, g, d, smem_raw); break;
+      default:
+        if constexpr (sizeof(typename Elem<T>::compute) == 4) run_node<T, 128>(a, nd, g, d, smem_raw);
+        break;
+    }
+    __syncthreads();  // every thread's stores of this node are issued
+    if (threadIdx.x == 0) {
+      __threadfence();
+      if (nd.kind == NODE_LEAF) add_release(a.solved + nd.group, 1);
+      else add_release(a.applied + g.leaf_base + nd.leaf, 1);
+    }
+  }
+}
+
+size_t node_smem_bytes(int dtype, int w_max) {
+  const int esz = dtype == NLA_F64 ? 8 : 4;
+  return std::max(update_elems(w_max, kc_of(esz)), leaf_elems(w_max)) * esz;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision batch (Float32 solves, Float64 residuals), on the plan's
+// groups: one CTA per group (map) or per (group, 64-row band) (residual).
+// ---------------------------------------------------------------------------
+enum MapOp { MAP_INIT = 0, MAP_SET = 1, MAP_ADD = 2 };
+
+struct MapArgs {
+  const nla_batch_desc* descs;
+  const Group* groups;
+  const double* A64;
+  float* A32;
+  double* B64;
+  double* R64;
+  float* X32;
+  double alpha;
+  int op;
+};
+
+// MAP_INIT: R = alpha B (Float64), X32 = (float) R, and (first group of each
+// system) A32 = (float) A over the n x n block; MAP_SET: B = (double) X32;
+// MAP_ADD: B += (double) X32.
+__global__ void __launch_bounds__(256) batched_map_kernel(MapArgs a) {
+  const Group g = a.groups[blockIdx.x];
+  const nla_batch_desc d = a.descs[g.sys];
+  const int n = (int)d.n;
+  const int total = n * g.ncols;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int64_t o = d.b_off + (int64_t)(idx % n) + (int64_t)(g.c0 + idx / n) * d.ldb;
+    if (a.op == MAP_INIT) {
+      const double r = a.alpha * a.B64[o];
+      a.R64[o] = r;
+      a.X32[o] = (float)r;
+    } else if (a.op == MAP_SET) {
+      a.B64[o] = (double)a.X32[o];
+    } else {
+      a.B64[o] += (double)a.X32[o];
+    }
+  }
+  if (a.op == MAP_INIT && g.c0 == 0) {
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+      const int64_t o = d.a_off + (int64_t)(idx % n) + (int64_t)(idx / n) * d.lda;
+      a.A32[o] = (float)a.A64[o];
+    }
+  }
+}
+
+struct ResidualArgs {
+  const nla_batch_desc* descs;
+  const Group* groups;
+  const double* A64;
+  const double* X64;  // current solution (the caller's B pool)
+  const double* R64;  // alpha B
+  float* D32;         // out: the residual, rounded to Float32
+  int tA, rev;
+};
+
+// D32 = (float)(R - L X) on one 64-row band of a group, L the canonical lower
+// triangle (diagonal included) of op(A), summed in Float64 with the
+// register-tiled product of the UPDATE nodes.
+template <int W>
+__device__ void residual_band(const ResidualArgs& a, const Group& g, const nla_batch_desc& d, int r0, double* smem) {
+  constexpr int KC = 16, CT = W / 16, AP = MAX_ROWS + 4, XP = W + 4;
+  double* As = smem;
+  double* Xs = smem + KC * AP;
+  const int t = threadIdx.x, tr = t % ROW_GROUPS, tc = t / ROW_GROUPS;
+  const int rows = min(MAX_ROWS, (int)d.n - r0), ncols = g.ncols;
+  const int kend = r0 + rows;  // k <= r
+  double acc[RT][CT];
+#pragma unroll
+  for (int i = 0; i < RT; ++i)
+#pragma unroll
+    for (int c = 0; c < CT; ++c) acc[i][c] = 0.0;
+  for (int k0 = 0; k0 < kend; k0 += KC) {
+    const int kw = min(KC, kend - k0);
+    __syncthreads();
+    for (int idx = t; idx < MAX_ROWS * KC; idx += NT) {
+      int r, k;
+      if (!a.tA) { r = idx % MAX_ROWS; k = idx / MAX_ROWS; }
+      else { k = idx % KC; r = idx / KC; }
+      As[k * AP + r] = r < rows && k < kw && k0 + k <= r0 + r ? a.A64[a_at(d, a.tA, a.rev, r0 + r, k0 + k)] : 0.0;
+    }
+    for (int idx = t; idx < KC * W; idx += NT) {
+      const int k = idx % KC, c = idx / KC;
+      Xs[k * XP + c] = k < kw && c < ncols ? a.X64[b_at(d, a.rev, k0 + k, g.c0 + c)] : 0.0;
+    }
+    __syncthreads();
+    for (int k = 0; k < kw; ++k) {
+      double av[RT], xv[CT];
+#pragma unroll
+      for (int i = 0; i < RT; ++i) av[i] = As[k * AP + tr + ROW_GROUPS * i];
+#pragma unroll
+      for (int c = 0; c < CT; ++c) xv[c] = Xs[k * XP + tc * CT + c];
+#pragma unroll
+      for (int i = 0; i < RT; ++i)
+#pragma unroll
+        for (int c = 0; c < CT; ++c) acc[i][c] = fma(av[i], xv[c], acc[i][c]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < RT; ++i) {
+    const int r = tr + ROW_GROUPS * i;
+    if (r >= rows) continue;
+#pragma unroll
+    for (int c = 0; c < CT; ++c) {
+      const int col = tc * CT + c;
+      if (col < ncols) {
+        const int64_t o = b_at(d, a.rev, r0 + r, g.c0 + col);
+        a.D32[o] = (float)(a.R64[o] - acc[i][c]);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(NT) batched_residual_kernel(ResidualArgs a) {
+  __shared__ __align__(16) double smem[16 * (MAX_ROWS + 4) + 16 * (128 + 4)];
+  const Group g = a.groups[blockIdx.x];
+  const nla_batch_desc d = a.descs[g.sys];
+  const int r0 = (int)blockIdx.y * MAX_ROWS;
+  if (r0 >= d.n) return;
+  switch (g.w) {
+    case 16: residual_band<16>(a, g, d, r0, smem); break;
+    case 32: residual_band<32>(a, g, d, r0, smem); break;
+    case 64: residual_band<64>(a, g, d, r0, smem); break;
+    default: residual_band<128>(a, g, d, r0, smem); break;
+  }
+}
+
+}  // namespace bat
+}  // namespace nla
+
+// ---------------------------------------------------------------------------
+// Host side: the plan.
+// ---------------------------------------------------------------------------
 struct nla_batch_plan_s {
   int dtype;
   int tA, rev;
   int64_t count;
-  int nitems;
+  std::vector<nla_batch_desc> h_descs;
+  int ngroups, nleaves, nnodes;
   int n_max;
-  int cw_max;
+  int w_max;
   size_t smem;
   int grid;
+  double flops;
   void* d_descs;
-  void* d_items;
-  int* d_counter;
-  std::vector<nla_batch_desc> h_descs;
-  // Graph cache (valid for one alpha / pool pair).
+  void* d_groups;
+  void* d_nodes;
+  int* d_counters;  // next, abort, then solved[ngroups], then applied[nleaves]
+  size_t counter_bytes;
   cudaStream_t cap_stream;
   cudaGraphExec_t exec;
   double g_alpha;
   const void* g_A;
   void* g_B;
-  double flops;
+  uint64_t g_limit;
   // Mixed-precision form (Float64 plans): pool extents in elements and the
   // plan-owned Float32 pools and Float64 residual buffer (allocated on first
   // use).
@@ -50,194 +585,8 @@ struct nla_batch_plan_s {
 namespace nla {
 namespace {
 
-using namespace leafdev;
-
-struct BatchItem {
-  int sys;
-  int c0;
-  int cw;
-  int pad;
-};
-
-struct BatchArgs {
-  const nla_batch_desc* descs;
-  const BatchItem* items;
-  int nitems;
-  int* counter;
-  const void* A;
-  void* B;
-  int tA, rev;
-  double alpha;
-};
-
-template <typename T>
-__global__ void __launch_bounds__(LEAF_THREADS) batched_solve_kernel(BatchArgs a) {
-  using Tc = typename Elem<T>::compute;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ int s_item;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
-    __syncthreads();
-    const int it = s_item;
-    __syncthreads();
-    if (it >= a.nitems) break;
-    const BatchItem w = a.items[it];
-    const nla_batch_desc d = a.descs[w.sys];
-    LeafArgs g;
-    g.A = static_cast<const T*>(a.A) + d.a_off;
-    g.lda = d.lda;
-    g.tA = a.tA;
-    g.B = static_cast<T*>(a.B) + d.b_off;
-    g.ldb = d.ldb;
-    g.tB = 0;
-    g.rev = a.rev;
-    g.unit = 0;
-    g.n = (int)d.n;
-    g.m = d.m;
-    const int ncols = (int)(d.m - w.c0 < w.cw ? d.m - w.c0 : w.cw);
-    const Tc al = (Tc)a.alpha;
-    if (w.cw == 8) solve_block<T, 8>(g, w.c0, ncols, smem_raw, al);
-    else if (w.cw == 16) solve_block<T, 16>(g, w.c0, ncols, smem_raw, al);
-    else solve_block<T, 32>(g, w.c0, ncols, smem_raw, al);
-    __syncthreads();
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Mixed-precision batch (Float32 solves, Float64 residuals).  Every kernel
-// below works on the plan's items, one CTA per item, so only the systems'
-// own elements of the caller's pools are read or written.
-// ---------------------------------------------------------------------------
-enum MapOp { MAP_INIT = 0, MAP_SET = 1, MAP_ADD = 2 };
-
-struct MapArgs {
-  const nla_batch_desc* descs;
-  const BatchItem* items;
-  const double* A64;
-  float* A32;
-  double* B64;
-  double* R64;
-  float* X32;
-  double alpha;
-  int op;
-};
-
-// MAP_INIT: R = alpha B (Float64), X32 = (float) R, and (first item of each
-// system) A32 = (float) A over the n x n block; MAP_SET: B = (double) X32;
-// MAP_ADD: B += (double) X32.  Elements are the item's n x ncols block.
-__global__ void __launch_bounds__(256) batched_map_kernel(MapArgs a) {
-  const BatchItem w = a.items[blockIdx.x];
-  const nla_batch_desc d = a.descs[w.sys];
-  const int n = (int)d.n;
-  const int ncols = (int)(d.m - w.c0 < w.cw ? d.m - w.c0 : w.cw);
-  const int total = n * ncols;
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int64_t o = d.b_off + (int64_t)(idx % n) + (int64_t)(w.c0 + idx / n) * d.ldb;
-    if (a.op == MAP_INIT) {
-      const double r = a.alpha * a.B64[o];
-      a.R64[o] = r;
-      a.X32[o] = (float)r;
-    } else if (a.op == MAP_SET) {
-      a.B64[o] = (double)a.X32[o];
-    } else {
-      a.B64[o] += (double)a.X32[o];
-    }
-  }
-  if (a.op == MAP_INIT && w.c0 == 0) {
-    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-      const int64_t o = d.a_off + (int64_t)(idx % n) + (int64_t)(idx / n) * d.lda;
-      a.A32[o] = (float)a.A64[o];
-    }
-  }
-}
-
-struct ResidualArgs {
-  const nla_batch_desc* descs;
-  const BatchItem* items;
-  const double* A64;
-  const double* X64;  // current solution (the caller's B pool)
-  const double* R64;  // alpha B
-  float* D32;         // out: the residual, rounded to Float32
-  int tA, rev;
-};
-
-// D32 = (float)(R - L X) on one 128-row band of an item's n x ncols block,
-// L the canonical lower triangle (diagonal included) of op(A).  A band is
-// its own CTA (blockIdx.y), and the X rows it needs are streamed through
-// shared memory 32 at a time, so a CTA holds about 45 KB and several run per
-// SM (the update is bound by the 2-FMA-per-clock DFMA rate, and one CTA per
-// SM leaves it waiting on shared memory).  Each panel is formed with the
-// register-tiled product of the diagonal-block kernels, summing in Float64.
-constexpr int RES_PANEL_ELEMS = PANEL * 32 + LEAF_THREADS * SLAB_PAD;  // X panel (CW <= 32) + slab
-
-template <int CW>
-__device__ __forceinline__ void residual_band(const ResidualArgs& a, const BatchItem& w, const nla_batch_desc& d,
-                                              int r0, double* smem) {
-  LeafArgs g;
-  g.A = a.A64 + d.a_off;
-  g.lda = d.lda;
-  g.tA = a.tA;
-  g.B = const_cast<double*>(a.X64) + d.b_off;
-  g.ldb = d.ldb;
-  g.tB = 0;
-  g.rev = a.rev;
-  g.unit = 0;
-  g.n = (int)d.n;
-  g.m = d.m;
-  const int ncols = (int)(d.m - w.c0 < CW ? d.m - w.c0 : CW);
-  const int rows = min(LEAF_THREADS, g.n - r0);
-  const int kmax = r0 + rows;  // k <= r
-  double* Xs = smem;                 // PANEL x CW
-  double* slab = smem + PANEL * 32;  // 128 x 33
-  constexpr int CT = CW / 4;
-  const int tr = threadIdx.x & 31, tc = threadIdx.x >> 5;
-  double acc[4][CT];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int c = 0; c < CT; ++c) acc[i][c] = 0.0;
-  const double* X = a.X64 + d.b_off;
-  for (int k0 = 0; k0 < kmax; k0 += PANEL) {
-    const int kw = min(PANEL, kmax - k0);
-    // X rows k0 .. k0 + kw of the item's columns (threads along the rows,
-    // which are contiguous in memory).
-    for (int idx = threadIdx.x; idx < PANEL * CW; idx += LEAF_THREADS) {
-      const int k = idx % PANEL, c = idx / PANEL;
-      Xs[k * CW + c] = k < kw && c < ncols ? X[b_off<double>(g, k0 + k, w.c0 + c)] : 0.0;
-    }
-    stage_slab<LEAF_THREADS, double>(g, slab, r0, rows, k0, kw, [](int i, int j) { return j <= i; });
-    __syncthreads();
-    tile_product<double, CW>(slab, Xs, kw, rows, acc);
-    __syncthreads();
-  }
-  const double* R = a.R64 + d.b_off;
-  float* D = a.D32 + d.b_off;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int r = tr + 32 * i;
-    if (r < rows) {
-#pragma unroll
-      for (int c = 0; c < CT; ++c) {
-        const int col = tc * CT + c;
-        if (col < ncols) {
-          const int64_t o = b_off<double>(g, r0 + r, w.c0 + col);
-          D[o] = (float)(R[o] - acc[i][c]);
-        }
-      }
-    }
-  }
-}
-
-__global__ void __launch_bounds__(LEAF_THREADS) batched_residual_kernel(ResidualArgs a) {
-  __shared__ __align__(16) double smem[RES_PANEL_ELEMS];
-  const BatchItem w = a.items[blockIdx.x];
-  const nla_batch_desc d = a.descs[w.sys];
-  const int r0 = (int)blockIdx.y * LEAF_THREADS;
-  if (r0 >= d.n) return;
-  if (w.cw == 8) residual_band<8>(a, w, d, r0, smem);
-  else if (w.cw == 16) residual_band<16>(a, w, d, r0, smem);
-  else residual_band<32>(a, w, d, r0, smem);
-}
+using bat::Group;
+using bat::Node;
 
 int bucket_of(int64_t n) {
   int b = 0;
@@ -249,46 +598,364 @@ int bucket_of(int64_t n) {
   return b;
 }
 
-template <typename T>
-int launch_batched(nla_batch_plan p, double alpha, const void* A, void* B, cudaStream_t s) {
-  BatchArgs a{static_cast<const nla_batch_desc*>(p->d_descs), static_cast<const BatchItem*>(p->d_items), p->nitems,
-              p->d_counter, A, B, p->tA, p->rev, alpha};
-  batched_solve_kernel<T><<<p->grid, LEAF_THREADS, p->smem, s>>>(a);
-  NLA_CHECK_LAUNCH("batched_solve_kernel");
+// Default tuning per size bucket (16 * 2^b <= n < 32 * 2^b), measured on a
+// GB300 with the autotuner (tune.py) and used when the caller passes none.
+void default_tuning(int dtype, nla_batch_tuning* t) {
+  for (int b = 0; b < NLA_BATCH_BUCKETS; ++b) {
+    t->cutoff[b] = 64;
+    t->cols[b] = dtype == NLA_F64 ? 64 : 128;
+  }
+}
+
+int check_tuning(const nla_batch_tuning& t) {
+  for (int b = 0; b < NLA_BATCH_BUCKETS; ++b) {
+    if (t.cutoff[b] != 16 && t.cutoff[b] != 32 && t.cutoff[b] != 64)
+      return fail(NLA_ERR_ARG, "batch tuning: cutoff entries must be 16, 32 or 64");
+    if (t.cols[b] != 16 && t.cols[b] != 32 && t.cols[b] != 64 && t.cols[b] != 128)
+      return fail(NLA_ERR_ARG, "batch tuning: cols entries must be 16, 32, 64 or 128");
+  }
   return NLA_OK;
 }
 
+struct HostNode {
+  Node d;
+  double cost;
+  double prio;
+  int pred[2];  // at most two: the leaf's previous update, the first half's last leaf
+  int npred;
+};
+
+// Relative cost of a node on one CTA (flop-equivalents): the update tiles
+// run near the register-tiled product's rate, the leaves' panel triangles at
+// a fraction of it, and every node pays a fixed start-up (staging, waits).
+double node_cost(const Node& nd, int w) {
+  const double overhead = 40000.0;
+  if (nd.kind == bat::NODE_UPDATE) return overhead + 2.0 * nd.rows * (double)nd.kw * w;
+  return overhead + 3.0 * (double)nd.rows * nd.rows * w;
+}
+
+// The recursion of unified_rec over canonical rows [start, start + len) of
+// one group, emitting leaves and update tiles in the recursion's order.
+// `first` of a node is its split point measured from the end solved first
+// (forward: the reference's mid; backward: len - mid, the reference's
+// second half read in reverse).
+struct GroupBuilder {
+  int gi;
+  int cutoff;
+  bool rev;
+  std::vector<int> leaf_start, leaf_len;  // leaves in solve order
+  std::vector<int> chain;                 // updates so far per leaf
+  std::vector<int> last_node;             // last node touching each leaf
+  std::vector<HostNode>* nodes;
+  int group_w;
+
+  void leaves(int start, int len) {
+    if (len <= cutoff) {
+      leaf_start.push_back(start);
+      leaf_len.push_back(len);
+      return;
+    }
+    const int mid = (int)split_point(len);
+    const int first = rev ? len - mid : mid;
+    leaves(start, first);
+    leaves(start + first, len - first);
+  }
+  int leaf_at(int row) const {
+    return (int)(std::upper_bound(leaf_start.begin(), leaf_start.end(), row) - leaf_start.begin()) - 1;
+  }
+  void link(int from, int to) {
+    if (from < 0) return;
+    HostNode& t = (*nodes)[to];
+    t.pred[t.npred++] = from;
+  }
+  int add(const Node& nd) {
+    HostNode h{};
+    h.d = nd;
+    h.cost = node_cost(nd, group_w);
+    h.npred = 0;
+    nodes->push_back(h);
+    return (int)nodes->size() - 1;
+  }
+  void rec(int start, int len) {
+    if (len <= cutoff) {
+      const int j = leaf_at(start);
+      Node nd{};
+      nd.group = gi;
+      nd.r0 = start;
+      nd.rows = len;
+      nd.leaf = j;
+      nd.kind = bat::NODE_LEAF;
+      nd.flags = chain[j] == 0 ? bat::FLAG_ALPHA : 0;
+      nd.wait_solved = j;
+      nd.wait_applied = (short)chain[j];
+      const int id = add(nd);
+      link(last_node[j], id);
+      last_node[j] = id;
+      return;
+    }
+    const int mid = (int)split_point(len);
+    const int first = rev ? len - mid : mid;
+    rec(start, first);
+    // The update between the halves, one tile per leaf of the second half.
+    const int j_first = leaf_at(start + first);
+    const int last_solved = j_first - 1;  // the first half's last leaf
+    for (int j = j_first; j < (int)leaf_start.size() && leaf_start[j] < start + len; ++j) {
+      Node nd{};
+      nd.group = gi;
+      nd.r0 = leaf_start[j];
+      nd.rows = leaf_len[j];
+      nd.k0 = start;
+      nd.kw = first;
+      nd.leaf = j;
+      nd.kind = bat::NODE_UPDATE;
+      nd.flags = chain[j] == 0 ? bat::FLAG_ALPHA : 0;
+      nd.wait_solved = j_first;
+      nd.wait_applied = (short)chain[j];
+      const int id = add(nd);
+      link(last_node[j], id);            // the leaf's previous update
+      link(last_node[last_solved], id);  // the first half solved (its last leaf)
+      last_node[j] = id;
+      chain[j]++;
+    }
+    rec(start + first, len - first);
+  }
+};
+
+// List scheduling of the nodes over `workers` CTAs: each free worker takes
+// the ready node with the longest remaining path (costs summed to the end of
+// its group); the order nodes start in is the queue order.  It is a
+// topological order, which the persistent kernel relies on.
+std::vector<int> schedule(std::vector<HostNode>& nodes, int workers) {
+  const int N = (int)nodes.size();
+  // Successor lists (CSR) from the predecessors.
+  std::vector<int> first(N + 1, 0), succ;
+  for (int i = 0; i < N; ++i)
+    for (int q = 0; q < nodes[i].npred; ++q) first[nodes[i].pred[q] + 1]++;
+  for (int i = 0; i < N; ++i) first[i + 1] += first[i];
+  succ.resize(first[N]);
+  {
+    std::vector<int> fill(first.begin(), first.end() - 1);
+    for (int i = 0; i < N; ++i)
+      for (int q = 0; q < nodes[i].npred; ++q) succ[fill[nodes[i].pred[q]]++] = i;
+  }
+  // Longest path to the end: predecessors were created before their
+  // successors, so a reverse sweep sees every successor first.
+  std::vector<double> below(N, 0.0);
+  for (int i = N - 1; i >= 0; --i) {
+    nodes[i].prio = nodes[i].cost + below[i];
+    for (int q = 0; q < nodes[i].npred; ++q) below[nodes[i].pred[q]] = std::max(below[nodes[i].pred[q]], nodes[i].prio);
+  }
+  std::vector<int> preds_left(N);
+  std::vector<double> ready_at(N, 0.0);
+  using Ready = std::pair<double, int>;  // (priority, node)
+  std::priority_queue<Ready> ready;
+  using Pending = std::pair<double, int>;  // (ready time, node), earliest first
+  std::priority_queue<Pending, std::vector<Pending>, std::greater<Pending>> pending;
+  for (int i = 0; i < N; ++i) {
+    preds_left[i] = nodes[i].npred;
+    if (preds_left[i] == 0) ready.push({nodes[i].prio, i});
+  }
+  std::priority_queue<double, std::vector<double>, std::greater<double>> free_at;
+  for (int w = 0; w < workers; ++w) free_at.push(0.0);
+  std::vector<int> order;
+  order.reserve(N);
+  while ((int)order.size() < N) {
+    double t = free_at.top();
+    free_at.pop();
+    while (!pending.empty() && pending.top().first <= t) {
+      ready.push({nodes[pending.top().second].prio, pending.top().second});
+      pending.pop();
+    }
+    if (ready.empty()) {
+      // Idle until the next node becomes ready.
+      t = pending.top().first;
+      while (!pending.empty() && pending.top().first <= t) {
+        ready.push({nodes[pending.top().second].prio, pending.top().second});
+        pending.pop();
+      }
+    }
+    const int i = ready.top().second;
+    ready.pop();
+    order.push_back(i);
+    const double fin = t + nodes[i].cost;
+    free_at.push(fin);
+    for (int k = first[i]; k < first[i + 1]; ++k) {
+      const int j = succ[k];
+      ready_at[j] = std::max(ready_at[j], fin);
+      if (--preds_left[j] == 0) pending.push({ready_at[j], j});
+    }
+  }
+  return order;
+}
+
 template <typename T>
-int batched_smem_attr(size_t smem) {
+int node_kernel_setup(size_t smem, int* per_sm) {
   static std::once_flag once;
   static cudaError_t st = cudaSuccess;
   std::call_once(once, [] {
-    st = cudaFuncSetAttribute(batched_solve_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    st = cudaFuncSetAttribute(bat::batched_node_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   });
+  if (st != cudaSuccess) return cuda_status(st, "cudaFuncSetAttribute(batched_node_kernel)");
   if (smem > 200 * 1024) return fail(NLA_ERR_UNSUPPORTED, "batch: shared memory plan too large");
-  return st == cudaSuccess ? NLA_OK : cuda_status(st, "cudaFuncSetAttribute(batched_solve_kernel)");
+  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, bat::batched_node_kernel<T>, bat::NT,
+                                                                      smem);
+  return e == cudaSuccess ? NLA_OK : cuda_status(e, "batch: occupancy query");
 }
 
 template <typename T>
-int occupancy(size_t smem, int* blocks) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, batched_solve_kernel<T>, LEAF_THREADS, smem) ==
-                 cudaSuccess
-             ? NLA_OK
-             : fail(NLA_ERR_UNSUPPORTED, "batch: occupancy query failed");
+int launch_nodes(nla_batch_plan p, double alpha, const void* A, void* B, cudaStream_t s) {
+  int* c = p->d_counters;  // next, abort, solved[ngroups], applied[nleaves]
+  bat::Args a{static_cast<const nla_batch_desc*>(p->d_descs), static_cast<const Group*>(p->d_groups),
+              static_cast<const Node*>(p->d_nodes), p->nnodes, c, c + 2, c + 2 + p->ngroups, c + 1, nullptr, A, B,
+              p->tA, p->rev, alpha, wait_limit_ns()};
+  void* errp = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&errp, bat::g_batch_error);
+  if (e != cudaSuccess) return cuda_status(e, "batch error word");
+  a.err = static_cast<int*>(errp);
+  bat::batched_node_kernel<T><<<p->grid, bat::NT, p->smem, s>>>(a);
+  NLA_CHECK_LAUNCH("batched_node_kernel");
+  return NLA_OK;
 }
 
 int enqueue(nla_batch_plan p, double alpha, const void* A, void* B, cudaStream_t s) {
-  cudaMemsetAsync(p->d_counter, 0, sizeof(int), s);
+  cudaError_t e = cudaMemsetAsync(p->d_counters, 0, p->counter_bytes, s);
+  if (e != cudaSuccess) return cuda_status(e, "batch counter reset");
   switch (p->dtype) {
-    case NLA_F64: return launch_batched<double>(p, alpha, A, B, s);
-    case NLA_F32: return launch_batched<float>(p, alpha, A, B, s);
-    default: return launch_batched<__half>(p, alpha, A, B, s);
+    case NLA_F64: return launch_nodes<double>(p, alpha, A, B, s);
+    case NLA_F32: return launch_nodes<float>(p, alpha, A, B, s);
+    default: return launch_nodes<__half>(p, alpha, A, B, s);
   }
+}
+
+int plan_create(nla_batch_plan* out, int dtype, char uplo, char trans, int64_t count, const nla_batch_desc* descs,
+                const nla_batch_tuning& tun) {
+  if (!out) return fail(NLA_ERR_ARG, "plan pointer is null");
+  *out = nullptr;
+  NLA_TRY(check_flags('L', uplo, trans, 'S', dtype));
+  NLA_TRY(check_tuning(tun));
+  if (count < 0 || (count > 0 && !descs)) return fail(NLA_ERR_ARG, "bad system count or descriptor array");
+  if (count > (int64_t)1 << 24) return fail(NLA_ERR_UNSUPPORTED, "too many systems");
+  for (int64_t i = 0; i < count; ++i) {
+    const nla_batch_desc& d = descs[i];
+    if (d.n < 0 || d.m < 0 || d.n > 1024 || d.lda < (d.n > 1 ? d.n : 1) || d.ldb < (d.n > 1 ? d.n : 1) ||
+        d.a_off < 0 || d.b_off < 0)
+      return fail(NLA_ERR_ARG, "system " + std::to_string(i) + ": bad size, leading dimension or offset");
+  }
+  nla_batch_plan p = new nla_batch_plan_s();
+  p->dtype = dtype;
+  p->tA = (trans == 'T' || trans == 'C') ? 1 : 0;
+  const char up = p->tA ? (uplo == 'L' ? 'U' : 'L') : uplo;
+  p->rev = up == 'U';
+  p->count = count;
+  p->h_descs.assign(descs, descs + count);
+  p->n_max = 1;
+  p->w_max = 16;
+  p->flops = 0;
+  p->a_elems = p->b_elems = 0;
+  p->a32 = p->x32 = nullptr;
+  p->r64 = nullptr;
+  p->exec = nullptr;
+  p->d_descs = p->d_groups = p->d_nodes = nullptr;
+  p->d_counters = nullptr;
+  p->cap_stream = nullptr;
+
+  std::vector<Group> groups;
+  std::vector<HostNode> nodes;
+  int leaves_total = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    const nla_batch_desc& d = descs[i];
+    if (d.n == 0 || d.m == 0) continue;
+    p->a_elems = std::max<int64_t>(p->a_elems, d.a_off + (d.n - 1) * d.lda + d.n);
+    p->b_elems = std::max<int64_t>(p->b_elems, d.b_off + (d.m - 1) * d.ldb + d.n);
+    p->n_max = std::max<int>(p->n_max, (int)d.n);
+    p->flops += (double)d.n * d.n * d.m;
+    const int b = bucket_of(d.n);
+    const int wcap = dtype == NLA_F64 ? std::min(tun.cols[b], 64) : tun.cols[b];
+    // Balanced blocks of right-hand sides, each at most wcap wide, each run
+    // with the narrowest column template that holds it.
+    const int64_t nblk = (d.m + wcap - 1) / wcap;
+    for (int64_t k = 0; k < nblk; ++k) {
+      const int64_t c0 = d.m * k / nblk, c1 = d.m * (k + 1) / nblk;
+      Group g{};
+      g.sys = (int)i;
+      g.c0 = (int)c0;
+      g.ncols = (int)(c1 - c0);
+      g.w = g.ncols <= 16 ? 16 : g.ncols <= 32 ? 32 : g.ncols <= 64 ? 64 : 128;
+      g.leaf_base = leaves_total;
+      g.n = (int)d.n;
+      p->w_max = std::max(p->w_max, g.w);
+      GroupBuilder gb;
+      gb.gi = (int)groups.size();
+      gb.cutoff = tun.cutoff[b];
+      gb.rev = p->rev != 0;
+      gb.nodes = &nodes;
+      gb.group_w = g.w;
+      gb.leaves(0, (int)d.n);
+      gb.chain.assign(gb.leaf_start.size(), 0);
+      gb.last_node.assign(gb.leaf_start.size(), -1);
+      gb.rec(0, (int)d.n);
+      leaves_total += (int)gb.leaf_start.size();
+      groups.push_back(g);
+    }
+  }
+  if (groups.size() > (size_t)INT32_MAX / 2 || nodes.size() > (size_t)INT32_MAX / 2) {
+    delete p;
+    return fail(NLA_ERR_UNSUPPORTED, "batch too large");
+  }
+  p->ngroups = (int)groups.size();
+  p->nleaves = leaves_total;
+  p->nnodes = (int)nodes.size();
+  p->smem = bat::node_smem_bytes(dtype, p->w_max);
+  int per_sm = 0, rc;
+  if (dtype == NLA_F64) rc = node_kernel_setup<double>(p->smem, &per_sm);
+  else if (dtype == NLA_F32) rc = node_kernel_setup<float>(p->smem, &per_sm);
+  else rc = node_kernel_setup<__half>(p->smem, &per_sm);
+  if (rc != NLA_OK) {
+    delete p;
+    return rc;
+  }
+  p->grid = std::max(1, std::min(std::max(p->nnodes, 1), num_sms() * std::max(per_sm, 1)));
+  const std::vector<int> order = schedule(nodes, p->grid);
+  std::vector<Node> queue(nodes.size());
+  for (size_t k = 0; k < order.size(); ++k) queue[k] = nodes[order[k]].d;
+
+  p->counter_bytes = sizeof(int) * (size_t)(2 + p->ngroups + p->nleaves);
+  cudaError_t e = cudaMalloc(&p->d_descs, sizeof(nla_batch_desc) * (size_t)std::max<int64_t>(count, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_groups, sizeof(Group) * (size_t)std::max(p->ngroups, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_nodes, sizeof(Node) * (size_t)std::max(p->nnodes, 1));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->d_counters), p->counter_bytes);
+  if (e == cudaSuccess && count > 0)
+    e = cudaMemcpy(p->d_descs, descs, sizeof(nla_batch_desc) * (size_t)count, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && p->ngroups > 0)
+    e = cudaMemcpy(p->d_groups, groups.data(), sizeof(Group) * groups.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && p->nnodes > 0)
+    e = cudaMemcpy(p->d_nodes, queue.data(), sizeof(Node) * queue.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    cudaFree(p->d_descs);
+    cudaFree(p->d_groups);
+    cudaFree(p->d_nodes);
+    cudaFree(p->d_counters);
+    delete p;
+    return cuda_status(e, "batch plan allocation");
+  }
+  *out = p;
+  return NLA_OK;
 }
 
 }  // namespace
 
-
+// Reads (and clears) the batched kernel's error word: the site of the first
+// dependency wait that gave up, or 0.
+int batch_device_error() {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, bat::g_batch_error, sizeof(int)) != cudaSuccess) return 0;
+  if (v != 0) {
+    const int zero = 0;
+    cudaMemcpyToSymbol(bat::g_batch_error, &zero, sizeof(int));
+  }
+  return v;
+}
 
 }  // namespace nla
 
@@ -299,109 +966,26 @@ extern "C" {
 int nla_batch_plan_create(nla_batch_plan* out, int dtype, char uplo, char trans, int64_t count,
                           const nla_batch_desc* descs, const int* cols_per_item) {
   clear_error();
-  if (!out) return fail(NLA_ERR_ARG, "plan pointer is null");
-  *out = nullptr;
-  NLA_TRY(check_flags('L', uplo, trans, 'S', dtype));
-  if (count < 0 || (count > 0 && !descs)) return fail(NLA_ERR_ARG, "bad system count or descriptor array");
-  if (count > (int64_t)1 << 30) return fail(NLA_ERR_UNSUPPORTED, "too many systems");
-  int cw[NLA_BATCH_BUCKETS] = {8, 16, 16, 16, 16, 16};
-  if (dtype != NLA_F64)
-    for (int b = 0; b < NLA_BATCH_BUCKETS; ++b) cw[b] = b == 0 ? 16 : 32;
+  nla_batch_tuning t;
+  default_tuning(dtype, &t);
   if (cols_per_item)
-    for (int b = 0; b < NLA_BATCH_BUCKETS; ++b) {
-      if (cols_per_item[b] != 8 && cols_per_item[b] != 16 && cols_per_item[b] != 32)
-        return fail(NLA_ERR_ARG, "cols_per_item entries must be 8, 16 or 32");
-      cw[b] = cols_per_item[b];
-    }
-  nla_batch_plan p = new nla_batch_plan_s();
-  p->dtype = dtype;
-  p->tA = (trans == 'T' || trans == 'C') ? 1 : 0;
-  const char up = p->tA ? (uplo == 'L' ? 'U' : 'L') : uplo;
-  p->rev = up == 'U';
-  p->count = count;
-  p->h_descs.assign(descs, descs + count);
-  std::vector<BatchItem> items;
-  int bucket_n_max[NLA_BATCH_BUCKETS] = {0, 0, 0, 0, 0, 0};
-  p->n_max = 1;
-  p->cw_max = 8;
-  p->flops = 0;
-  p->a_elems = 0;
-  p->b_elems = 0;
-  p->a32 = nullptr;
-  p->x32 = nullptr;
-  p->r64 = nullptr;
-  for (int64_t i = 0; i < count; ++i) {
-    const nla_batch_desc& d = descs[i];
-    if (d.n < 0 || d.m < 0 || d.n > 1024 || d.lda < (d.n > 1 ? d.n : 1) || d.ldb < (d.n > 1 ? d.n : 1) ||
-        d.a_off < 0 || d.b_off < 0) {
-      delete p;
-      return fail(NLA_ERR_ARG, "system " + std::to_string(i) + ": bad size, leading dimension or offset");
-    }
-    if (d.n == 0 || d.m == 0) continue;
-    p->a_elems = std::max<int64_t>(p->a_elems, d.a_off + (d.n - 1) * d.lda + d.n);
-    p->b_elems = std::max<int64_t>(p->b_elems, d.b_off + (d.m - 1) * d.ldb + d.n);
-    const int bk = bucket_of(d.n);
-    const int c = cw[bk];
-    bucket_n_max[bk] = std::max<int>(bucket_n_max[bk], (int)d.n);
-    p->n_max = std::max<int>(p->n_max, (int)d.n);
-    p->cw_max = std::max(p->cw_max, c);
-    p->flops += (double)d.n * d.n * d.m;
-    for (int64_t c0 = 0; c0 < d.m; c0 += c) items.push_back(BatchItem{(int)i, (int)c0, c, 0});
-  }
-  // Largest items first: the tail of the schedule is made of small items.
-  std::stable_sort(items.begin(), items.end(), [&](const BatchItem& x, const BatchItem& y) {
-    const double cx = (double)descs[x.sys].n * descs[x.sys].n * std::min<int64_t>(x.cw, descs[x.sys].m - x.c0);
-    const double cy = (double)descs[y.sys].n * descs[y.sys].n * std::min<int64_t>(y.cw, descs[y.sys].m - y.c0);
-    return cx > cy;
-  });
-  p->nitems = (int)items.size();
-  const size_t esz = dtype == NLA_F64 ? 8 : 4;
-  // Shared memory for the largest block any item stages: n_max of a bucket
-  // times that bucket's width (narrow items for the large systems keep the
-  // plan at two or more CTAs per SM).
-  p->smem = 0;
-  for (int b = 0; b < NLA_BATCH_BUCKETS; ++b)
-    if (bucket_n_max[b] > 0)
-      p->smem = std::max(p->smem, leaf_solve_smem_elems(bucket_n_max[b], cw[b]) * esz);
-  int rc = NLA_OK;
-  int per_sm = 0;
-  if (dtype == NLA_F64) rc = batched_smem_attr<double>(p->smem);
-  else if (dtype == NLA_F32) rc = batched_smem_attr<float>(p->smem);
-  else rc = batched_smem_attr<__half>(p->smem);
-  if (rc == NLA_OK) {
-    if (dtype == NLA_F64) rc = occupancy<double>(p->smem, &per_sm);
-    else if (dtype == NLA_F32) rc = occupancy<float>(p->smem, &per_sm);
-    else rc = occupancy<__half>(p->smem, &per_sm);
-  }
-  if (rc != NLA_OK) {
-    delete p;
-    return rc;
-  }
-  p->grid = std::max(1, std::min(p->nitems, num_sms() * std::max(per_sm, 1)));
-  cudaError_t e = cudaMalloc(&p->d_descs, sizeof(nla_batch_desc) * (size_t)std::max<int64_t>(count, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&p->d_items, sizeof(BatchItem) * (size_t)std::max(p->nitems, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&p->d_counter, sizeof(int));
-  if (e == cudaSuccess && count > 0)
-    e = cudaMemcpy(p->d_descs, descs, sizeof(nla_batch_desc) * (size_t)count, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && p->nitems > 0)
-    e = cudaMemcpy(p->d_items, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking);
-  if (e != cudaSuccess) {
-    cudaFree(p->d_descs);
-    cudaFree(p->d_items);
-    cudaFree(p->d_counter);
-    delete p;
-    return cuda_status(e, "batch plan allocation");
-  }
-  p->exec = nullptr;
-  *out = p;
-  return NLA_OK;
+    for (int b = 0; b < NLA_BATCH_BUCKETS; ++b) t.cols[b] = cols_per_item[b];
+  return plan_create(out, dtype, uplo, trans, count, descs, t);
+}
+
+int nla_batch_plan_create_tuned(nla_batch_plan* out, int dtype, char uplo, char trans, int64_t count,
+                                const nla_batch_desc* descs, const nla_batch_tuning* tuning) {
+  clear_error();
+  nla_batch_tuning t;
+  default_tuning(dtype, &t);
+  if (tuning) t = *tuning;
+  return plan_create(out, dtype, uplo, trans, count, descs, t);
 }
 
 int nla_batch_plan_info(nla_batch_plan p, int64_t* items, int64_t* grid, double* flops) {
   clear_error();
   if (!p) return fail(NLA_ERR_ARG, "null plan");
-  if (items) *items = p->nitems;
+  if (items) *items = p->nnodes;
   if (grid) *grid = p->grid;
   if (flops) *flops = p->flops;
   return NLA_OK;
@@ -410,7 +994,7 @@ int nla_batch_plan_info(nla_batch_plan p, int64_t* items, int64_t* grid, double*
 int nla_batch_solve(nla_batch_plan p, double alpha, const void* A_pool, void* B_pool, int mode, void* stream) {
   clear_error();
   if (!p) return fail(NLA_ERR_ARG, "null plan");
-  if (p->nitems == 0) return NLA_OK;
+  if (p->nnodes == 0) return NLA_OK;
   if (!A_pool || !B_pool) return fail(NLA_ERR_ARG, "null pool pointer");
   cudaStream_t s = (cudaStream_t)stream;
   if (mode == NLA_BATCH_LOOP) {
@@ -430,7 +1014,7 @@ int nla_batch_solve(nla_batch_plan p, double alpha, const void* A_pool, void* B_
   TraceScope trace(NLA_K_BATCHED, s, p->flops, 0.0);
   if (mode == NLA_BATCH_PERSISTENT) return enqueue(p, alpha, A_pool, B_pool, s);
   if (mode != NLA_BATCH_GRAPH) return fail(NLA_ERR_ARG, "unknown batch mode");
-  if (!p->exec || p->g_alpha != alpha || p->g_A != A_pool || p->g_B != B_pool) {
+  if (!p->exec || p->g_alpha != alpha || p->g_A != A_pool || p->g_B != B_pool || p->g_limit != wait_limit_ns()) {
     if (p->exec) {
       cudaGraphExecDestroy(p->exec);
       p->exec = nullptr;
@@ -454,6 +1038,7 @@ int nla_batch_solve(nla_batch_plan p, double alpha, const void* A_pool, void* B_
     p->g_alpha = alpha;
     p->g_A = A_pool;
     p->g_B = B_pool;
+    p->g_limit = wait_limit_ns();
   }
   cudaError_t e = cudaGraphLaunch(p->exec, s);
   return e == cudaSuccess ? NLA_OK : cuda_status(e, "batch graph launch");
@@ -465,7 +1050,7 @@ int nla_batch_solve_mixed(nla_batch_plan p, double alpha, const void* A_pool, vo
   if (!p) return fail(NLA_ERR_ARG, "null plan");
   if (p->dtype != NLA_F64) return fail(NLA_ERR_DTYPE, "mixed batch: the plan must be Float64");
   if (sweeps < 0 || sweeps > 8) return fail(NLA_ERR_ARG, "mixed batch: sweeps must be 0..8");
-  if (p->nitems == 0) return NLA_OK;
+  if (p->nnodes == 0) return NLA_OK;
   if (!A_pool || !B_pool) return fail(NLA_ERR_ARG, "null pool pointer");
   cudaStream_t s = (cudaStream_t)stream;
   if (!p->a32) {
@@ -482,31 +1067,36 @@ int nla_batch_solve_mixed(nla_batch_plan p, double alpha, const void* A_pool, vo
       return cuda_status(e, "mixed batch buffers");
     }
   }
-  NLA_TRY(batched_smem_attr<float>(p->smem));
+  int per_sm = 0;
+  NLA_TRY(node_kernel_setup<float>(p->smem, &per_sm));
   const auto* descs = static_cast<const nla_batch_desc*>(p->d_descs);
-  const auto* items = static_cast<const BatchItem*>(p->d_items);
+  const auto* groups = static_cast<const Group*>(p->d_groups);
   double* B64 = static_cast<double*>(B_pool);
   const double* A64 = static_cast<const double*>(A_pool);
   TraceScope trace(NLA_K_BATCHED, s, p->flops, 0.0);
-  MapArgs m{descs, items, A64, p->a32, B64, p->r64, p->x32, alpha, MAP_INIT};
-  batched_map_kernel<<<p->nitems, 256, 0, s>>>(m);
+  bat::MapArgs m{descs, groups, A64, p->a32, B64, p->r64, p->x32, alpha, bat::MAP_INIT};
+  bat::batched_map_kernel<<<p->ngroups, 256, 0, s>>>(m);
   NLA_CHECK_LAUNCH("batched_map_kernel");
+  // The Float32 solves run on the same node queue (the plan's Float64 layout
+  // of nodes and shared memory covers the Float32 kernel).
   auto solve32 = [&]() -> int {
-    cudaMemsetAsync(p->d_counter, 0, sizeof(int), s);
-    return launch_batched<float>(p, 1.0, p->a32, p->x32, s);
+    cudaError_t e = cudaMemsetAsync(p->d_counters, 0, p->counter_bytes, s);
+    if (e != cudaSuccess) return cuda_status(e, "batch counter reset");
+    return launch_nodes<float>(p, 1.0, p->a32, p->x32, s);
   };
   NLA_TRY(solve32());
-  m.op = MAP_SET;
-  batched_map_kernel<<<p->nitems, 256, 0, s>>>(m);
+  m.op = bat::MAP_SET;
+  bat::batched_map_kernel<<<p->ngroups, 256, 0, s>>>(m);
   NLA_CHECK_LAUNCH("batched_map_kernel");
-  const ResidualArgs r{descs, items, A64, B64, p->r64, p->x32, p->tA, p->rev};
+  const bat::ResidualArgs r{descs, groups, A64, B64, p->r64, p->x32, p->tA, p->rev};
   for (int k = 0; k < sweeps; ++k) {
-    batched_residual_kernel<<<dim3((unsigned)p->nitems, (unsigned)((p->n_max + LEAF_THREADS - 1) / LEAF_THREADS)),
-                              LEAF_THREADS, 0, s>>>(r);
+    bat::batched_residual_kernel<<<dim3((unsigned)p->ngroups,
+                                        (unsigned)((p->n_max + bat::MAX_ROWS - 1) / bat::MAX_ROWS)),
+                                   bat::NT, 0, s>>>(r);
     NLA_CHECK_LAUNCH("batched_residual_kernel");
     NLA_TRY(solve32());
-    m.op = MAP_ADD;
-    batched_map_kernel<<<p->nitems, 256, 0, s>>>(m);
+    m.op = bat::MAP_ADD;
+    bat::batched_map_kernel<<<p->ngroups, 256, 0, s>>>(m);
     NLA_CHECK_LAUNCH("batched_map_kernel");
   }
   return NLA_OK;
@@ -519,10 +1109,11 @@ int nla_batch_plan_destroy(nla_batch_plan p) {
   cudaFree(p->x32);
   cudaFree(p->r64);
   if (p->exec) cudaGraphExecDestroy(p->exec);
-  cudaStreamDestroy(p->cap_stream);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   cudaFree(p->d_descs);
-  cudaFree(p->d_items);
-  cudaFree(p->d_counter);
+  cudaFree(p->d_groups);
+  cudaFree(p->d_nodes);
+  cudaFree(p->d_counters);
   delete p;
   return NLA_OK;
 }

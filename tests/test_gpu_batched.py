@@ -77,6 +77,8 @@ def test_batched_rejects_bad_descriptors(pkg, cuda):
         batched.BatchPlan(torch.float64, "L", "N", [(64, 4, 0, 32, 0, 64)])
     with pytest.raises(_lib.NLAArgumentError):
         batched.BatchPlan(torch.float64, "L", "N", [(64, 4, 0, 64, 0, 64)], cols_per_item=[7] * 6)
+    with pytest.raises(_lib.NLAArgumentError):
+        batched.BatchPlan(torch.float64, "L", "N", [(64, 4, 0, 64, 0, 64)], cutoff=[128] * 6)
 
 
 def test_tuner_writes_cache(pkg, cuda, tmp_path, monkeypatch):
@@ -87,10 +89,12 @@ def test_tuner_writes_cache(pkg, cuda, tmp_path, monkeypatch):
     from nextla_gb300 import tune
 
     monkeypatch.setenv("NLA_TUNE_CACHE", str(tmp_path / "tune.json"))
-    chosen, timings = tune.tune(torch.float32, cuda, systems_per_bucket=32, m=32, reps=1)
-    assert len(chosen) == 6 and all(c in (8, 16, 32) for c in chosen)
+    (cut, cols), timings = tune.tune(torch.float32, cuda, systems_per_bucket=24, reps=1)
+    assert len(cut) == 6 and all(c in tune.CUTOFFS for c in cut)
+    assert len(cols) == 6 and all(w in tune.COLS for w in cols)
+    assert all(len(timings[b]) == len(tune.candidates(torch.float32)) for b in range(6))
     data = json.load(open(tmp_path / "tune.json"))
-    assert tune.lookup(torch.float32, cuda) == chosen
+    assert tune.lookup(torch.float32, cuda) == (cut, cols)
     assert torch.cuda.get_device_name(cuda) in data
 
 

@@ -39,9 +39,13 @@ def test_tuner_cache_roundtrip(pkg, tmp_path, monkeypatch):
     monkeypatch.setenv("NLA_TUNE_CACHE", str(path))
     monkeypatch.setattr(torch.cuda, "get_device_name", lambda device=None: "Test GPU")
     assert tune.lookup(torch.float64) is None
-    path.write_text(json.dumps({"Test GPU": {"f64": {str(b): c for b, c in enumerate([8, 16, 16, 32, 32, 16])}}}))
-    assert tune.lookup(torch.float64) == [8, 16, 16, 32, 32, 16]
+    cut, cols = [16, 16, 32, 64, 64, 64], [32, 64, 64, 64, 32, 64]
+    path.write_text(json.dumps({"Test GPU": {"f64": {str(b): {"cutoff": c, "cols": w}
+                                                     for b, (c, w) in enumerate(zip(cut, cols))}}}))
+    assert tune.lookup(torch.float64) == (cut, cols)
     assert tune.lookup(torch.float32) is None
+    path.write_text(json.dumps({"Test GPU": {"f64": {"0": 8}}}))  # an older cache layout
+    assert tune.lookup(torch.float64) is None
     path.write_text("not json")
     assert tune.lookup(torch.float64) is None
 
@@ -57,7 +61,12 @@ def test_batch_plan_rejects_without_gpu_work(pkg, lib):
     assert lib.nla_batch_plan_create(ctypes.byref(plan), 2, b"L", b"N", 1, bad, None) == -1
     bad = (_lib.BatchDesc * 1)(_lib.BatchDesc(64, 4, 0, 32, 0, 64))  # lda < n
     assert lib.nla_batch_plan_create(ctypes.byref(plan), 2, b"L", b"N", 1, bad, None) == -1
-    cw = (ctypes.c_int * 6)(8, 8, 8, 8, 8, 7)
+    cw = (ctypes.c_int * 6)(32, 32, 32, 32, 32, 7)
     good = (_lib.BatchDesc * 1)(_lib.BatchDesc(64, 4, 0, 64, 0, 64))
     assert lib.nla_batch_plan_create(ctypes.byref(plan), 2, b"L", b"N", 1, good, cw) == -1
     assert lib.nla_batch_plan_create(ctypes.byref(plan), 2, b"X", b"N", 1, good, None) == -1
+    t = _lib.BatchTuning()
+    for b in range(6):
+        t.cutoff[b], t.cols[b] = 32, 64
+    t.cutoff[3] = 48  # not a leaf order the kernel has
+    assert lib.nla_batch_plan_create_tuned(ctypes.byref(plan), 2, b"L", b"N", 1, good, ctypes.byref(t)) == -1
