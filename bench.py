@@ -82,7 +82,7 @@ def parse():
     ap.add_argument("--sweep-plain", action="store_true",
                     help="plain F32/F64 TRSM and TRMM over the 8 side/uplo/trans forms, alpha 0.5 (config 1)")
     ap.add_argument("--sizes", default="4096,8192,16384")
-    ap.add_argument("--kernel-case", choices=["exact", "fast", "leaf", "dfma", "feed"], default=None,
+    ap.add_argument("--kernel-case", choices=["exact", "fast", "leaf", "dfma"], default=None,
                     help="run single launches of one kernel on a moderate case (for ncu captures)")
     ap.add_argument("--case-size", type=int, default=4096)
     ap.add_argument("--case-reps", type=int, default=2)
@@ -161,18 +161,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def traffic_per_launch():
-    """DRAM bytes (read + write) per launch of the dominant tensor-core kernel,
-    from the committed ncu summary of the same workload
-    (profiles/umma_exact_kernel_n16384_dram.md), or None."""
-    path = os.path.join(ROOT, "profiles", "umma_exact_kernel_n16384_dram.md")
-    if not os.path.exists(path):
-        return None
-    with open(path) as f:
-        for line in f:
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1])
-    return None
+PLAIN_STEPS = 3  # timed solves of the plain FP64 comparison
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# exact tensor-core kernel, averaged over the 255 updates of one default
+# solve at n = m = 16384.  ncu cannot run inside the timed bench, so this is
+# the figure of one ncu capture of the same workload, with the commit and
+# command it was taken on (TRAFFIC_SOURCE).
+TRAFFIC_BYTES_PER_LAUNCH = 219e6
+TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:umma_exact -s 510 -c 510 "
+                  "python bench.py --steps 1 --warmup 1 --no-plain --no-cpu-baseline, at commit 9df2745")
 
 
 def make_inputs(n, m, seed=0):
@@ -273,8 +271,9 @@ def run_batched(args):
     n, m = batched.uneven_sizes(count=args.count, seed=7)
     A, B0, systems = batched.make_batch(n, m, dtype, dev, seed=7)
     flops = float((n.astype(float) ** 2 * m).sum())
-    cw = tune.tune(dtype, dev)[0] if args.tune else tune.lookup(dtype, dev)
-    plan = batched.BatchPlan(dtype, "L", "N", systems, cols_per_item=cw)
+    tuned = tune.tune(dtype, dev)[0] if args.tune else tune.lookup(dtype, dev)
+    cutoff, cw = tuned if tuned else (None, None)
+    plan = batched.BatchPlan(dtype, "L", "N", systems, cutoff=cutoff, cols=cw)
     B = B0.clone()
     stream = torch.cuda.current_stream(dev)
 
@@ -330,7 +329,8 @@ def run_batched(args):
         "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded)",
         "config": {"workload": "batched_trsm_LLN_%s_%d_uneven" % (args.dtype, args.count), "count": args.count,
                    "n": "log-uniform [16, 1024]", "m": "uniform 1..128", "seed": 7, "flops": flops,
-                   "work_items": items, "persistent_ctas": grid, "cols_per_item": cw or "library defaults"},
+                   "nodes": items, "persistent_ctas": grid,
+                   "tuning": {"cutoff": cutoff, "cols": cw} if tuned else "library defaults"},
         "one_launch_per_system": {"ms": loop_ms, "tflops": flops / (loop_ms / 1e3) / 1e12},
         "speedup_vs_one_launch_per_system": loop_ms / ms,
         "trace": {k: {"launches": v[0], "ms": v[1]} for k, v in trace.items()},
@@ -658,8 +658,7 @@ def run_kernel_case(args):
       fast   the same with 3 BF16 slices (FP32 accumulation);
       leaf   one FP64 diagonal-block solve of order 128 with 8 s right-hand
              sides (--case-shape n,m for order n with m right-hand sides);
-      dfma   one FP64 update on CUDA cores, s x s x s;
-      feed   the tensor-core feed probes (nla_measure_tensor_feed)."""
+      dfma   one FP64 update on CUDA cores, s x s x s."""
     import torch
 
     import __graft_entry__ as graft
@@ -673,12 +672,6 @@ def run_kernel_case(args):
     def cm(r, c):
         return torch.randn(c, r, generator=g, device=dev, dtype=torch.float64).T
 
-    if args.kernel_case == "feed":
-        from nextla_gb300 import _lib
-
-        print(json.dumps({"kernel_case": "feed", "sms": torch.cuda.get_device_properties(dev).multi_processor_count,
-                          **_lib.measure_tensor_feed(torch.cuda.current_stream(dev).cuda_stream)}), flush=True)
-        return 0
     times = []
     for _ in range(args.case_reps):
         if args.kernel_case in ("exact", "fast"):
@@ -896,20 +889,24 @@ def main():
     berr, berr_parts = backward_error(B)
     plain = None
     if args.variant == "mixed" and not args.no_plain:
+        # The plain FP64 path on the same inputs: one warm-up solve, then
+        # PLAIN_STEPS timed solves (each restoring B first), the slowest
+        # rank's time, the whole-job rate, as for `value`.
         Bp = torch.empty_like(B0.T).T
         Bp.copy_(B0)
         solve_plain(A, Bp)  # warm-up of the plain path's kernels
-        Bp.copy_(B0)
         barrier()
         p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         p0.record(stream)
-        solve_plain(A, Bp)
+        for _ in range(PLAIN_STEPS):
+            Bp.copy_(B0)
+            solve_plain(A, Bp)
         p1.record(stream)
         barrier()
-        pms = p0.elapsed_time(p1)
+        pms = max_over_ranks(p0.elapsed_time(p1), world, dev)
         pb, pparts = backward_error(Bp)
-        plain = {"tflops": flops / (pms / 1e3) / 1e12, "ms": pms, "backward_error": pb, "norms": pparts,
-                 "steps": 1}
+        plain = {"tflops": job_tflops(world, PLAIN_STEPS * flops, pms), "ms_per_step": pms / PLAIN_STEPS,
+                 "backward_error": pb, "norms": pparts, "steps": PLAIN_STEPS}
         del Bp
 
     # Roofline of the dominant kernel class.
@@ -929,7 +926,8 @@ def main():
             peak = float(pk.get("bf16_tflops_sustained", pk.get("bf16_tflops")))
             roofline = {"kernel": "umma_gemm/umma_exact (tcgen05 BF16 slice products)", "bound": "tensor",
                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                        "traffic": traffic_per_launch() if exact_headline else None,
+                        "traffic": TRAFFIC_BYTES_PER_LAUNCH if exact_headline else None,
+                        "traffic_source": TRAFFIC_SOURCE if exact_headline else None,
                         "launches": launches, "share": share,
                         "peak_source": "bf16_tflops_sustained of %s MEASURED_PEAKS.json" % pk_kind}
         else:

@@ -107,6 +107,7 @@ int copy_a(HostRun& h, int64_t i, int64_t j, int64_t r, int64_t q) {
   if (r <= 0 || q <= 0) return NLA_OK;
   const int64_t si = h.at ? j : i, sj = h.at ? i : j, sr = h.at ? q : r, sq = h.at ? r : q;
   const size_t es = h.es;
+  TraceScope trace(NLA_K_COPY_IN, h.in, 0.0, (double)sr * (double)sq * (double)es);
   cudaError_t e = cudaMemcpy2DAsync(h.Ad + (size_t)(si + sj * h.ldad) * es, (size_t)h.ldad * es,
                                     h.Ah + (size_t)(si + sj * h.ldah) * es, (size_t)h.ldah * es, (size_t)sr * es,
                                     (size_t)sq, cudaMemcpyHostToDevice, h.in);
@@ -120,6 +121,8 @@ cudaError_t copy_b(const HostRun& h, const BlockB& b, bool to_device) {
   const bool L = h.c.side == 'L';
   const size_t width = (size_t)(L ? b.len : h.c.m) * es, height = (size_t)(L ? h.c.m : b.len);
   char* d = h.Bd + (size_t)(L ? b.k : b.k * h.ldbd) * es;
+  TraceScope trace(to_device ? NLA_K_COPY_IN : NLA_K_COPY_OUT, to_device ? h.in : h.out, 0.0,
+                   (double)width * (double)height);
   if (to_device)
     return cudaMemcpy2DAsync(d, (size_t)h.ldbd * es, h.Bh + (size_t)(L ? b.k : b.k * h.ldbh) * es,
                              (size_t)h.ldbh * es, width, height, cudaMemcpyHostToDevice, h.in);

@@ -5,6 +5,8 @@ collectives are the barriers and the max-over-ranks reduction of the timed
 region.  Checked here:
   - every rank gets the slowest rank's time;
   - the whole-job rate counts all ranks' work in that time;
+  - the speed-up over the plain FP64 path compares two whole-job rates, so
+    it does not grow with the number of ranks;
   - under torchrun, the reference arm runs on rank 0 only.
 """
 
@@ -37,9 +39,13 @@ def _rank_main(rank, world, port, out_dir):
         dist.barrier()
         ms = bench.max_over_ranks(10.0 * (rank + 1), world, torch.device("cpu"))
         rate = bench.job_tflops(world, 2e12, ms)
+        # The plain comparison goes through the same reduction and rate: its
+        # ranks take 400 and 200 ms for 3 steps of the same work.
+        plain_ms = bench.max_over_ranks(400.0 - 200.0 * rank, world, torch.device("cpu"))
+        plain_rate = bench.job_tflops(world, 3 * 2e12, plain_ms)
         dist.barrier()
         with open(os.path.join(out_dir, "rank%d.json" % rank), "w") as f:
-            json.dump({"ms": ms, "rate": rate}, f)
+            json.dump({"ms": ms, "rate": rate, "speedup": rate / plain_rate}, f)
     finally:
         dist.destroy_process_group()
 
@@ -53,6 +59,8 @@ def test_two_gloo_ranks_max_over_ranks(tmp_path):
         got = json.load(open(tmp_path / ("rank%d.json" % rank)))
         assert got["ms"] == 20.0  # the slower rank's 20 ms, on both ranks
         assert got["rate"] == pytest.approx(2 * 2e12 / 0.020 / 1e12)  # 200 TFLOP/s of whole-job work
+        # 20 ms per step against 400 / 3 ms per plain step: 6.67x, whatever the world size.
+        assert got["speedup"] == pytest.approx((400.0 / 3) / 20.0)
 
 
 def test_single_rank_is_unchanged():
