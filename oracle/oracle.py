@@ -32,15 +32,15 @@ _lock = threading.Lock()
 def build(force: bool = False) -> str:
     """Compile the C oracle with gcc (no FMA contraction, so x86 and Arm agree)."""
     src = os.path.join(HERE, "rectrxm_oracle.c")
-    hdr = os.path.join(HERE, "rectrxm_oracle_impl.h")
+    hdrs = [os.path.join(HERE, "rectrxm_oracle_impl.h"), os.path.join(HERE, "rectrxm_oracle_cplx.h")]
     if not force and os.path.exists(LIB_PATH):
-        newest = max(os.path.getmtime(src), os.path.getmtime(hdr))
+        newest = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in hdrs])
         if os.path.getmtime(LIB_PATH) >= newest:
             return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
     cmd = ["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-           "-o", tmp, src, "-lpthread"]
+           "-o", tmp, src, "-lpthread", "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -59,6 +59,8 @@ def lib():
             L.oracle_matmul.restype = i32
             L.oracle_leaf.argtypes = [c, c, c, i32, i64, i64, p, i64, i32, p, i64]
             L.oracle_leaf.restype = i32
+            L.oracle_rectrxm_cplx.argtypes = [c, c, c, d, d, c, i32, i64, i64, p, i64, p, i64, i64, i64, i32]
+            L.oracle_rectrxm_cplx.restype = i32
             L.oracle_split_point.argtypes = [i64]
             L.oracle_split_point.restype = i64
             _lib = L
@@ -96,6 +98,27 @@ def rectrxm(side, uplo, trans, alpha, func, A, B, *, dtype=None, thresholds=(256
                               int(nthreads))
     if rc != 0:
         raise ValueError("oracle_rectrxm rejected its arguments")
+    return Bf.astype(dt)
+
+
+def rectrxm_complex(side, uplo, trans, alpha, func, A, B, *, dtype=None, thresholds=(256, 16), nthreads=1):
+    """unified_rectrxm! on complex A and B (ComplexF32 or ComplexF64, from
+    ``dtype`` or B's type) with complex alpha; trans 'C' takes the Adjoint.
+    Returns the result in that type; B is not modified."""
+    dt = np.dtype(dtype if dtype is not None else B.dtype)
+    code = {np.dtype(np.complex64): 3, np.dtype(np.complex128): 4}[dt]
+    Af = np.asfortranarray(np.asarray(A).astype(dt).astype(np.complex128))
+    Bf = np.asfortranarray(np.asarray(B).astype(dt).astype(np.complex128)).copy(order="F")
+    n = Af.shape[0]
+    m = Bf.shape[1] if side == "L" else Bf.shape[0]
+    if Af.shape != (n, n) or (side == "L" and Bf.shape[0] != n) or (side == "R" and Bf.shape[1] != n):
+        raise ValueError("A must be square and B must conform with it")
+    al = complex(alpha)
+    rc = lib().oracle_rectrxm_cplx(_ch(side), _ch(uplo), _ch(trans), al.real, al.imag, _ch(func), code, n, m,
+                                   _ptr(Af), max(n, 1), _ptr(Bf), max(Bf.shape[0], 1), int(thresholds[0]),
+                                   int(thresholds[1]), int(nthreads))
+    if rc != 0:
+        raise ValueError("oracle_rectrxm_cplx rejected its arguments")
     return Bf.astype(dt)
 
 
@@ -142,8 +165,8 @@ def blas_rectrxm(side, uplo, trans, alpha, func, A, B):
     from scipy.linalg import blas
 
     dt = np.dtype(B.dtype)
-    pre = "s" if dt == np.float32 else "d"
-    work = np.float32 if dt == np.float32 else np.float64
+    pre = {np.dtype(np.float32): "s", np.dtype(np.complex64): "c", np.dtype(np.complex128): "z"}.get(dt, "d")
+    work = {"s": np.float32, "c": np.complex64, "z": np.complex128, "d": np.float64}[pre]
     a = np.asfortranarray(np.asarray(A, dtype=work))
     b = np.asfortranarray(np.asarray(B, dtype=work))
     ta = {"N": 0, "T": 1, "C": 2}[trans]
@@ -159,8 +182,9 @@ def op_matrix(A, uplo, trans):
 
 
 def rel_err(X, Xref) -> float:
-    X = np.asarray(X, dtype=np.float64)
-    Xref = np.asarray(Xref, dtype=np.float64)
+    wide = np.complex128 if (np.iscomplexobj(X) or np.iscomplexobj(Xref)) else np.float64
+    X = np.asarray(X, dtype=wide)
+    Xref = np.asarray(Xref, dtype=wide)
     den = np.linalg.norm(Xref)
     return float(np.linalg.norm(X - Xref) / (den if den > 0 else 1.0))
 

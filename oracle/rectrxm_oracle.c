@@ -18,6 +18,7 @@
  * (Float32); the test suite checks this oracle against the same contract and
  * against exact rational solutions of small integer systems.
  */
+#include <math.h>
 #include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -65,7 +66,49 @@ static int64_t split_point(int64_t n) {
 #undef SUF
 #undef RND
 
-/* dtype codes: 0 = Float16, 1 = Float32, 2 = Float64 (same as the library). */
+/* Complex matrices: interleaved (re, im) doubles, column-major; element
+ * (i, j) at p[2 (i + j ld)], or p[2 (j + i ld)] when t is set; c reads the
+ * conjugate (an Adjoint view). */
+typedef struct {
+  double re, im;
+} cz;
+typedef struct {
+  double* p;
+  int64_t ld;
+  int t, c;
+} zview;
+
+static inline double* zat(zview v, int64_t i, int64_t j) { return v.p + 2 * (v.t ? j + i * v.ld : i + j * v.ld); }
+static inline cz zget(zview v, int64_t i, int64_t j) {
+  const double* q = zat(v, i, j);
+  cz r = {q[0], v.c ? -q[1] : q[1]};
+  return r;
+}
+static inline void zset(zview v, int64_t i, int64_t j, cz x) {
+  double* q = zat(v, i, j);
+  q[0] = x.re;
+  q[1] = x.im;
+}
+static inline zview zsub(zview v, int64_t i0, int64_t j0) {
+  zview r = v;
+  r.p = zat(v, i0, j0);
+  return r;
+}
+
+#define SUF c64
+#define RND(x) (x)
+#include "rectrxm_oracle_cplx.h"
+#undef SUF
+#undef RND
+
+#define SUF c32
+#define RND(x) ((double)(float)(x))
+#include "rectrxm_oracle_cplx.h"
+#undef SUF
+#undef RND
+
+/* dtype codes: 0 = Float16, 1 = Float32, 2 = Float64, 3 = ComplexF32,
+ * 4 = ComplexF64 (same as the library). */
 
 typedef struct {
   char side, uplo, trans, func;
@@ -176,3 +219,70 @@ int oracle_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m
 /* The recursion's split point (src/rectrxm.jl:129-133), exported so the
  * host-side planner can be checked against it. */
 int64_t oracle_split_point(int64_t n) { return split_point(n); }
+
+/* unified_rectrxm! on complex column-major arrays (interleaved re, im
+ * doubles), dtype 3 (ComplexF32, values rounded to float after every
+ * operation) or 4 (ComplexF64), alpha = alpha_re + i alpha_im.  Arguments as
+ * for oracle_rectrxm; the right-hand sides are split over nthreads. */
+typedef struct {
+  char side, uplo, trans, func;
+  cz alpha;
+  int dtype;
+  zview A;
+  int64_t n;
+  zview B;
+  int64_t m;
+  int64_t thr_s, thr_m;
+} zjob;
+
+static void* zjob_thread(void* arg) {
+  const zjob* j = (const zjob*)arg;
+  if (j->m <= 0) return NULL;
+  if (j->dtype == 3)
+    rectrxm_c32(j->side, j->uplo, j->trans, j->alpha, j->func, j->A, j->n, j->B, j->m, j->thr_s, j->thr_m);
+  else
+    rectrxm_c64(j->side, j->uplo, j->trans, j->alpha, j->func, j->A, j->n, j->B, j->m, j->thr_s, j->thr_m);
+  return NULL;
+}
+
+int oracle_rectrxm_cplx(char side, char uplo, char trans, double alpha_re, double alpha_im, char func, int dtype,
+                        int64_t n, int64_t m, double* A, int64_t lda, double* B, int64_t ldb, int64_t thr_s,
+                        int64_t thr_m, int nthreads) {
+  if (n < 0 || m < 0 || lda < (n > 1 ? n : 1) || thr_s < 1 || thr_m < 1 || (dtype != 3 && dtype != 4)) return -1;
+  int64_t rows = side == 'L' ? n : m;
+  if (ldb < (rows > 1 ? rows : 1)) return -1;
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > m) nthreads = (int)(m > 0 ? m : 1);
+  zjob* jobs = (zjob*)calloc((size_t)nthreads, sizeof(zjob));
+  pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+  char* started = (char*)calloc((size_t)nthreads, 1);
+  if (!jobs || !th || !started) {
+    free(jobs);
+    free(th);
+    free(started);
+    return -1;
+  }
+  zview Av = {A, lda, 0, 0};
+  int64_t start = 0;
+  for (int t = 0; t < nthreads; ++t) {
+    int64_t cnt = m / nthreads + (t < m % nthreads ? 1 : 0);
+    zview Bv = {B, ldb, 0, 0};
+    Bv = side == 'L' ? zsub(Bv, 0, start) : zsub(Bv, start, 0);
+    zjob j = {side, uplo, trans, func, {alpha_re, alpha_im}, dtype, Av, n, Bv, cnt, thr_s, thr_m};
+    jobs[t] = j;
+    start += cnt;
+  }
+  for (int t = 1; t < nthreads; ++t) {
+    if (pthread_create(&th[t], NULL, zjob_thread, &jobs[t]) == 0)
+      started[t] = 1;
+    else
+      zjob_thread(&jobs[t]);
+  }
+  zjob_thread(&jobs[0]);
+  for (int t = 1; t < nthreads; ++t)
+    if (started[t]) pthread_join(th[t], NULL);
+  free(started);
+  free(jobs);
+  free(th);
+  return 0;
+}

@@ -93,3 +93,26 @@ def test_float16_rounds_every_operation(oracle):
     # alpha * b = 3 * (1 + 2^-10) = 3.0029296875 -> Float16 spacing at 3 is 2^-9
     X = oracle.rectrxm("L", "L", "N", 3.0, "M", A, B)
     assert float(X[0, 0]) == float(np.float16(3.0 * (1.0 + 2.0 ** -10)))
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-14), (np.complex64, 1e-5)])
+def test_complex_contract(oracle, dtype, tol):
+    """The complex restatement meets the reference's real contract against
+    BLAS ztrsm/ztrmm (ctrsm/ctrmm) for every side, uplo, trans (with 'C' the
+    conjugate transpose) and both functions, with a complex alpha."""
+    rng = np.random.default_rng(13)
+    for n, m, side, uplo, trans, func in itertools.product([16, 300], [1, 9], "LR", "LU", "NTC", "SM"):
+        Z = (rng.random((n, n)) + 1) + 1j * (rng.random((n, n)) - 0.5)
+        A = (np.tril(Z) if uplo == "L" else np.triu(Z)) + 10 * np.eye(n)
+        shape = (n, m) if side == "L" else (m, n)
+        B = rng.random(shape) + 1j * rng.random(shape)
+        X = oracle.rectrxm_complex(side, uplo, trans, 0.5 - 0.25j, func, A.astype(dtype), B.astype(dtype),
+                                   nthreads=4)
+        assert X.dtype == dtype
+        ref = oracle.blas_rectrxm(side, uplo, trans, 0.5 - 0.25j, func, A.astype(dtype), B.astype(dtype))
+        assert oracle.rel_err(X, ref) < tol, (n, m, side, uplo, trans, func)
+    # 'C' conjugates: it differs from 'T' on complex data
+    A = np.tril(rng.random((6, 6)) + 1j * rng.random((6, 6))) + 5 * np.eye(6)
+    B = rng.random((6, 2)) + 0j
+    assert oracle.rel_err(oracle.rectrxm_complex("L", "L", "T", 1, "M", A, B),
+                          oracle.rectrxm_complex("L", "L", "C", 1, "M", A, B)) > 1e-3
