@@ -42,7 +42,9 @@ class BatchPlan:
         import torch
 
         self.dtype = dtype
-        code = {torch.float16: _lib.NLA_F16, torch.float32: _lib.NLA_F32, torch.float64: _lib.NLA_F64}[dtype]
+        code = {torch.float16: _lib.NLA_F16, torch.float32: _lib.NLA_F32, torch.float64: _lib.NLA_F64}.get(dtype)
+        if code is None:
+            raise ValueError("batched solves take Float16, Float32 or Float64, got %s" % dtype)
         arr = (_lib.BatchDesc * max(len(systems), 1))()
         for i, s in enumerate(systems):
             arr[i] = _lib.BatchDesc(*[int(v) for v in s])

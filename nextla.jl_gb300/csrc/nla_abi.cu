@@ -111,6 +111,7 @@ __global__ void scale_kernel(int64_t rows, int64_t cols, Tm alpha, T* B, int64_t
 }
 
 int launch_scale(int dtype, int64_t rows, int64_t cols, double alpha, const Mat& B, cudaStream_t s) {
+  if (is_complex(dtype)) return launch_scale_complex(dtype, rows, cols, alpha, 0.0, B, s);
   if (rows <= 0 || cols <= 0 || alpha == 1.0) return NLA_OK;
   const int64_t total = rows * cols;
   int64_t blocks = (total + 255) / 256;
@@ -156,6 +157,7 @@ static bool umma_enabled() {
 // cores (FP32 accumulation); everything else on CUDA cores.
 int launch_gemm(int dtype, int64_t N, int64_t M, int64_t K, double alpha, const Mat& A, const Mat& B, const Mat& C,
                 cudaStream_t s) {
+  if (is_complex(dtype)) return launch_gemm_complex(dtype, N, M, K, alpha, A, B, C, s);
   if (dtype == NLA_F16 && umma_enabled() && N >= 128 && M >= 128 && K >= 64)
     return launch_sliced_gemm(N, M, K, alpha, A, B, C, NLA_F16, NLA_F16, 1, false, nullptr, 0, s);
   return launch_gemm_simt(dtype, N, M, K, alpha, A, B, C, s);
@@ -175,7 +177,9 @@ static bool valid_side(char c) { return c == 'L' || c == 'R'; }
 static bool valid_uplo(char c) { return c == 'L' || c == 'U'; }
 static bool valid_trans(char c) { return c == 'N' || c == 'T' || c == 'C'; }
 static bool valid_func(char c) { return c == 'S' || c == 'M'; }
-static bool valid_dtype(int d) { return d == NLA_F16 || d == NLA_F32 || d == NLA_F64; }
+static bool valid_dtype(int d) {
+  return d == NLA_F16 || d == NLA_F32 || d == NLA_F64 || d == NLA_C32 || d == NLA_C64;
+}
 
 int check_flags(char side, char uplo, char trans, char func, int dtype) {
   if (!valid_side(side)) return fail(NLA_ERR_ARG, std::string("side must be 'L' or 'R', got '") + side + "'");
@@ -183,7 +187,7 @@ int check_flags(char side, char uplo, char trans, char func, int dtype) {
   if (!valid_trans(trans))
     return fail(NLA_ERR_ARG, std::string("transpose must be 'N', 'T' or 'C', got '") + trans + "'");
   if (!valid_func(func)) return fail(NLA_ERR_ARG, std::string("func must be 'S' or 'M', got '") + func + "'");
-  if (!valid_dtype(dtype)) return fail(NLA_ERR_DTYPE, "dtype must be NLA_F16, NLA_F32 or NLA_F64");
+  if (!valid_dtype(dtype)) return fail(NLA_ERR_DTYPE, "dtype must be NLA_F16, NLA_F32, NLA_F64, NLA_C32 or NLA_C64");
   return NLA_OK;
 }
 
@@ -290,23 +294,32 @@ int trxm_plan(char side, char uplo, char trans, char func, int dtype, int64_t n,
   c->unit = unit;
   const int64_t cut = func == 'S' ? (cutoff_s > 0 ? cutoff_s : default_cutoff('S', dtype))
                                   : (cutoff_m > 0 ? cutoff_m : default_cutoff('M', dtype));
-  c->threshold = cut > 1024 ? 1024 : cut;
+  // Complex diagonal blocks hold their rows of right-hand sides and a panel
+  // of the triangle in shared memory: at most 128 rows.
+  const int64_t cap = is_complex(dtype) ? 128 : 1024;
+  c->threshold = cut > cap ? cap : cut;
   return NLA_OK;
 }
 
 int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
               const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, cudaStream_t s,
-              bool unit) {
+              bool unit, double alpha_im) {
   RecPlan c{};
   int at = 0;
   NLA_TRY(trxm_plan(side, uplo, trans, func, dtype, n, m, A, lda, B, ldb, cutoff_s, cutoff_m, s, unit, &c, &at));
+  if (alpha_im != 0.0 && !is_complex(dtype)) return fail(NLA_ERR_DTYPE, "a complex alpha needs a complex dtype");
   if (n == 0 || m == 0) return NLA_OK;
-  const Mat Am{const_cast<void*>(A), lda, at};
+  Mat Am{const_cast<void*>(A), lda, at};
+  Am.c = trans == 'C' && is_complex(dtype);  // Adjoint(A), src/rectrxm.jl:56-59
   const Mat Bm{B, ldb, 0};
   const int64_t rows = side == 'L' ? n : m, cols = side == 'L' ? m : n;
-  if (func == 'S') NLA_TRY(launch_scale(dtype, rows, cols, alpha, Bm, s));  // src/rectrxm.jl:64
+  auto scale = [&]() {
+    return is_complex(dtype) ? launch_scale_complex(dtype, rows, cols, alpha, alpha_im, Bm, s)
+                             : launch_scale(dtype, rows, cols, alpha, Bm, s);
+  };
+  if (func == 'S') NLA_TRY(scale());  // src/rectrxm.jl:64
   NLA_TRY(recurse(c, Am, n, Bm));
-  if (func == 'M') NLA_TRY(launch_scale(dtype, rows, cols, alpha, Bm, s));  // src/rectrxm.jl:72
+  if (func == 'M') NLA_TRY(scale());  // src/rectrxm.jl:72
   return NLA_OK;
 }
 
@@ -359,6 +372,14 @@ int nla_trxm(char side, char uplo, char trans, double alpha, char func, int dtyp
   return trxm_impl(side, uplo, trans, alpha, func, dtype, n, m, A, lda, B, ldb, 0, 0, (cudaStream_t)stream);
 }
 
+int nla_trxm_complex(char side, char uplo, char trans, double alpha_re, double alpha_im, char func, int dtype,
+                     int64_t n, int64_t m, const void* A, int64_t lda, void* B, int64_t ldb, void* stream) {
+  clear_error();
+  if (!is_complex(dtype)) return fail(NLA_ERR_DTYPE, "nla_trxm_complex: dtype must be NLA_C32 or NLA_C64");
+  return trxm_impl(side, uplo, trans, alpha_re, func, dtype, n, m, A, lda, B, ldb, 0, 0, (cudaStream_t)stream, false,
+                   alpha_im);
+}
+
 int nla_trxm_ex(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
                 const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, void* stream) {
   clear_error();
@@ -382,7 +403,8 @@ int nla_diag_block(char func, char side, char uplo, int transA, int dtype, int64
   if (n > 1024) return fail(NLA_ERR_ARG, "diag block: n must be <= 1024");
   NLA_TRY(check_matrix("A", A, n, n, lda));
   NLA_TRY(check_matrix("B", B, side == 'L' ? n : m, side == 'L' ? m : n, ldb));
-  Mat Am{const_cast<void*>(A), lda, transA ? 1 : 0};
+  Mat Am{const_cast<void*>(A), lda, transA & 1};
+  Am.c = (transA & 2) && is_complex(dtype);
   Mat Bm{B, ldb, 0};
   return launch_leaf(func, side, uplo, dtype, n, m, Am, Bm, (cudaStream_t)stream);
 }
@@ -390,23 +412,35 @@ int nla_diag_block(char func, char side, char uplo, int transA, int dtype, int64
 int nla_gemm_update(int dtype, int trans1, int trans2, int64_t N, int64_t R, int64_t M, double alpha,
                     const void* in1, int64_t ld1, const void* in2, int64_t ld2, void* out, int64_t ldo, void* stream) {
   clear_error();
-  if (!valid_dtype(dtype)) return fail(NLA_ERR_DTYPE, "dtype must be NLA_F16, NLA_F32 or NLA_F64");
+  if (!valid_dtype(dtype)) return fail(NLA_ERR_DTYPE, "dtype must be NLA_F16, NLA_F32, NLA_F64, NLA_C32 or NLA_C64");
   if (N < 0 || R < 0 || M < 0) return fail(NLA_ERR_ARG, "N, R and M must be non-negative");
-  NLA_TRY(check_matrix("in1", in1, trans1 ? R : N, trans1 ? N : R, ld1));
-  NLA_TRY(check_matrix("in2", in2, trans2 ? M : R, trans2 ? R : M, ld2));
+  const int t1 = trans1 & 1, t2 = trans2 & 1;
+  NLA_TRY(check_matrix("in1", in1, t1 ? R : N, t1 ? N : R, ld1));
+  NLA_TRY(check_matrix("in2", in2, t2 ? M : R, t2 ? R : M, ld2));
   NLA_TRY(check_matrix("out", out, N, M, ldo));
-  Mat A{const_cast<void*>(in1), ld1, trans1 ? 1 : 0};
-  Mat B{const_cast<void*>(in2), ld2, trans2 ? 1 : 0};
+  Mat A{const_cast<void*>(in1), ld1, t1};
+  Mat B{const_cast<void*>(in2), ld2, t2};
+  A.c = (trans1 & 2) && is_complex(dtype);
+  B.c = (trans2 & 2) && is_complex(dtype);
   Mat C{out, ldo, 0};
   return launch_gemm(dtype, N, M, R, alpha, A, B, C, (cudaStream_t)stream);
 }
 
 int nla_scale(int dtype, int64_t rows, int64_t cols, double alpha, void* B, int64_t ldb, void* stream) {
   clear_error();
-  if (!valid_dtype(dtype)) return fail(NLA_ERR_DTYPE, "dtype must be NLA_F16, NLA_F32 or NLA_F64");
+  if (!valid_dtype(dtype)) return fail(NLA_ERR_DTYPE, "dtype must be NLA_F16, NLA_F32, NLA_F64, NLA_C32 or NLA_C64");
   NLA_TRY(check_matrix("B", B, rows, cols, ldb));
   Mat Bm{B, ldb, 0};
   return launch_scale(dtype, rows, cols, alpha, Bm, (cudaStream_t)stream);
+}
+
+int nla_scale_complex(int dtype, int64_t rows, int64_t cols, double alpha_re, double alpha_im, void* B, int64_t ldb,
+                      void* stream) {
+  clear_error();
+  if (!is_complex(dtype)) return fail(NLA_ERR_DTYPE, "nla_scale_complex: dtype must be NLA_C32 or NLA_C64");
+  NLA_TRY(check_matrix("B", B, rows, cols, ldb));
+  Mat Bm{B, ldb, 0};
+  return launch_scale_complex(dtype, rows, cols, alpha_re, alpha_im, Bm, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -41,9 +41,12 @@ struct Mat {
   void* p;
   int64_t ld;
   int t;
+  int c = 0;  // complex types: read the conjugate of every element (an Adjoint view with t set)
 };
 
-inline size_t dtype_size(int dtype) { return dtype == NLA_F64 ? 8 : dtype == NLA_F32 ? 4 : 2; }
+inline size_t dtype_size(int dtype) {
+  return dtype == NLA_C64 ? 16 : dtype == NLA_F64 || dtype == NLA_C32 ? 8 : dtype == NLA_F32 ? 4 : 2;
+}
 
 // Element offset of (i, j) in a view.
 __host__ __device__ inline int64_t mat_off(int64_t i, int64_t j, int64_t ld, int t) {
@@ -117,6 +120,16 @@ int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m
 
 // B .= alpha .* B on a rows x cols view.
 int launch_scale(int dtype, int64_t rows, int64_t cols, double alpha, const Mat& B, cudaStream_t s);
+
+// Complex element types (nla_complex.cu): the same three pieces, with
+// conjugated views (Mat::c) and a complex alpha for the scaling.
+bool is_complex(int dtype);
+int launch_leaf_complex(char func, char side, char uplo, int dtype, int64_t n, int64_t m, const Mat& A, const Mat& B,
+                        cudaStream_t s, bool unit);
+int launch_gemm_complex(int dtype, int64_t N, int64_t M, int64_t K, double alpha, const Mat& A, const Mat& B,
+                        const Mat& C, cudaStream_t s);
+int launch_scale_complex(int dtype, int64_t rows, int64_t cols, double alpha_re, double alpha_im, const Mat& B,
+                         cudaStream_t s);
 
 // Tensor-core update on staged slices (nla_umma.cu).  C (M x N) += alpha *
 // op(A) (M x K) * op(B) (K x N); in_dtype NLA_F64 (split into S BF16/FP16
@@ -192,7 +205,7 @@ int trxm_plan(char side, char uplo, char trans, char func, int dtype, int64_t n,
               RecPlan* c, int* a_trans);
 int trxm_impl(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
               const void* A, int64_t lda, void* B, int64_t ldb, int64_t cutoff_s, int64_t cutoff_m, cudaStream_t s,
-              bool unit = false);
+              bool unit = false, double alpha_im = 0.0);
 // The mixed-precision recursion behind nla_trxm_mixed, and its checks and plan
 // (which also sizes the update workspace on stream s).
 int mixed_plan(char side, char uplo, char trans, char func, int64_t n, int64_t m, const void* A, int64_t lda,

@@ -241,6 +241,7 @@ int launch_solve_wide<double>(const LeafArgs& g, int, cudaStream_t s) {
 
 int launch_leaf(char func, char side, char uplo, int dtype, int64_t n, int64_t m, const Mat& A, const Mat& B,
                 cudaStream_t s, bool unit) {
+  if (is_complex(dtype)) return launch_leaf_complex(func, side, uplo, dtype, n, m, A, B, s, unit);
   if (n <= 0 || m <= 0) return NLA_OK;
   if (n > 1024) return fail(NLA_ERR_ARG, "diag block: n must be <= 1024");
   if (B.t) return fail(NLA_ERR_UNSUPPORTED, "diag block: transposed B view");

@@ -29,10 +29,14 @@ const libnla = get(ENV, "NEXTLA_GB300_LIB", joinpath(@__DIR__, "..", "libnextla_
 const NLA_F16 = Cint(0)
 const NLA_F32 = Cint(1)
 const NLA_F64 = Cint(2)
+const NLA_C32 = Cint(3)
+const NLA_C64 = Cint(4)
 
 dtype_code(::Type{Float16}) = NLA_F16
 dtype_code(::Type{Float32}) = NLA_F32
 dtype_code(::Type{Float64}) = NLA_F64
+dtype_code(::Type{ComplexF32}) = NLA_C32
+dtype_code(::Type{ComplexF64}) = NLA_C64
 
 function check(rc::Cint)
     rc == 0 && return nothing
@@ -77,6 +81,31 @@ function unified_rectrxm!(side::Char, uplo::Char, transpose::Char, alpha::Number
                 (Cchar, Cchar, Cchar, Cdouble, Cchar, Cint, Int64, Int64, CuPtr{Cvoid}, Int64, CuPtr{Cvoid}, Int64,
                  Ptr{Cvoid}),
                 side, up, tr, Float64(alpha), func, dtype_code(T), n, m, pA, lda, pB, ldb, stream_handle()))
+    return B
+end
+
+"""
+    unified_rectrxm!(side, uplo, transpose, alpha, func, A, B) -> B   (ComplexF32, ComplexF64)
+
+The same for complex CuArrays (`nla_trxm_complex`): the reference's
+unified_rec takes only real element types (src/rectrxm.jl:101), though its
+base-case docstrings list complex ones (src/trsm.jl:180-183).  transpose 'C'
+applies the Adjoint; alpha may be complex.  A plain (not Transpose or
+Adjoint) A is expected.
+"""
+function unified_rectrxm!(side::Char, uplo::Char, transpose::Char, alpha::Number, func::Char,
+                          A::AbstractMatrix{T}, B::AbstractMatrix{T}) where {T<:Union{ComplexF32,ComplexF64}}
+    n = size(A, 1)
+    m = side == 'L' ? size(B, 2) : size(B, 1)
+    pA, lda, tA = operand(A)
+    pB, ldb, tB = operand(B)
+    (tA || tB) && throw(ArgumentError("pass A and B as plain column-major arrays and use `transpose`"))
+    a = ComplexF64(alpha)
+    check(ccall((:nla_trxm_complex, libnla), Cint,
+                (Cchar, Cchar, Cchar, Cdouble, Cdouble, Cchar, Cint, Int64, Int64, CuPtr{Cvoid}, Int64, CuPtr{Cvoid},
+                 Int64, Ptr{Cvoid}),
+                side, uplo, transpose, real(a), imag(a), func, dtype_code(T), n, m, pA, lda, pB, ldb,
+                stream_handle()))
     return B
 end
 

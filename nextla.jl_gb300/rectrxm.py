@@ -35,29 +35,39 @@ def _dtype_code(t) -> int:
     if _DTYPE_CODES is None:
         import torch
 
-        _DTYPE_CODES = {torch.float16: _lib.NLA_F16, torch.float32: _lib.NLA_F32, torch.float64: _lib.NLA_F64}
+        _DTYPE_CODES = {torch.float16: _lib.NLA_F16, torch.float32: _lib.NLA_F32, torch.float64: _lib.NLA_F64,
+                        torch.complex64: _lib.NLA_C32, torch.complex128: _lib.NLA_C64}
     try:
         return _DTYPE_CODES[t.dtype]
     except KeyError:
-        raise ValueError("element type must be Float16, Float32 or Float64, got %s" % t.dtype) from None
+        raise ValueError("element type must be Float16, Float32, Float64, ComplexF32 or ComplexF64, got %s"
+                         % t.dtype) from None
+
+
+def _is_complex(t) -> bool:
+    return t.dtype.is_complex
 
 
 def _mat(X):
-    """(pointer, leading dimension, transposed) of a 2-D strided view."""
+    """(pointer, leading dimension, transposed) of a 2-D strided view.  A
+    complex view with torch's conjugate bit set (``A.T.conj()``, Julia's
+    Adjoint) adds 2 to the transposed flag: the library then reads the
+    conjugate of every element."""
     if X.dim() != 2:
         raise ValueError("expected a matrix, got a tensor of shape %s" % (tuple(X.shape),))
     if not X.is_cuda:
         raise ValueError("expected a CUDA tensor (the reference's CuArray), got one on %s" % X.device)
     r, c = X.shape
     s0, s1 = X.stride()
+    cj = 2 if X.is_conj() else 0
     if s0 == 1 or r <= 1:
         ld = s1 if c > 1 else max(r, 1)
         if ld >= max(r, 1):
-            return X.data_ptr(), ld, 0
+            return X.data_ptr(), ld, 0 | cj
     if s1 == 1 or c <= 1:
         ld = s0 if r > 1 else max(c, 1)
         if ld >= max(c, 1):
-            return X.data_ptr(), ld, 1
+            return X.data_ptr(), ld, 1 | cj
     raise ValueError("matrix views need a unit stride in one dimension (strides %s)" % ((s0, s1),))
 
 
@@ -183,12 +193,17 @@ def GEMM_SUB_(A, B, C):
 
 
 def scale_(B, alpha):
-    """B .= alpha .* B (src/rectrxm.jl:64,72), Float64 product rounded to B's type."""
+    """B .= alpha .* B (src/rectrxm.jl:64,72), Float64 (ComplexF64) product
+    rounded to B's type."""
     b, ldb, tb = _mat(B)
     if tb:
         raise ValueError("B must be a column-major view")
     L = _lib.load()
-    _lib.check(L.nla_scale(_dtype_code(B), B.shape[0], B.shape[1], float(alpha), b, ldb, _stream(B)))
+    if _is_complex(B):
+        a = complex(alpha)
+        _lib.check(L.nla_scale_complex(_dtype_code(B), B.shape[0], B.shape[1], a.real, a.imag, b, ldb, _stream(B)))
+    else:
+        _lib.check(L.nla_scale(_dtype_code(B), B.shape[0], B.shape[1], float(alpha), b, ldb, _stream(B)))
     return B
 
 
@@ -373,26 +388,43 @@ def unified_rectrxm_(side, uplo, transpose, alpha, func, A, B, *, native=False, 
     """
     _check_flags(side, uplo, transpose, func)
     _check_operands(A, B, side)
+    cplx = _is_complex(B)
+    if B.is_conj():
+        raise ValueError("B must not be a conjugate view (resolve it with B.resolve_conj())")
     n = A.shape[0]
     if native:
         a, lda, ta = _mat(A)
         b, ldb, tb = _mat(B)
         if tb:
             raise ValueError("B must be a column-major view")
+        if ta & 2:
+            raise ValueError("pass A without torch's conjugate bit and use transpose='C'")
         tr, up = transpose, uplo
         if ta:  # A is a transposed view of its parent: fold that into the flags
+            if cplx and transpose == "C":
+                raise ValueError("a transposed view of a complex A with transpose='C' is a conjugate without "
+                                 "transpose, which unified_rectrxm! cannot express; pass the parent")
             tr = "N" if transpose in ("T", "C") else "T"
             up = "U" if uplo == "L" else "L"
         m = B.shape[1] if side == "L" else B.shape[0]
-        cs, cm = thresholds if thresholds is not None else (0, 0)
         L = _lib.load()
-        _lib.check(L.nla_trxm_ex(_lib.ch(side), _lib.ch(up), _lib.ch(tr), float(alpha), _lib.ch(func),
-                                 _dtype_code(B), n, m, a, lda, b, ldb, int(cs), int(cm), _stream(B)))
+        if cplx and complex(alpha).imag != 0.0:
+            if thresholds is not None:
+                raise ValueError("thresholds are not supported with a complex alpha")
+            a_ = complex(alpha)
+            _lib.check(L.nla_trxm_complex(_lib.ch(side), _lib.ch(up), _lib.ch(tr), a_.real, a_.imag, _lib.ch(func),
+                                          _dtype_code(B), n, m, a, lda, b, ldb, _stream(B)))
+            return B
+        cs, cm = thresholds if thresholds is not None else (0, 0)
+        _lib.check(L.nla_trxm_ex(_lib.ch(side), _lib.ch(up), _lib.ch(tr), float(complex(alpha).real),
+                                 _lib.ch(func), _dtype_code(B), n, m, a, lda, b, ldb, int(cs), int(cm), _stream(B)))
         return B
 
     threshold = 16 if thresholds is None else int(thresholds[1])
     if transpose in ("T", "C"):
-        A = A.T  # Transpose(A); for real data Adjoint(A) is the same view
+        # Transpose(A), or Adjoint(A): for complex data the conjugate view,
+        # which the base cases and updates read through torch's conjugate bit.
+        A = A.T.conj() if (cplx and transpose == "C") else A.T
         uplo = "U" if uplo == "L" else "L"
     if func == "S":
         threshold = 256 if thresholds is None else int(thresholds[0])
