@@ -52,6 +52,8 @@ constexpr int RT = 4;            // rows per thread (strided by ROW_GROUPS)
 constexpr int PANEL = 16;        // triangle panel of a leaf
 constexpr int LEAF_PAD = 1;      // row padding of the staged diagonal block
 
+static_assert(NT % MAX_ROWS == 0 && NT % 32 == 0 && NT % 16 == 0, "staging index steps");
+
 enum { NODE_LEAF = 0, NODE_UPDATE = 1 };
 enum { FLAG_ALPHA = 1 };
 
@@ -147,6 +149,46 @@ template <> __device__ __forceinline__ float scaled<__half>(__half b, double alp
   return __half2float(__double2half(alpha * (double)__half2float(b)));
 }
 
+// N consecutive compute-type values from shared memory, read as the widest
+// vectors N allows (callers keep p aligned to that width).
+template <int N>
+__device__ __forceinline__ void lds_vec(const float* p, float (&v)[N]) {
+  if constexpr (N % 4 == 0) {
+#pragma unroll
+    for (int j = 0; j < N; j += 4) {
+      const float4 q = *reinterpret_cast<const float4*>(p + j);
+      v[j] = q.x;
+      v[j + 1] = q.y;
+      v[j + 2] = q.z;
+      v[j + 3] = q.w;
+    }
+  } else if constexpr (N % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < N; j += 2) {
+      const float2 q = *reinterpret_cast<const float2*>(p + j);
+      v[j] = q.x;
+      v[j + 1] = q.y;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < N; ++j) v[j] = p[j];
+  }
+}
+template <int N>
+__device__ __forceinline__ void lds_vec(const double* p, double (&v)[N]) {
+  if constexpr (N % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < N; j += 2) {
+      const double2 q = *reinterpret_cast<const double2*>(p + j);
+      v[j] = q.x;
+      v[j + 1] = q.y;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < N; ++j) v[j] = p[j];
+  }
+}
+
 // Element offsets in canonical coordinates: row i / column k of the lower
 // triangle applied from the left (rev maps i -> n - 1 - i; tA reads A's
 // transpose).
@@ -171,9 +213,11 @@ __host__ __device__ constexpr size_t leaf_elems(int W) {
 // ---------------------------------------------------------------------------
 // UPDATE: X[r0 + r, c] = base(r, c) - sum_k A[r0 + r, k0 + k] X[k0 + k, c] for
 // r < rows, c < ncols, base = alpha B (first touch) or B.  Thread (tr, tc)
-// owns rows tr + 16 i (i < 4) and columns tc * CT .. + CT.  K is walked in
-// chunks of KC staged in shared memory (A k-major, X k-major), the next
-// chunk's elements prefetched into registers during the current chunk.
+// owns rows 4 tr .. 4 tr + 3 and columns tc * CT .. + CT, both read from
+// shared memory as vectors (A's 4 values serve 16 lanes of a warp, X's CT
+// values are broadcasts).  K is walked in chunks of KC staged in shared
+// memory (A k-major, X k-major), the next chunk's elements prefetched into
+// registers during the current chunk.
 // ---------------------------------------------------------------------------
 template <typename T, int W>
 __device__ void run_update(const Args& a, const Node& nd, const Group& g, const nla_batch_desc& d, void* smem) {
@@ -188,6 +232,7 @@ __device__ void run_update(const Args& a, const Node& nd, const Group& g, const 
   const T* B = static_cast<const T*>(a.B);
   const int t = threadIdx.x, tr = t % ROW_GROUPS, tc = t / ROW_GROUPS;
   const int rows = nd.rows, ncols = g.ncols;
+  const bool warp_cols_live = (tc & ~1) * CT < ncols;  // the warp's first column group
 
   Tc acc[RT][CT];
 #pragma unroll
@@ -195,38 +240,38 @@ __device__ void run_update(const Args& a, const Node& nd, const Group& g, const 
 #pragma unroll
     for (int c = 0; c < CT; ++c) acc[i][c] = Tc(0);
 
+  // Element (r, k) of a chunk, for this thread's u-th load: A's canonical
+  // (r0 + r, k0 + k) and X's (k0 + k, c0 + c) are affine in r, k and c, and
+  // (NT being a multiple of 64 and KC) so is u: every load below is a base
+  // address plus u times a per-node stride.
+  const int64_t sgn = a.rev ? -1 : 1;
+  const int64_t dr = sgn * (a.tA ? d.lda : 1), dk = sgn * (a.tA ? 1 : d.lda);
+  const int ar = a.tA ? t / KC : t % MAX_ROWS, ak = a.tA ? t % KC : t / MAX_ROWS;
+  const int ar_step = a.tA ? NT / KC : 0, ak_step = a.tA ? 0 : NT / MAX_ROWS;
+  const int64_t a_step = (int64_t)ar_step * dr + (int64_t)ak_step * dk;
+  const int xk = t % KC, xc = t / KC;
+  constexpr int XC_STEP = NT / KC;
+  const int64_t x_step = (int64_t)XC_STEP * d.ldb;
+  const T* A0 = A + a_at(d, a.tA, a.rev, nd.r0, nd.k0) + ar * dr + ak * dk;
+  const T* X0 = B + b_at(d, a.rev, nd.k0, g.c0) + sgn * xk + (int64_t)xc * d.ldb;
+
   Tc pa[A_PER], px[X_PER];
   auto fetch = [&](int k0) {
     const int kw = min(KC, nd.k0 + nd.kw - k0);
+    const T* pA = A0 + (int64_t)(k0 - nd.k0) * dk;
+    const T* pX = X0 + (int64_t)(k0 - nd.k0) * sgn;
 #pragma unroll
-    for (int u = 0; u < A_PER; ++u) {
-      const int idx = t + u * NT;
-      int r, k;
-      if (!a.tA) { r = idx % MAX_ROWS; k = idx / MAX_ROWS; }
-      else { k = idx % KC; r = idx / KC; }
-      pa[u] = r < rows && k < kw ? to_c(A[a_at(d, a.tA, a.rev, nd.r0 + r, k0 + k)]) : Tc(0);
-    }
+    for (int u = 0; u < A_PER; ++u)
+      pa[u] = ar + u * ar_step < rows && ak + u * ak_step < kw ? to_c(pA[u * a_step]) : Tc(0);
 #pragma unroll
-    for (int u = 0; u < X_PER; ++u) {
-      const int idx = t + u * NT;
-      const int k = idx % KC, c = idx / KC;
-      px[u] = k < kw && c < ncols ? to_c(ldcg(B + b_at(d, a.rev, k0 + k, g.c0 + c))) : Tc(0);
-    }
+    for (int u = 0; u < X_PER; ++u)
+      px[u] = xk < kw && xc + u * XC_STEP < ncols ? to_c(ldcg(pX + u * x_step)) : Tc(0);
   };
   auto stash = [&]() {
 #pragma unroll
-    for (int u = 0; u < A_PER; ++u) {
-      const int idx = t + u * NT;
-      int r, k;
-      if (!a.tA) { r = idx % MAX_ROWS; k = idx / MAX_ROWS; }
-      else { k = idx % KC; r = idx / KC; }
-      As[k * AP + r] = pa[u];
-    }
+    for (int u = 0; u < A_PER; ++u) As[(ak + u * ak_step) * AP + ar + u * ar_step] = pa[u];
 #pragma unroll
-    for (int u = 0; u < X_PER; ++u) {
-      const int idx = t + u * NT;
-      Xs[(idx % KC) * XP + idx / KC] = px[u];
-    }
+    for (int u = 0; u < X_PER; ++u) Xs[xk * XP + xc + u * XC_STEP] = px[u];
   };
 
   const int kend = nd.k0 + nd.kw;
@@ -236,14 +281,15 @@ __device__ void run_update(const Args& a, const Node& nd, const Group& g, const 
     stash();
     __syncthreads();
     if (k0 + KC < kend) fetch(k0 + KC);
-    const int kw = min(KC, kend - k0);
+    // A warp holds the columns of two column groups; one whose columns all
+    // lie past the group's right-hand sides (a narrow block in a wider
+    // template) skips the products.
+    const int kw = warp_cols_live ? min(KC, kend - k0) : 0;
 #pragma unroll 4
     for (int k = 0; k < kw; ++k) {
       Tc av[RT], xv[CT];
-#pragma unroll
-      for (int i = 0; i < RT; ++i) av[i] = As[k * AP + tr + ROW_GROUPS * i];
-#pragma unroll
-      for (int c = 0; c < CT; ++c) xv[c] = Xs[k * XP + tc * CT + c];
+      lds_vec<RT>(As + k * AP + RT * tr, av);
+      lds_vec<CT>(Xs + k * XP + tc * CT, xv);
 #pragma unroll
       for (int i = 0; i < RT; ++i)
 #pragma unroll
@@ -254,7 +300,7 @@ __device__ void run_update(const Args& a, const Node& nd, const Group& g, const 
   const bool first = nd.flags & FLAG_ALPHA;
 #pragma unroll
   for (int i = 0; i < RT; ++i) {
-    const int r = tr + ROW_GROUPS * i;
+    const int r = RT * tr + i;
     if (r >= rows) continue;
 #pragma unroll
     for (int c = 0; c < CT; ++c) {
@@ -287,30 +333,61 @@ __device__ void run_leaf(const Args& a, const Node& nd, const Group& g, const nl
   const int t = threadIdx.x, rows = nd.rows, ncols = g.ncols;
   const bool first = nd.flags & FLAG_ALPHA;
 
-  // Stage the block of A (threads along the index contiguous in memory) and X.
-  for (int idx = t; idx < rows * rows; idx += NT) {
-    int r, k;
-    if (!a.tA) { r = idx % rows; k = idx / rows; }
-    else { k = idx % rows; r = idx / rows; }
-    if (k < r) Ls[r * LP + k] = to_c(A[a_at(d, a.tA, a.rev, nd.r0 + r, nd.r0 + k)]);
-    else if (k == r) inv[r] = Tc(1) / to_c(A[a_at(d, a.tA, a.rev, nd.r0 + r, nd.r0 + r)]);
-  }
-  for (int idx = t; idx < rows * W; idx += NT) {
-    const int r = idx % rows, c = idx / rows;
-    Tc v = Tc(0);
-    if (c < ncols) {
-      const T b = ldcg(B + b_at(d, a.rev, nd.r0 + r, g.c0 + c));
-      v = first ? scaled<T>(b, a.alpha) : to_c(b);
+  // Stage the block of A (threads along the index contiguous in memory) and
+  // X; offsets are affine in the block's row and column (as in run_update).
+  // Each thread issues all of its loads of a block before it stores any, so
+  // their latencies overlap instead of adding up.
+  const int64_t sgn = a.rev ? -1 : 1;
+  const int64_t dr = sgn * (a.tA ? d.lda : 1), dk = sgn * (a.tA ? 1 : d.lda);
+  const T* A0 = A + a_at(d, a.tA, a.rev, nd.r0, nd.r0);
+  {
+    constexpr int PER = MAX_ROWS * MAX_ROWS / NT;
+    Tc v[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int idx = t + u * NT;
+      const int r = a.tA ? idx / MAX_ROWS : idx % MAX_ROWS, k = a.tA ? idx % MAX_ROWS : idx / MAX_ROWS;
+      v[u] = r < rows && k <= r ? to_c(A0[r * dr + k * dk]) : Tc(0);
     }
-    Xs[r * XP + c] = v;
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int idx = t + u * NT;
+      const int r = a.tA ? idx / MAX_ROWS : idx % MAX_ROWS, k = a.tA ? idx % MAX_ROWS : idx / MAX_ROWS;
+      if (r < rows && k < r) Ls[r * LP + k] = v[u];
+      else if (r < rows && k == r) inv[r] = Tc(1) / v[u];
+    }
+  }
+  const T* X0 = B + b_at(d, a.rev, nd.r0, g.c0);
+  {
+    constexpr int PER = MAX_ROWS * W / NT, BATCH = PER < 16 ? PER : 16;
+    const int r = t % MAX_ROWS;  // NT is a multiple of MAX_ROWS: each thread keeps one row
+    for (int u0 = 0; u0 < PER; u0 += BATCH) {
+      Tc v[BATCH];
+#pragma unroll
+      for (int u = 0; u < BATCH; ++u) {
+        const int c = (t + (u0 + u) * NT) / MAX_ROWS;
+        Tc x = Tc(0);
+        if (r < rows && c < ncols) {
+          const T b = ldcg(X0 + r * sgn + (int64_t)c * d.ldb);
+          x = first ? scaled<T>(b, a.alpha) : to_c(b);
+        }
+        v[u] = x;
+      }
+#pragma unroll
+      for (int u = 0; u < BATCH; ++u) {
+        const int c = (t + (u0 + u) * NT) / MAX_ROWS;
+        if (r < rows) Xs[r * XP + c] = v[u];
+      }
+    }
   }
   __syncthreads();
 
   const int tr = t % ROW_GROUPS, tc = t / ROW_GROUPS;
   for (int p0 = 0; p0 < rows; p0 += PANEL) {
     const int pw = min(PANEL, rows - p0);
-    // The panel's triangle: one right-hand side per thread.
-    if (t < W) {
+    // The panel's triangle: one right-hand side per thread (warps whose
+    // right-hand sides all lie past the group's skip it).
+    if (t < W && (t & ~31) < ncols) {
       Tc x[PANEL];
 #pragma unroll
       for (int i = 0; i < PANEL; ++i) {
@@ -327,7 +404,7 @@ __device__ void run_leaf(const Args& a, const Node& nd, const Group& g, const nl
     __syncthreads();
     // Rows below the panel: X[r, :] -= L[r, panel] X[panel, :].
     const int rb = p0 + pw;
-    if (rb < rows) {
+    if (rb < rows && (tc & ~1) * CT < ncols) {
       Tc acc[RT][CT];
 #pragma unroll
       for (int i = 0; i < RT; ++i)
@@ -356,9 +433,10 @@ __device__ void run_leaf(const Args& a, const Node& nd, const Group& g, const nl
     }
     __syncthreads();
   }
-  for (int idx = t; idx < rows * W; idx += NT) {
-    const int r = idx % rows, c = idx / rows;
-    if (c < ncols) Elem<T>::store(B + b_at(d, a.rev, nd.r0 + r, g.c0 + c), Xs[r * XP + c]);
+  T* Xw = B + b_at(d, a.rev, nd.r0, g.c0);
+  for (int idx = t; idx < MAX_ROWS * W; idx += NT) {
+    const int r = idx % MAX_ROWS, c = idx / MAX_ROWS;
+    if (r < rows && c < ncols) Elem<T>::store(Xw + r * sgn + (int64_t)c * d.ldb, Xs[r * XP + c]);
   }
 }
 
@@ -832,6 +910,7 @@ int plan_create(nla_batch_plan* out, int dtype, char uplo, char trans, int64_t c
   if (!out) return fail(NLA_ERR_ARG, "plan pointer is null");
   *out = nullptr;
   NLA_TRY(check_flags('L', uplo, trans, 'S', dtype));
+  if (is_complex(dtype)) return fail(NLA_ERR_DTYPE, "batch: real element types only");
   NLA_TRY(check_tuning(tun));
   if (count < 0 || (count > 0 && !descs)) return fail(NLA_ERR_ARG, "bad system count or descriptor array");
   if (count > (int64_t)1 << 24) return fail(NLA_ERR_UNSUPPORTED, "too many systems");
