@@ -37,10 +37,17 @@
 extern "C" {
 #endif
 
-/* Element types (Float16, Float32, Float64). */
+/* Element types (Float16, Float32, Float64; ComplexF32, ComplexF64 stored as
+ * interleaved (re, im) pairs, as Julia and torch store them).  The complex
+ * types run the plain path (nla_trxm, nla_trxm_ex, nla_trxm_diag,
+ * nla_trxm_complex, nla_diag_block, nla_gemm_update, nla_scale and the
+ * host-buffer nla_trxm_host); the mixed, batched and no-allocation forms are
+ * real only. */
 #define NLA_F16 0
 #define NLA_F32 1
 #define NLA_F64 2
+#define NLA_C32 3
+#define NLA_C64 4
 
 /* Status codes. */
 #define NLA_OK 0
@@ -67,12 +74,25 @@ NLA_API const char* nla_last_error(void);
  *   func 'M': B := alpha op(A) B ('L') or alpha B op(A) ('R').
  * A is n x n (only the `uplo` triangle is read, diagonal non-unit); B is
  * n x m for side 'L' and m x n for side 'R'; the result overwrites B.
- * dtype is NLA_F16, NLA_F32 or NLA_F64 and applies to A and B.
+ * dtype is NLA_F16, NLA_F32, NLA_F64, NLA_C32 or NLA_C64 and applies to A
+ * and B.  trans 'T' takes A's transpose, 'C' its conjugate transpose (the
+ * Adjoint wrapper; the same as 'T' for real types).
  * The recursion cut-offs are the library's tuned defaults (environment
- * NLA_TRXM_CUTOFF_S / NLA_TRXM_CUTOFF_M override them).
+ * NLA_TRXM_CUTOFF_S / NLA_TRXM_CUTOFF_M override them; complex diagonal
+ * blocks are at most 128).
  */
 NLA_API int nla_trxm(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
              const void* A, int64_t lda, void* B, int64_t ldb, void* stream);
+
+/*
+ * nla_trxm for complex element types with a complex alpha = alpha_re +
+ * i alpha_im (dtype NLA_C32 or NLA_C64).  The reference's unified_rec accepts
+ * only real element types (src/rectrxm.jl:101) though its base-case
+ * docstrings list complex ones (src/trsm.jl:180-183); this runs the same
+ * recursion on complex data.
+ */
+NLA_API int nla_trxm_complex(char side, char uplo, char trans, double alpha_re, double alpha_im, char func, int dtype,
+                             int64_t n, int64_t m, const void* A, int64_t lda, void* B, int64_t ldb, void* stream);
 
 /*
  * nla_trxm with explicit recursion cut-offs for solve and multiply (the
@@ -99,7 +119,9 @@ NLA_API int nla_trxm_diag(char side, char uplo, char trans, char diag, double al
  * LeftLowerTRMM!/LeftUpperTRMM!/RightLowerTRMM!/RightUpperTRMM!
  * (src/trmm.jl:332-389, kernels :43-312) for func 'M'.
  * op(A) = A (transA 0) or A^T (transA 1) is the n x n triangle named by uplo
- * (the reference passes Transpose views here); B is n x m (side 'L') or
+ * (the reference passes Transpose views here); for complex types bit 1 of
+ * transA conjugates A's elements (3: the conjugate transpose); B is n x m
+ * (side 'L') or
  * m x n (side 'R').  No alpha: the reference's base cases have none.
  * n <= 1024 (the reference's shared buffers hold 1024 entries,
  * src/trsm.jl:10-12).
@@ -112,7 +134,8 @@ NLA_API int nla_diag_block(char func, char side, char uplo, int transA, int dtyp
  * Replaces matmul! (src/matmul.jl:5-66) as launched by GEMM_ADD!
  * (src/matmul.jl:69-74, alpha = +1) and GEMM_SUB! (src/matmul.jl:76-81,
  * alpha = -1).  trans1/trans2 select op() = transpose (1) or identity (0),
- * matching matmul!'s transA/transB arguments for real data.  Float16 inputs
+ * matching matmul!'s transA/transB arguments for real data; for complex
+ * types bit 1 also conjugates the operand (3: conjugate transpose).  Float16 inputs
  * accumulate in Float32 (the reference accumulates in Float16).
  * `out` must not overlap `in1` or `in2`.
  */
@@ -124,6 +147,21 @@ NLA_API int nla_gemm_update(int dtype, int trans1, int trans2, int64_t N, int64_
  * in Float64 and rounded back to the element type, as Julia's promotion does.
  */
 NLA_API int nla_scale(int dtype, int64_t rows, int64_t cols, double alpha, void* B, int64_t ldb, void* stream);
+
+/* nla_scale for complex types with a complex alpha (the product in
+ * ComplexF64, rounded to the element type). */
+NLA_API int nla_scale_complex(int dtype, int64_t rows, int64_t cols, double alpha_re, double alpha_im, void* B,
+                              int64_t ldb, void* stream);
+
+/*
+ * Page-locked host memory for the host-buffer entry points (no counterpart in
+ * the reference; a Julia caller would use CUDA.jl's pinned buffers):
+ * nla_host_alloc returns `bytes` of page-locked, 256-byte aligned host memory
+ * (cudaHostAlloc), nla_host_free releases it.  Copies from and to it run at
+ * the copy engines' rate without staging.
+ */
+NLA_API int nla_host_alloc(size_t bytes, void** out);
+NLA_API int nla_host_free(void* p);
 
 /*
  * Mixed-precision form (no counterpart in the reference): the FP64 answer of

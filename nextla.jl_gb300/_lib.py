@@ -13,7 +13,7 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libnextla_gb300.so")
 
-NLA_F16, NLA_F32, NLA_F64 = 0, 1, 2
+NLA_F16, NLA_F32, NLA_F64, NLA_C32, NLA_C64 = 0, 1, 2, 3, 4
 NLA_OK = 0
 NLA_ERR_ARG = -1
 NLA_ERR_DTYPE = -2
@@ -34,6 +34,10 @@ SIGNATURES = {
     "nla_diag_block": ([_c, _c, _c, _i32, _i32, _i64, _i64, _p, _i64, _p, _i64, _p], _i32),
     "nla_gemm_update": ([_i32, _i32, _i32, _i64, _i64, _i64, _d, _p, _i64, _p, _i64, _p, _i64, _p], _i32),
     "nla_scale": ([_i32, _i64, _i64, _d, _p, _i64, _p], _i32),
+    "nla_host_alloc": ([_sz, ctypes.POINTER(_p)], _i32),
+    "nla_host_free": ([_p], _i32),
+    "nla_scale_complex": ([_i32, _i64, _i64, _d, _d, _p, _i64, _p], _i32),
+    "nla_trxm_complex": ([_c, _c, _c, _d, _d, _c, _i32, _i64, _i64, _p, _i64, _p, _i64, _p], _i32),
     "nla_trace_enable": ([_i32], _i32),
     "nla_trace_summary": ([_i32, ctypes.POINTER(_i64), ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d)],
                           _i32),
@@ -105,6 +109,24 @@ def measure_pipes(stream=None) -> dict:
     a, b, c = _d(), _d(), _d()
     check(load().nla_measure_pipes(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), stream))
     return {"dfma": a.value, "dmma": b.value, "ffma": c.value}
+
+
+def host_empty(numel, dtype):
+    """A 1-D CPU tensor of `numel` elements of torch `dtype` in page-locked
+    memory from nla_host_alloc (cudaHostAlloc), freed with the tensor; reshape
+    it to the layout the host-buffer entry points are given."""
+    import weakref
+
+    import numpy as np
+    import torch
+
+    es = torch.empty((), dtype=dtype).element_size()
+    nbytes = max(int(numel) * es, 1)
+    p = _p()
+    check(load().nla_host_alloc(nbytes, ctypes.byref(p)))
+    arr = np.frombuffer((ctypes.c_byte * nbytes).from_address(p.value), dtype=np.uint8)
+    weakref.finalize(arr, load().nla_host_free, ctypes.c_void_p(p.value))
+    return torch.from_numpy(arr).view(dtype)[: int(numel)]
 
 
 KERNEL_CLASSES = ["leaf_solve", "leaf_mult", "gemm_simt", "gemm_umma", "split", "scale", "residual", "batched",

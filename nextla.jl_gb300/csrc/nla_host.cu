@@ -69,6 +69,7 @@ struct HostRun {
   char* Ad;
   int64_t ldad;
   int at;  // A is used transposed
+  int conj = 0;  // complex types: and conjugated (trans 'C')
   const char* Bh;
   int64_t ldbh;
   char* Xh;
@@ -94,7 +95,11 @@ int order(HostRun& h, cudaStream_t from, cudaStream_t to) {
   return r == cudaSuccess ? NLA_OK : cuda_status(r, "host copy ordering");
 }
 
-Mat a_view(const HostRun& h, int64_t i, int64_t j) { return sub(Mat{h.Ad, h.ldad, h.at}, i, j, h.c.dtype); }
+Mat a_view(const HostRun& h, int64_t i, int64_t j) {
+  Mat A{h.Ad, h.ldad, h.at};
+  A.c = h.conj;
+  return sub(A, i, j, h.c.dtype);
+}
 
 Mat b_view(const HostRun& h, int64_t k) {
   const Mat B{h.Bd, h.ldbd, 0};
@@ -261,6 +266,27 @@ using namespace nla;
 
 extern "C" {
 
+int nla_host_alloc(size_t bytes, void** out) {
+  clear_error();
+  if (!out) return fail(NLA_ERR_ARG, "nla_host_alloc: null output pointer");
+  *out = nullptr;
+  if (bytes == 0) return NLA_OK;
+  const cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return e == cudaErrorMemoryAllocation ? fail(NLA_ERR_NOMEM, "nla_host_alloc: out of page-locked memory")
+                                          : cuda_status(e, "cudaHostAlloc");
+  }
+  return NLA_OK;
+}
+
+int nla_host_free(void* p) {
+  clear_error();
+  if (!p) return NLA_OK;
+  const cudaError_t e = cudaFreeHost(p);
+  return e == cudaSuccess ? NLA_OK : cuda_status(e, "cudaFreeHost");
+}
+
 int nla_trxm_host(char side, char uplo, char trans, double alpha, char func, int dtype, int64_t n, int64_t m,
                   const void* A_host, int64_t lda, const void* B_host, int64_t ldb, void* X_host, int64_t ldx,
                   void* A_dev, int64_t lda_dev, void* B_dev, int64_t ldb_dev, int levels, void* stream) {
@@ -280,6 +306,7 @@ int nla_trxm_host(char side, char uplo, char trans, double alpha, char func, int
   h.Ad = static_cast<char*>(A_dev);
   h.ldad = lda_dev;
   h.at = at;
+  h.conj = trans == 'C' && is_complex(dtype);
   h.Bh = static_cast<const char*>(B_host);
   h.ldbh = ldb;
   h.Xh = static_cast<char*>(X_host);
