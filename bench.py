@@ -173,9 +173,9 @@ E2E_STEPS = 15   # synchronised end-to-end steps (host buffers to host result)
 # solve at n = m = 16384.  ncu cannot run inside the timed bench, so this is
 # the figure of one ncu capture of the same workload, with the commit and
 # command it was taken on (TRAFFIC_SOURCE).
-TRAFFIC_BYTES_PER_LAUNCH = 219e6
+TRAFFIC_BYTES_PER_LAUNCH = 214.7e6
 TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:umma_exact -s 510 -c 510 "
-                  "python bench.py --steps 1 --warmup 1 --no-plain --no-cpu-baseline, at commit 9df2745")
+                  "python bench.py --steps 1 --warmup 1 --no-plain --no-cpu-baseline, at commit cd51b7e")
 
 
 def make_inputs(n, m, seed=0):
@@ -402,10 +402,10 @@ def run_batched(args):
         X64 = B.clone()
         ref = float(torch.linalg.norm(X64))
         mixed = []
-        for sweeps in (0, 1, 2, 3):
+        for sweeps, res in ((0, "split"), (1, "split"), (2, "split"), (3, "split"), (2, "fp64")):
             def mstep():
                 B.copy_(B0)
-                plan.solve_mixed(1.0, A, B, sweeps=sweeps)
+                plan.solve_mixed(1.0, A, B, sweeps=sweeps, residual=res)
             for _ in range(args.warmup):
                 mstep()
             torch.cuda.synchronize(dev)
@@ -416,7 +416,9 @@ def run_batched(args):
             e1.record(stream)
             torch.cuda.synchronize(dev)
             mms = e0.elapsed_time(e1) / args.steps
-            mixed.append({"sweeps": sweeps, "ms": mms, "tflops": flops / (mms / 1e3) / 1e12,
+            mixed.append({"sweeps": sweeps, "residual": {"split": "tensor cores, exact BF16 slices",
+                                                          "fp64": "FP64 pipe"}[res],
+                          "ms": mms, "tflops": flops / (mms / 1e3) / 1e12,
                           "rel_err_vs_fp64": float(torch.linalg.norm(B - X64)) / ref})
         del X64
     line = {

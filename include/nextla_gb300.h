@@ -361,13 +361,20 @@ NLA_API int nla_batch_plan_destroy(nla_batch_plan plan);
  * Mixed-precision form of a Float64 batch (plan created with NLA_F64; no
  * counterpart in the reference).  Every system is solved in Float32 (A_i and
  * alpha B_i rounded to Float32) and then refined `sweeps` times (0..8):
- * R_i = alpha B_i - op(A_i) X_i in Float64, a Float32 solve of op(A_i) D_i =
- * R_i, X_i += D_i.  X_i (Float64) replaces B_i.  The elements of A and B must
- * lie in the Float32 range.  The plan allocates Float32 copies of the pools
- * and a Float64 residual buffer on first use and keeps them until destroyed.
+ * R_i = alpha B_i - op(A_i) X_i, a Float32 solve of op(A_i) D_i = R_i,
+ * X_i += D_i.  X_i (Float64) replaces B_i.  The residual is Float64-accurate:
+ * with `residual` NLA_RESIDUAL_SPLIT (the default of nla_batch_solve_mixed)
+ * op(A_i) X_i is formed on the tcgen05 tensor cores from seven BF16 slices of
+ * every 64-wide block of each row and column, the slice products summed
+ * exactly; with NLA_RESIDUAL_FP64 on the FP64 pipe.  The elements of A and B
+ * must be finite and lie in the Float32 range.  The plan allocates Float32
+ * copies of the pools, a Float64 residual buffer and the residual's tile list
+ * on first use and keeps them until destroyed.
  */
 NLA_API int nla_batch_solve_mixed(nla_batch_plan plan, double alpha, const void* A_pool, void* B_pool, int sweeps,
                                   void* stream);
+NLA_API int nla_batch_solve_mixed_ex(nla_batch_plan plan, double alpha, const void* A_pool, void* B_pool, int sweeps,
+                                     int residual, void* stream);
 
 /*
  * Measured throughput (TFLOP/s) of the pipes the plain paths use on the

@@ -92,6 +92,7 @@ SIGNATURES.update({
     "nla_batch_solve": ([_p, _d, _p, _p, _i32, _p], _i32),
     "nla_batch_plan_destroy": ([_p], _i32),
     "nla_batch_solve_mixed": ([_p, _d, _p, _p, _i32, _p], _i32),
+    "nla_batch_solve_mixed_ex": ([_p, _d, _p, _p, _i32, _i32, _p], _i32),
 })
 
 SIGNATURES["nla_trxm_diag"] = ([_c, _c, _c, _c, _d, _c, _i32, _i64, _i64, _p, _i64, _p, _i64, _p], _i32)

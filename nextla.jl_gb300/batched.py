@@ -80,17 +80,20 @@ class BatchPlan:
                                                MODES[mode], _stream(B_pool)))
         return B_pool
 
-    def solve_mixed(self, alpha, A_pool, B_pool, sweeps=2):
+    def solve_mixed(self, alpha, A_pool, B_pool, sweeps=2, residual="split"):
         """Mixed-precision form of a Float64 batch: Float32 solves refined by
-        ``sweeps`` Float64 residuals (nla_batch_solve_mixed); X replaces B."""
+        ``sweeps`` Float64-accurate residuals (nla_batch_solve_mixed_ex),
+        formed on the tensor cores from exact BF16 slice products
+        (``residual`` 'split') or on the FP64 pipe ('fp64'); X replaces B."""
         import torch
 
         if self.dtype != torch.float64 or A_pool.dtype != torch.float64 or B_pool.dtype != torch.float64:
             raise ValueError("the mixed batch form needs a Float64 plan and Float64 pools")
         if not (A_pool.is_cuda and B_pool.is_cuda):
             raise ValueError("pools must be CUDA tensors")
-        _lib.check(_lib.load().nla_batch_solve_mixed(self._plan, float(alpha), A_pool.data_ptr(), B_pool.data_ptr(),
-                                                     int(sweeps), _stream(B_pool)))
+        code = {"split": _lib.NLA_RESIDUAL_SPLIT, "fp64": _lib.NLA_RESIDUAL_FP64}[residual]
+        _lib.check(_lib.load().nla_batch_solve_mixed_ex(self._plan, float(alpha), A_pool.data_ptr(),
+                                                        B_pool.data_ptr(), int(sweeps), code, _stream(B_pool)))
         return B_pool
 
     def close(self):

@@ -41,6 +41,7 @@
 #include <vector>
 
 #include "nla_common.cuh"
+#include "nla_umma.cuh"
 
 namespace nla {
 namespace bat {
@@ -49,7 +50,10 @@ constexpr int NT = 256;          // threads per CTA
 constexpr int MAX_ROWS = 64;     // largest leaf (and update-tile height)
 constexpr int ROW_GROUPS = 16;   // 16 row groups x 16 column groups of threads
 constexpr int RT = 4;            // rows per thread (strided by ROW_GROUPS)
-constexpr int PANEL = 16;        // triangle panel of a leaf
+#ifndef NLA_BATCH_PANEL
+#define NLA_BATCH_PANEL 16
+#endif
+constexpr int PANEL = NLA_BATCH_PANEL;  // triangle panel of a leaf (rows solved one chain per thread)
 constexpr int LEAF_PAD = 1;      // row padding of the staged diagonal block
 
 static_assert(NT % MAX_ROWS == 0 && NT % 32 == 0 && NT % 16 == 0, "staging index steps");
@@ -189,6 +193,15 @@ __device__ __forceinline__ void lds_vec(const double* p, double (&v)[N]) {
   }
 }
 
+// RT consecutive values to shared memory as 16-byte vectors (p 16-byte aligned).
+__device__ __forceinline__ void sts4(float* p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void sts4(double* p, double a, double b, double c, double d) {
+  *reinterpret_cast<double2*>(p) = make_double2(a, b);
+  *reinterpret_cast<double2*>(p + 2) = make_double2(c, d);
+}
+
 // Element offsets in canonical coordinates: row i / column k of the lower
 // triangle applied from the left (rev maps i -> n - 1 - i; tA reads A's
 // transpose).
@@ -296,20 +309,34 @@ __device__ void run_update(const Args& a, const Node& nd, const Group& g, const 
         for (int c = 0; c < CT; ++c) acc[i][c] = fma(av[i], xv[c], acc[i][c]);
     }
   }
-  T* Bw = static_cast<T*>(a.B);
+  // Epilogue: the products go through shared memory (column-major, TP rows)
+  // so that the tile of B is read and written along its contiguous rows, all
+  // of a thread's loads issued before its first store (a store to the pool
+  // may alias a later load of it, which would otherwise wait for it).
+  constexpr int TP = MAX_ROWS + 4;
+  static_assert(RT == 4 && TP * W <= KC * (AP + XP) + MAX_ROWS * (MAX_ROWS + LEAF_PAD), "tile fits the node's smem");
+  Tc* Ts = As;
+  __syncthreads();  // the last chunk is no longer read
+#pragma unroll
+  for (int c = 0; c < CT; ++c)
+    sts4(Ts + (tc * CT + c) * TP + RT * tr, acc[0][c], acc[1][c], acc[2][c], acc[3][c]);
+  __syncthreads();
+  constexpr int PER = MAX_ROWS * W / NT, CSTEP = NT / MAX_ROWS;
+  const int r = t % MAX_ROWS, cb = t / MAX_ROWS;
+  T* const Bt = static_cast<T*>(a.B) + b_at(d, a.rev, nd.r0, g.c0) + sgn * r;
   const bool first = nd.flags & FLAG_ALPHA;
+  T bv[PER];
 #pragma unroll
-  for (int i = 0; i < RT; ++i) {
-    const int r = RT * tr + i;
-    if (r >= rows) continue;
+  for (int u = 0; u < PER; ++u) {
+    const int c = cb + u * CSTEP;
+    bv[u] = r < rows && c < ncols ? ldcg(Bt + (int64_t)c * d.ldb) : T(0);
+  }
 #pragma unroll
-    for (int c = 0; c < CT; ++c) {
-      const int col = tc * CT + c;
-      if (col >= ncols) continue;
-      const int64_t o = b_at(d, a.rev, nd.r0 + r, g.c0 + col);
-      const T b = ldcg(B + o);
-      const Tc base = first ? scaled<T>(b, a.alpha) : to_c(b);
-      Elem<T>::store(Bw + o, base - acc[i][c]);
+  for (int u = 0; u < PER; ++u) {
+    const int c = cb + u * CSTEP;
+    if (r < rows && c < ncols) {
+      const Tc base = first ? scaled<T>(bv[u], a.alpha) : to_c(bv[u]);
+      Elem<T>::store(Bt + (int64_t)c * d.ldb, base - Ts[c * TP + r]);
     }
   }
 }
@@ -623,6 +650,283 @@ __global__ void __launch_bounds__(NT) batched_residual_kernel(ResidualArgs a) {
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Exact residual of a mixed batch on the tensor cores.  One CTA per tile of
+// 128 rows x 64 right-hand sides of a group: D32 = (float)(R - L X), with L
+// the canonical lower triangle (diagonal included) and X the current
+// Float64 solution, L X accumulated exactly enough for Float64 refinement.
+//
+// Per 64-wide block of K, every row of L and every column of X is scaled by
+// its own power of two (largest element in [1/4, 1/2)) and split into seven
+// balanced 8-bit digits, y = round(v 2^(56 - e)) = sum_p d_p 2^(8 (6 - p)),
+// |d_p| <= 128, each stored as a BF16 slice in shared memory (K-major,
+// 128-byte swizzle, as tcgen05.mma reads it).  The 28 slice pairs (p, q)
+// with p + q <= 6 are multiplied on the tensor cores, the pairs of one weight
+// w = p + q into one FP32 accumulator in TMEM: 7 x 64 x 2^14 < 2^24, so each
+// block's sums are exact integers.  The epilogue warps combine them into two
+// exact integers, H = sum_{w<4} T_w 2^(24 - 8 w) and L = sum_{4<=w<7} T_w
+// 2^(48 - 8 w), and add H 2^(e_r + e_c - 40) + L 2^(e_r + e_c - 64) to a
+// Float64 accumulator per element, so that the block's products are rounded
+// only by that accumulation (as in a Float64 dot product).  The pairs left
+// out (w >= 7) stay below 2^-53 of the block's largest |l| |x| per product.
+// ---------------------------------------------------------------------------
+constexpr int XR_ROWS = 128, XR_COLS = 64, XR_KB = 64, XR_SL = 7;
+constexpr int XR_THREADS = 288;  // 8 worker warps + 1 MMA warp
+constexpr int XR_A_BYTES = XR_SL * XR_ROWS * 128;  // 7 slices x 128 rows x 64 BF16
+constexpr int XR_X_BYTES = XR_SL * XR_COLS * 128;  // 7 slices x 64 columns x 64 BF16
+constexpr int XR_SMEM = XR_A_BYTES + XR_X_BYTES + 1024 + 8192;  // slices, alignment, maxima, exponents, barrier
+
+struct ExactTile {
+  int group;
+  int r0;  // canonical first row
+  int c0;  // first right-hand side within the group
+  int nkb;  // blocks of K
+};
+
+struct ExactResArgs {
+  const nla_batch_desc* descs;
+  const Group* groups;
+  const ExactTile* tiles;
+  const double* A64;
+  const double* X64;
+  const double* R64;
+  float* D32;
+  int tA, rev;
+  int* err;
+};
+
+// Seven balanced digits of y (|y| < 2^55), most significant first.
+__device__ __forceinline__ void digits7(long long y, int (&d)[XR_SL]) {
+#pragma unroll
+  for (int i = XR_SL - 1; i > 0; --i) {
+    const int s = (int)(((y + 128) & 255) - 128);
+    d[i] = s;
+    y = (y - s) >> 8;
+  }
+  d[0] = (int)y;
+}
+
+__device__ __forceinline__ uint32_t bf16_pair(int a, int b) {
+  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)a)) |
+         ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)b)) << 16);
+}
+
+// Exponent e with max * 2^-e in [1/4, 1/2) (0 for a zero block).
+__device__ __forceinline__ int block_exp(double mx) {
+  if (mx == 0.0) return 0;
+  int E;
+  frexp(mx, &E);
+  return E + 1;
+}
+
+// 8 values (k = 8 j .. 8 j + 7 of a row) as 7 slices of one 16-byte chunk.
+__device__ __forceinline__ void store_chunks(uint8_t* base, int slice_bytes, int row, int j, const double (&v)[8],
+                                             double sc) {
+  int d[8][XR_SL];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) digits7(llrint(v[u] * sc), d[u]);
+  const int off = row * 128 + ((j ^ (row & 7)) << 4);
+#pragma unroll
+  for (int p = 0; p < XR_SL; ++p) {
+    uint4 q;
+    q.x = bf16_pair(d[0][p], d[1][p]);
+    q.y = bf16_pair(d[2][p], d[3][p]);
+    q.z = bf16_pair(d[4][p], d[5][p]);
+    q.w = bf16_pair(d[6][p], d[7][p]);
+    *reinterpret_cast<uint4*>(base + p * slice_bytes + off) = q;
+  }
+}
+
+__global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(ExactResArgs a) {
+  extern __shared__ uint8_t xr_smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(xr_smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sA = smem;
+  uint8_t* sX = smem + XR_A_BYTES;
+  double* amax = reinterpret_cast<double*>(sX + XR_X_BYTES);  // [2][128]
+  double* xmax = amax + 2 * XR_ROWS;                            // [4][64]
+  int* ea_s = reinterpret_cast<int*>(xmax + 4 * XR_COLS);       // [128]
+  int* eb_s = ea_s + XR_ROWS;                                   // [64]
+  uint64_t* mma_bar = reinterpret_cast<uint64_t*>(eb_s + XR_COLS);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_bar + 1);
+  __shared__ volatile int s_abort;
+
+  const ExactTile tile = a.tiles[blockIdx.x];
+  const Group g = a.groups[tile.group];
+  const nla_batch_desc d = a.descs[g.sys];
+  const int n = (int)d.n, r0 = tile.r0, c0 = tile.c0;
+  const int ncols = min(XR_COLS, g.ncols - c0);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int64_t dk = (a.rev ? -1 : 1) * (a.tA ? 1 : d.lda);  // step of canonical k within a row of A
+
+  if (t == 0) {
+    s_abort = 0;
+    umma::mbar_init(umma::smem_u32(mma_bar), 1);
+    umma::fence_barrier_init();
+  }
+  if (warp == 8) umma::tmem_alloc(umma::smem_u32(tmem_slot), 512);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  // Epilogue role of a worker: rows q * 32 + lane, columns h * 32 .. + 32.
+  const int q = warp & 3, h = (warp >> 2) & 1;
+  double acc[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) acc[j] = 0.0;
+  bool ok = true;
+
+  for (int kb = 0; kb < tile.nkb && ok; ++kb) {
+    const int k0 = kb * XR_KB;
+    // Two passes over the block: the largest magnitudes first, then the
+    // values again (from L1 / L2) to split them, so that no block of values
+    // stays in registers across the barrier.
+    if (warp < 8) {
+      // A: thread -> row t % 128, half t / 128 of the block's 64 values of k.
+      const int row = t & 127, half = t >> 7, r = r0 + row;
+      const double* arow = a.A64 + a_at(d, a.tA, a.rev, min(r, n - 1), 0);
+      double m = 0.0;
+#pragma unroll 8
+      for (int u = 0; u < 32; ++u) {
+        const int k = k0 + half * 32 + u;
+        if (r < n && k <= r) m = fmax(m, fabs(arow[(int64_t)k * dk]));
+      }
+      amax[half * XR_ROWS + row] = m;
+      // X: thread -> column t % 64, quarter t / 64 of the block's rows.
+      const int col = t & 63, qu = t >> 6;
+      double mx = 0.0;
+#pragma unroll 8
+      for (int u = 0; u < 16; ++u) {
+        const int k = k0 + qu * 16 + u;
+        if (k < n && col < ncols) mx = fmax(mx, fabs(__ldcg(a.X64 + b_at(d, a.rev, k, g.c0 + c0 + col))));
+      }
+      xmax[qu * XR_COLS + col] = mx;
+    }
+    __syncthreads();
+    if (warp < 8) {
+      const int row = t & 127, half = t >> 7, r = r0 + row;
+      const double* arow = a.A64 + a_at(d, a.tA, a.rev, min(r, n - 1), 0);
+      const int ea = block_exp(fmax(amax[row], amax[XR_ROWS + row]));
+      if (half == 0) ea_s[row] = ea;
+      const double sca = ldexp(1.0, 56 - ea);
+#pragma unroll 1
+      for (int c = 0; c < 4; ++c) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int k = k0 + half * 32 + c * 8 + u;
+          v[u] = r < n && k <= r ? arow[(int64_t)k * dk] : 0.0;
+        }
+        store_chunks(sA, XR_ROWS * 128, row, half * 4 + c, v, sca);
+      }
+      const int col = t & 63, qu = t >> 6;
+      const int eb = block_exp(fmax(fmax(xmax[col], xmax[XR_COLS + col]),
+                                    fmax(xmax[2 * XR_COLS + col], xmax[3 * XR_COLS + col])));
+      if (qu == 0) eb_s[col] = eb;
+      const double scx = ldexp(1.0, 56 - eb);
+#pragma unroll 1
+      for (int c = 0; c < 2; ++c) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int k = k0 + qu * 16 + c * 8 + u;
+          v[u] = k < n && col < ncols ? __ldcg(a.X64 + b_at(d, a.rev, k, g.c0 + c0 + col)) : 0.0;
+        }
+        store_chunks(sX, XR_COLS * 128, col, qu * 2 + c, v, scx);
+      }
+      // The tensor cores read shared memory through the async proxy.
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    if (warp == 8 && lane == 0) {
+      const uint32_t idesc = umma::idesc_f16(XR_ROWS, XR_COLS, true);
+      const uint32_t a0 = umma::smem_u32(sA), x0 = umma::smem_u32(sX);
+#pragma unroll 1
+      for (int w = 0; w < XR_SL; ++w) {
+        const int p0 = w > XR_SL - 1 ? w - (XR_SL - 1) : 0;
+        for (int p = p0; p <= w && p < XR_SL; ++p) {
+          const int qq = w - p;
+#pragma unroll
+          for (int kk = 0; kk < XR_KB / 16; ++kk)
+            umma::mma_f16(tmem + (uint32_t)(w * XR_COLS),
+                          umma::desc_kmajor_sw128(a0 + p * XR_ROWS * 128 + kk * 32),
+                          umma::desc_kmajor_sw128(x0 + qq * XR_COLS * 128 + kk * 32), idesc,
+                          (p > p0 || kk > 0) ? 1u : 0u);
+        }
+      }
+      umma::mma_commit(umma::smem_u32(mma_bar));
+    }
+    if (warp < 8) {
+      ok = __all_sync(0xffffffffu, umma::mbar_wait(umma::smem_u32(mma_bar), (uint32_t)kb & 1u, &s_abort, a.err, 21));
+      umma::fence_after_sync();
+      if (ok) {
+        const int row = q * 32 + lane;
+        const double sa = ldexp(1.0, ea_s[row] - 24);
+#pragma unroll
+        for (int j0 = 0; j0 < 32; j0 += 16) {
+          // Two exact integer parts per element: weights 0..3 (H, in units of
+          // 2^72 of the digit products) and 4..6 (L, units of 2^48); each fits
+          // a double exactly, so nothing is rounded before the accumulator.
+#pragma unroll
+          for (int part = 0; part < 2; ++part) {
+            const int w0 = part == 0 ? 0 : 4, w1 = part == 0 ? 4 : XR_SL;
+            long long S[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) S[j] = 0;
+#pragma unroll
+            for (int w = w0; w < w1; ++w) {
+              uint32_t rr[16];
+              umma::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(w * XR_COLS + h * 32 + j0), rr);
+              const int sh = 8 * (w1 - 1 - w);
+#pragma unroll
+              for (int j = 0; j < 16; ++j) S[j] += (long long)__float2int_rn(__uint_as_float(rr[j])) << sh;
+            }
+            const double sp = sa * (part == 0 ? 256.0 : 1.0 / 65536.0);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) acc[j0 + j] += (double)S[j] * sp * ldexp(1.0, eb_s[h * 32 + j0 + j] - 24);
+          }
+        }
+      }
+    } else if (lane == 0) {
+      // Keep the MMA warp in step with the workers' view of the barrier.
+      umma::mbar_wait(umma::smem_u32(mma_bar), (uint32_t)kb & 1u, &s_abort, a.err, 22, false);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    ok = ok && !s_abort;
+  }
+
+  if (warp < 8 && ok) {
+    const int row = q * 32 + lane, r = r0 + row;
+    if (r < n) {
+      // Loads of a half before its stores (the pools may alias as far as
+      // the compiler knows).
+#pragma unroll
+      for (int j0 = 0; j0 < 32; j0 += 16) {
+        double rv[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int col = h * 32 + j0 + j;
+          rv[j] = col < ncols ? a.R64[b_at(d, a.rev, r, g.c0 + c0 + col)] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int col = h * 32 + j0 + j;
+          if (col < ncols) a.D32[b_at(d, a.rev, r, g.c0 + c0 + col)] = (float)(rv[j] - acc[j0 + j]);
+        }
+      }
+    }
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 8) {
+    umma::fence_after_sync();
+    umma::tmem_dealloc(tmem, 512);
+  }
+}
 }  // namespace bat
 }  // namespace nla
 
@@ -634,6 +938,7 @@ struct nla_batch_plan_s {
   int tA, rev;
   int64_t count;
   std::vector<nla_batch_desc> h_descs;
+  std::vector<nla::bat::Group> h_groups;
   int ngroups, nleaves, nnodes;
   int n_max;
   int w_max;
@@ -658,6 +963,9 @@ struct nla_batch_plan_s {
   float* a32;
   float* x32;
   double* r64;
+  // Tiles of the tensor-core residual (built on first use).
+  void* d_xtiles;
+  int nxtiles;
 };
 
 namespace nla {
@@ -933,6 +1241,8 @@ int plan_create(nla_batch_plan* out, int dtype, char uplo, char trans, int64_t c
   p->a_elems = p->b_elems = 0;
   p->a32 = p->x32 = nullptr;
   p->r64 = nullptr;
+  p->d_xtiles = nullptr;
+  p->nxtiles = 0;
   p->exec = nullptr;
   p->d_descs = p->d_groups = p->d_nodes = nullptr;
   p->d_counters = nullptr;
@@ -981,6 +1291,7 @@ int plan_create(nla_batch_plan* out, int dtype, char uplo, char trans, int64_t c
     delete p;
     return fail(NLA_ERR_UNSUPPORTED, "batch too large");
   }
+  p->h_groups = groups;
   p->ngroups = (int)groups.size();
   p->nleaves = leaves_total;
   p->nnodes = (int)nodes.size();
@@ -1019,6 +1330,42 @@ int plan_create(nla_batch_plan* out, int dtype, char uplo, char trans, int64_t c
     return cuda_status(e, "batch plan allocation");
   }
   *out = p;
+  return NLA_OK;
+}
+
+// Tiles of the tensor-core residual: 128 rows x 64 right-hand sides of a
+// group, with their blocks of K (k <= row), longest first; and the kernel's
+// shared-memory limit.
+int exact_residual_setup(nla_batch_plan p) {
+  static std::once_flag once;
+  static cudaError_t st = cudaSuccess;
+  std::call_once(once, [] {
+    st = cudaFuncSetAttribute(bat::batched_exact_residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              bat::XR_SMEM);
+  });
+  if (st != cudaSuccess) return cuda_status(st, "cudaFuncSetAttribute(batched_exact_residual_kernel)");
+  if (p->d_xtiles) return NLA_OK;
+  std::vector<bat::ExactTile> tiles;
+  for (int gi = 0; gi < (int)p->h_groups.size(); ++gi) {
+    const bat::Group& g = p->h_groups[gi];
+    for (int r0 = 0; r0 < g.n; r0 += bat::XR_ROWS)
+      for (int c0 = 0; c0 < g.ncols; c0 += bat::XR_COLS) {
+        const int kend = std::min(g.n, r0 + bat::XR_ROWS);
+        tiles.push_back(bat::ExactTile{gi, r0, c0, (kend + bat::XR_KB - 1) / bat::XR_KB});
+      }
+  }
+  std::stable_sort(tiles.begin(), tiles.end(),
+                   [](const bat::ExactTile& x, const bat::ExactTile& y) { return x.nkb > y.nkb; });
+  if (tiles.empty()) return NLA_OK;  // nothing to launch
+  cudaError_t e = cudaMalloc(&p->d_xtiles, sizeof(bat::ExactTile) * tiles.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p->d_xtiles, tiles.data(), sizeof(bat::ExactTile) * tiles.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(p->d_xtiles);
+    p->d_xtiles = nullptr;
+    return cuda_status(e, "residual tiles");
+  }
+  p->nxtiles = (int)tiles.size();
   return NLA_OK;
 }
 
@@ -1125,7 +1472,14 @@ int nla_batch_solve(nla_batch_plan p, double alpha, const void* A_pool, void* B_
 
 int nla_batch_solve_mixed(nla_batch_plan p, double alpha, const void* A_pool, void* B_pool, int sweeps,
                           void* stream) {
+  return nla_batch_solve_mixed_ex(p, alpha, A_pool, B_pool, sweeps, NLA_RESIDUAL_SPLIT, stream);
+}
+
+int nla_batch_solve_mixed_ex(nla_batch_plan p, double alpha, const void* A_pool, void* B_pool, int sweeps,
+                             int residual, void* stream) {
   clear_error();
+  if (residual != NLA_RESIDUAL_SPLIT && residual != NLA_RESIDUAL_FP64)
+    return fail(NLA_ERR_ARG, "mixed batch: residual must be NLA_RESIDUAL_SPLIT or NLA_RESIDUAL_FP64");
   if (!p) return fail(NLA_ERR_ARG, "null plan");
   if (p->dtype != NLA_F64) return fail(NLA_ERR_DTYPE, "mixed batch: the plan must be Float64");
   if (sweeps < 0 || sweeps > 8) return fail(NLA_ERR_ARG, "mixed batch: sweeps must be 0..8");
@@ -1168,11 +1522,23 @@ int nla_batch_solve_mixed(nla_batch_plan p, double alpha, const void* A_pool, vo
   bat::batched_map_kernel<<<p->ngroups, 256, 0, s>>>(m);
   NLA_CHECK_LAUNCH("batched_map_kernel");
   const bat::ResidualArgs r{descs, groups, A64, B64, p->r64, p->x32, p->tA, p->rev};
+  if (sweeps > 0 && residual == NLA_RESIDUAL_SPLIT) NLA_TRY(exact_residual_setup(p));
+  void* errp = nullptr;
+  cudaError_t ee = cudaGetSymbolAddress(&errp, bat::g_batch_error);
+  if (ee != cudaSuccess) return cuda_status(ee, "batch error word");
+  const bat::ExactResArgs xr{descs, groups, static_cast<const bat::ExactTile*>(p->d_xtiles), A64, B64, p->r64,
+                             p->x32, p->tA, p->rev, static_cast<int*>(errp)};
   for (int k = 0; k < sweeps; ++k) {
-    bat::batched_residual_kernel<<<dim3((unsigned)p->ngroups,
-                                        (unsigned)((p->n_max + bat::MAX_ROWS - 1) / bat::MAX_ROWS)),
-                                   bat::NT, 0, s>>>(r);
-    NLA_CHECK_LAUNCH("batched_residual_kernel");
+    if (residual == NLA_RESIDUAL_SPLIT) {
+      if (p->nxtiles == 0) return fail(NLA_ERR_UNSUPPORTED, "mixed batch: no residual tiles");
+      bat::batched_exact_residual_kernel<<<(unsigned)p->nxtiles, bat::XR_THREADS, bat::XR_SMEM, s>>>(xr);
+      NLA_CHECK_LAUNCH("batched_exact_residual_kernel");
+    } else {
+      bat::batched_residual_kernel<<<dim3((unsigned)p->ngroups,
+                                          (unsigned)((p->n_max + bat::MAX_ROWS - 1) / bat::MAX_ROWS)),
+                                     bat::NT, 0, s>>>(r);
+      NLA_CHECK_LAUNCH("batched_residual_kernel");
+    }
     NLA_TRY(solve32());
     m.op = bat::MAP_ADD;
     bat::batched_map_kernel<<<p->ngroups, 256, 0, s>>>(m);
@@ -1187,6 +1553,7 @@ int nla_batch_plan_destroy(nla_batch_plan p) {
   cudaFree(p->a32);
   cudaFree(p->x32);
   cudaFree(p->r64);
+  cudaFree(p->d_xtiles);
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   cudaFree(p->d_descs);
