@@ -66,9 +66,17 @@ void clear_trace_locked() {
 }
 }  // namespace
 
+namespace {
+thread_local int t_trace_class = -1;  // TraceClassScope's override, or -1
+}
+
+TraceClassScope::TraceClassScope(int kclass) : prev(t_trace_class) { t_trace_class = kclass; }
+TraceClassScope::~TraceClassScope() { t_trace_class = prev; }
+
 void trace_begin(int kclass, cudaStream_t s, double flops, double bytes, void** handle) {
   *handle = nullptr;
   if (!g_trace_on.load(std::memory_order_relaxed)) return;
+  if (t_trace_class >= 0) kclass = t_trace_class;
   std::lock_guard<std::mutex> lk(g_trace_mu);
   TraceRec* r = new TraceRec{kclass, pooled_event(), pooled_event(), flops, bytes};
   cudaEventRecord(r->e0, s);
@@ -250,7 +258,10 @@ int rec_update(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
 }
 
 int recurse(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
-  if (n <= c.threshold) return launch_leaf(c.func, c.side, c.uplo, c.dtype, n, c.m, A, B, c.s, c.unit);
+  if (n <= c.threshold) {
+    if (c.inv) return leaf_inverse_apply(c, A, n, B);
+    return launch_leaf(c.func, c.side, c.uplo, c.dtype, n, c.m, A, B, c.s, c.unit);
+  }
   const int64_t mid = split_point(n), rem = n - mid;
   const int d = c.dtype;
   const Mat A11 = A, A22 = sub(A, mid, mid, d);

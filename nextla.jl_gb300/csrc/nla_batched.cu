@@ -223,6 +223,23 @@ __host__ __device__ constexpr size_t leaf_elems(int W) {
   return (size_t)MAX_ROWS * (MAX_ROWS + LEAF_PAD) + (size_t)MAX_ROWS * (W + 4) + MAX_ROWS;
 }
 
+// Thread 0 waits for the node's dependencies (acquire loads of the group's
+// counters); every thread learns the outcome through *s_ok.  False when a
+// wait gave up or another CTA has aborted.  Nodes call it after issuing the
+// loads of A, which no other node writes, so that those are in flight
+// during the wait.
+__device__ __forceinline__ bool node_deps(const Args& a, const Node& nd, volatile int* s_ok) {
+  if (threadIdx.x == 0) {
+    bool ok = *(volatile int*)a.abort == 0;
+    if (ok && nd.kind == NODE_UPDATE && nd.wait_solved > 0) ok = wait_geq(a.solved + nd.group, nd.wait_solved, a, 1);
+    if (ok && nd.wait_applied > 0)
+      ok = wait_geq(a.applied + a.groups[nd.group].leaf_base + nd.leaf, nd.wait_applied, a, 2);
+    *s_ok = ok ? 1 : 0;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
 // ---------------------------------------------------------------------------
 // UPDATE: X[r0 + r, c] = base(r, c) - sum_k A[r0 + r, k0 + k] X[k0 + k, c] for
 // r < rows, c < ncols, base = alpha B (first touch) or B.  Thread (tr, tc)
@@ -233,7 +250,8 @@ __host__ __device__ constexpr size_t leaf_elems(int W) {
 // registers during the current chunk.
 // ---------------------------------------------------------------------------
 template <typename T, int W>
-__device__ void run_update(const Args& a, const Node& nd, const Group& g, const nla_batch_desc& d, void* smem) {
+__device__ bool run_update(const Args& a, const Node& nd, const Group& g, const nla_batch_desc& d, void* smem,
+                           volatile int* s_ok) {
   using Tc = typename Elem<T>::compute;
   constexpr int KC = kc_of(sizeof(Tc));
   constexpr int CT = W / 16;
@@ -269,13 +287,16 @@ __device__ void run_update(const Args& a, const Node& nd, const Group& g, const 
   const T* X0 = B + b_at(d, a.rev, nd.k0, g.c0) + sgn * xk + (int64_t)xc * d.ldb;
 
   Tc pa[A_PER], px[X_PER];
-  auto fetch = [&](int k0) {
+  auto fetch_a = [&](int k0) {
     const int kw = min(KC, nd.k0 + nd.kw - k0);
     const T* pA = A0 + (int64_t)(k0 - nd.k0) * dk;
-    const T* pX = X0 + (int64_t)(k0 - nd.k0) * sgn;
 #pragma unroll
     for (int u = 0; u < A_PER; ++u)
       pa[u] = ar + u * ar_step < rows && ak + u * ak_step < kw ? to_c(pA[u * a_step]) : Tc(0);
+  };
+  auto fetch_x = [&](int k0) {
+    const int kw = min(KC, nd.k0 + nd.kw - k0);
+    const T* pX = X0 + (int64_t)(k0 - nd.k0) * sgn;
 #pragma unroll
     for (int u = 0; u < X_PER; ++u)
       px[u] = xk < kw && xc + u * XC_STEP < ncols ? to_c(ldcg(pX + u * x_step)) : Tc(0);
@@ -288,12 +309,17 @@ __device__ void run_update(const Args& a, const Node& nd, const Group& g, const 
   };
 
   const int kend = nd.k0 + nd.kw;
-  fetch(nd.k0);
+  fetch_a(nd.k0);
+  if (!node_deps(a, nd, s_ok)) return false;
+  fetch_x(nd.k0);
   for (int k0 = nd.k0; k0 < kend; k0 += KC) {
     __syncthreads();  // the previous chunk is no longer read
     stash();
     __syncthreads();
-    if (k0 + KC < kend) fetch(k0 + KC);
+    if (k0 + KC < kend) {
+      fetch_a(k0 + KC);
+      fetch_x(k0 + KC);
+    }
     // A warp holds the columns of two column groups; one whose columns all
     // lie past the group's right-hand sides (a narrow block in a wider
     // template) skips the products.
@@ -339,6 +365,7 @@ __device__ void run_update(const Args& a, const Node& nd, const Group& g, const 
       Elem<T>::store(Bt + (int64_t)c * d.ldb, base - Ts[c * TP + r]);
     }
   }
+  return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -349,7 +376,8 @@ __device__ void run_update(const Args& a, const Node& nd, const Group& g, const 
 // updated with the register-tiled product.
 // ---------------------------------------------------------------------------
 template <typename T, int W>
-__device__ void run_leaf(const Args& a, const Node& nd, const Group& g, const nla_batch_desc& d, void* smem) {
+__device__ bool run_leaf(const Args& a, const Node& nd, const Group& g, const nla_batch_desc& d, void* smem,
+                         volatile int* s_ok) {
   using Tc = typename Elem<T>::compute;
   constexpr int LP = MAX_ROWS + LEAF_PAD, XP = W + 4, CT = W / 16;
   Tc* Ls = static_cast<Tc*>(smem);    // [64][LP]: Ls[r][k], k < r, of the block
@@ -362,50 +390,44 @@ __device__ void run_leaf(const Args& a, const Node& nd, const Group& g, const nl
 
   // Stage the block of A (threads along the index contiguous in memory) and
   // X; offsets are affine in the block's row and column (as in run_update).
-  // Each thread issues all of its loads of a block before it stores any, so
-  // their latencies overlap instead of adding up.
+  // A's loads are issued before the dependency wait, X's (which other nodes
+  // write) after it, and every load before the first store, so that their
+  // latencies overlap instead of adding up.
   const int64_t sgn = a.rev ? -1 : 1;
   const int64_t dr = sgn * (a.tA ? d.lda : 1), dk = sgn * (a.tA ? 1 : d.lda);
   const T* A0 = A + a_at(d, a.tA, a.rev, nd.r0, nd.r0);
-  {
-    constexpr int PER = MAX_ROWS * MAX_ROWS / NT;
-    Tc v[PER];
+  constexpr int A_PER = MAX_ROWS * MAX_ROWS / NT, X_PER = MAX_ROWS * W / NT;
+  Tc va[A_PER], vx[X_PER];
 #pragma unroll
-    for (int u = 0; u < PER; ++u) {
-      const int idx = t + u * NT;
-      const int r = a.tA ? idx / MAX_ROWS : idx % MAX_ROWS, k = a.tA ? idx % MAX_ROWS : idx / MAX_ROWS;
-      v[u] = r < rows && k <= r ? to_c(A0[r * dr + k * dk]) : Tc(0);
-    }
-#pragma unroll
-    for (int u = 0; u < PER; ++u) {
-      const int idx = t + u * NT;
-      const int r = a.tA ? idx / MAX_ROWS : idx % MAX_ROWS, k = a.tA ? idx % MAX_ROWS : idx / MAX_ROWS;
-      if (r < rows && k < r) Ls[r * LP + k] = v[u];
-      else if (r < rows && k == r) inv[r] = Tc(1) / v[u];
-    }
+  for (int u = 0; u < A_PER; ++u) {
+    const int idx = t + u * NT;
+    const int r = a.tA ? idx / MAX_ROWS : idx % MAX_ROWS, k = a.tA ? idx % MAX_ROWS : idx / MAX_ROWS;
+    va[u] = r < rows && k <= r ? to_c(A0[r * dr + k * dk]) : Tc(0);
   }
+  if (!node_deps(a, nd, s_ok)) return false;
   const T* X0 = B + b_at(d, a.rev, nd.r0, g.c0);
-  {
-    constexpr int PER = MAX_ROWS * W / NT, BATCH = PER < 16 ? PER : 16;
-    const int r = t % MAX_ROWS;  // NT is a multiple of MAX_ROWS: each thread keeps one row
-    for (int u0 = 0; u0 < PER; u0 += BATCH) {
-      Tc v[BATCH];
+  const int xr = t % MAX_ROWS;  // NT is a multiple of MAX_ROWS: each thread keeps one row of X
 #pragma unroll
-      for (int u = 0; u < BATCH; ++u) {
-        const int c = (t + (u0 + u) * NT) / MAX_ROWS;
-        Tc x = Tc(0);
-        if (r < rows && c < ncols) {
-          const T b = ldcg(X0 + r * sgn + (int64_t)c * d.ldb);
-          x = first ? scaled<T>(b, a.alpha) : to_c(b);
-        }
-        v[u] = x;
-      }
-#pragma unroll
-      for (int u = 0; u < BATCH; ++u) {
-        const int c = (t + (u0 + u) * NT) / MAX_ROWS;
-        if (r < rows) Xs[r * XP + c] = v[u];
-      }
+  for (int u = 0; u < X_PER; ++u) {
+    const int c = (t + u * NT) / MAX_ROWS;
+    Tc x = Tc(0);
+    if (xr < rows && c < ncols) {
+      const T b = ldcg(X0 + xr * sgn + (int64_t)c * d.ldb);
+      x = first ? scaled<T>(b, a.alpha) : to_c(b);
     }
+    vx[u] = x;
+  }
+#pragma unroll
+  for (int u = 0; u < A_PER; ++u) {
+    const int idx = t + u * NT;
+    const int r = a.tA ? idx / MAX_ROWS : idx % MAX_ROWS, k = a.tA ? idx % MAX_ROWS : idx / MAX_ROWS;
+    if (r < rows && k < r) Ls[r * LP + k] = va[u];
+    else if (r < rows && k == r) inv[r] = Tc(1) / va[u];
+  }
+#pragma unroll
+  for (int u = 0; u < X_PER; ++u) {
+    const int c = (t + u * NT) / MAX_ROWS;
+    if (xr < rows) Xs[xr * XP + c] = vx[u];
   }
   __syncthreads();
 
@@ -465,33 +487,23 @@ __device__ void run_leaf(const Args& a, const Node& nd, const Group& g, const nl
     const int r = idx % MAX_ROWS, c = idx / MAX_ROWS;
     if (r < rows && c < ncols) Elem<T>::store(Xw + r * sgn + (int64_t)c * d.ldb, Xs[r * XP + c]);
   }
+  return true;
 }
 
 template <typename T, int W>
-__device__ __forceinline__ void run_node(const Args& a, const Node& nd, const Group& g, const nla_batch_desc& d,
-                                         void* smem) {
-  if (nd.kind == NODE_LEAF) run_leaf<T, W>(a, nd, g, d, smem);
-  else run_update<T, W>(a, nd, g, d, smem);
+__device__ __forceinline__ bool run_node(const Args& a, const Node& nd, const Group& g, const nla_batch_desc& d,
+                                         void* smem, volatile int* s_ok) {
+  if (nd.kind == NODE_LEAF) return run_leaf<T, W>(a, nd, g, d, smem, s_ok);
+  return run_update<T, W>(a, nd, g, d, smem, s_ok);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(NT, 2) batched_node_kernel(Args a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_idx;
+  __shared__ volatile int s_ok;
   for (;;) {
-    if (threadIdx.x == 0) {
-      int idx = atomicAdd(a.next, 1);
-      if (idx < a.nnodes) {
-        const Node nd = a.nodes[idx];
-        bool ok = *(volatile int*)a.abort == 0;
-        if (ok && nd.kind == NODE_UPDATE && nd.wait_solved > 0)
-          ok = wait_geq(a.solved + nd.group, nd.wait_solved, a, 1);
-        if (ok && nd.wait_applied > 0)
-          ok = wait_geq(a.applied + a.groups[nd.group].leaf_base + nd.leaf, nd.wait_applied, a, 2);
-        if (!ok) idx = a.nnodes;  // stop: a dependency did not arrive in time
-      }
-      s_idx = idx;
-    }
+    if (threadIdx.x == 0) s_idx = atomicAdd(a.next, 1);
     __syncthreads();
     const int idx = s_idx;
     if (idx >= a.nnodes) break;
@@ -501,14 +513,16 @@ __global__ void __launch_bounds__(NT, 2) batched_node_kernel(Args a) {
     // Float64 groups are at most 64 wide (the plan splits wider blocks): a
     // 128-wide Float64 tile would not fit the register budget of two CTAs
     // per SM, and the FP64 pipe is saturated at 64.
+    bool ok = false;
     switch (g.w) {
-      case 16: run_node<T, 16>(a, nd, g, d, smem_raw); break;
-      case 32: run_node<T, 32>(a, nd, g, d, smem_raw); break;
-      case 64: run_node<T, 64>(a, nd, g, d, smem_raw); break;
+      case 16: ok = run_node<T, 16>(a, nd, g, d, smem_raw, &s_ok); break;
+      case 32: ok = run_node<T, 32>(a, nd, g, d, smem_raw, &s_ok); break;
+      case 64: ok = run_node<T, 64>(a, nd, g, d, smem_raw, &s_ok); break;
       default:
-        if constexpr (sizeof(typename Elem<T>::compute) == 4) run_node<T, 128>(a, nd, g, d, smem_raw);
+        if constexpr (sizeof(typename Elem<T>::compute) == 4) ok = run_node<T, 128>(a, nd, g, d, smem_raw, &s_ok);
         break;
     }
+    if (!ok) break;  // a dependency did not arrive in time (the same on every thread)
     __syncthreads();  // every thread's stores of this node are issued
     if (threadIdx.x == 0) {
       __threadfence();
@@ -657,25 +671,32 @@ __global__ void __launch_bounds__(NT) batched_residual_kernel(ResidualArgs a) {
 // the canonical lower triangle (diagonal included) and X the current
 // Float64 solution, L X accumulated exactly enough for Float64 refinement.
 //
-// Per 64-wide block of K, every row of L and every column of X is scaled by
-// its own power of two (largest element in [1/4, 1/2)) and split into seven
-// balanced 8-bit digits, y = round(v 2^(56 - e)) = sum_p d_p 2^(8 (6 - p)),
-// |d_p| <= 128, each stored as a BF16 slice in shared memory (K-major,
-// 128-byte swizzle, as tcgen05.mma reads it).  The 28 slice pairs (p, q)
-// with p + q <= 6 are multiplied on the tensor cores, the pairs of one weight
-// w = p + q into one FP32 accumulator in TMEM: 7 x 64 x 2^14 < 2^24, so each
-// block's sums are exact integers.  The epilogue warps combine them into two
-// exact integers, H = sum_{w<4} T_w 2^(24 - 8 w) and L = sum_{4<=w<7} T_w
-// 2^(48 - 8 w), and add H 2^(e_r + e_c - 40) + L 2^(e_r + e_c - 64) to a
-// Float64 accumulator per element, so that the block's products are rounded
-// only by that accumulation (as in a Float64 dot product).  The pairs left
-// out (w >= 7) stay below 2^-53 of the block's largest |l| |x| per product.
+// Every row of L and every column of X is scaled by its own power of two over
+// the tile's K range (largest element in [1/4, 1/2)) and, one 64-wide block
+// of K at a time, split into seven balanced 8-bit digits,
+// y = round(v 2^(56 - e)) = sum_p d_p 2^(8 (6 - p)), |d_p| <= 128, each
+// stored as a BF16 slice in shared memory (K-major, 128-byte swizzle, as
+// tcgen05.mma reads it).  The 28 slice pairs (p, q) with p + q <= 6 are
+// multiplied on the tensor cores, the pairs of one weight w = p + q into one
+// FP32 accumulator in TMEM: 7 x 64 x 2^14 < 2^24, so each block's sums T_w
+// are exact integers.  The epilogue warps add each block's
+// S = H 2^a + round(L 2^(a - 24)) to an int64 per element, with
+// H = sum_{w<4} T_w 2^(24 - 8 w), L = sum_{4<=w<7} T_w 2^(48 - 8 w) and
+// a = 18 - ceil(log2(blocks)) (headroom for the tile's blocks), and the tile
+// ends with one conversion: L X = acc 2^(e_r + e_c - 40 - a).  The rounding
+// of L and the pairs left out (w >= 7) stay below 2^-53 of |l| |x| of the
+// row's and column's largest elements per block.  Splitting, combining and
+// accumulating are integer work: the FP64 pipe, slow on this part, is used
+// once per output element.
 // ---------------------------------------------------------------------------
 constexpr int XR_ROWS = 128, XR_COLS = 64, XR_KB = 64, XR_SL = 7;
-constexpr int XR_THREADS = 288;  // 8 worker warps + 1 MMA warp
+constexpr int XR_THREADS = 512;  // 16 warps: all split and drain; one thread issues the MMAs
 constexpr int XR_A_BYTES = XR_SL * XR_ROWS * 128;  // 7 slices x 128 rows x 64 BF16
 constexpr int XR_X_BYTES = XR_SL * XR_COLS * 128;  // 7 slices x 64 columns x 64 BF16
-constexpr int XR_SMEM = XR_A_BYTES + XR_X_BYTES + 1024 + 8192;  // slices, alignment, maxima, exponents, barrier
+constexpr int XR_XRP = XR_KB + 1;                  // row pitch (doubles) of the raw X block, per column
+constexpr int XR_XRAW_BYTES = XR_COLS * XR_XRP * 8;
+constexpr int XR_SMEM = XR_A_BYTES + XR_X_BYTES + XR_XRAW_BYTES + 1024 + 4096;  // + alignment, exponents, barrier
+constexpr int XR_NONFINITE = 0x7FFFFFFF;  // exponent marker of a row or column holding Inf or NaN
 
 struct ExactTile {
   int group;
@@ -696,44 +717,62 @@ struct ExactResArgs {
   int* err;
 };
 
-// Seven balanced digits of y (|y| < 2^55), most significant first.
-__device__ __forceinline__ void digits7(long long y, int (&d)[XR_SL]) {
+// Biased exponent field of a double.
+__device__ __forceinline__ int exp_field(double v) { return (__double2hiint(v) >> 20) & 0x7FF; }
+
+// Scale exponent e of a row or column from the largest biased exponent of
+// its elements: |v| < 2^(e - 1) for all of them (0 when all are zero or
+// subnormal, XR_NONFINITE when one is Inf or NaN).
+__device__ __forceinline__ int scale_exp(int bmax) {
+  return bmax == 0x7FF ? XR_NONFINITE : (bmax == 0 ? 0 : bmax - 1021);
+}
+
+// y = round(v 2^(56 - e)) from the bits of v (|v| < 2^(e - 1), so |y| < 2^55;
+// subnormals, Inf and NaN give 0).
+__device__ __forceinline__ long long fixed56(double v, int e) {
+  const long long b = __double_as_longlong(v);
+  const int be = (int)((b >> 52) & 0x7FF);
+  if (be == 0 || be == 0x7FF || e == XR_NONFINITE) return 0;
+  const long long m = (b & 0xFFFFFFFFFFFFFll) | (1ll << 52);
+  const int s = be - 1019 - e;  // y = m 2^s, s <= 2
+  const long long y = s >= 0 ? (m << s) : (s > -62 ? ((m + (1ll << (-s - 1))) >> (-s)) : 0ll);
+  return b < 0 ? -y : y;
+}
+
+// FP32 bit pattern of byte `sel` of w minus 128, an exact small integer:
+// 0x4B4000uu is 2^23 + 2^22 + uu as a float.
+__device__ __forceinline__ uint32_t digit_f32(uint32_t w, uint32_t sel) {
+  return __float_as_uint(__uint_as_float(__byte_perm(w, 0x4B4000u, 0x6540u + sel)) - 12583040.0f);
+}
+
+// 8 values (k = 8 j .. 8 j + 7 of a row), as fixed-point integers y, stored
+// as 7 BF16 slices of one 16-byte chunk each.  The balanced digits are the
+// bytes of y + 0x0080808080808080 minus 128 (the top digit: bits 48 and up),
+// so no carries need propagating; an integer |d| <= 256 is exact in BF16,
+// which is the upper half of its FP32 pattern.
+__device__ __forceinline__ void store_chunks(uint8_t* base, int slice_bytes, int row, int j, const long long (&y)[8]) {
+  uint32_t lo[8], hi[8];
 #pragma unroll
-  for (int i = XR_SL - 1; i > 0; --i) {
-    const int s = (int)(((y + 128) & 255) - 128);
-    d[i] = s;
-    y = (y - s) >> 8;
+  for (int u = 0; u < 8; ++u) {
+    const unsigned long long o = (unsigned long long)y[u] + 0x0080808080808080ull;
+    lo[u] = (uint32_t)o;
+    hi[u] = (uint32_t)(o >> 32);
   }
-  d[0] = (int)y;
-}
-
-__device__ __forceinline__ uint32_t bf16_pair(int a, int b) {
-  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)a)) |
-         ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)b)) << 16);
-}
-
-// Exponent e with max * 2^-e in [1/4, 1/2) (0 for a zero block).
-__device__ __forceinline__ int block_exp(double mx) {
-  if (mx == 0.0) return 0;
-  int E;
-  frexp(mx, &E);
-  return E + 1;
-}
-
-// 8 values (k = 8 j .. 8 j + 7 of a row) as 7 slices of one 16-byte chunk.
-__device__ __forceinline__ void store_chunks(uint8_t* base, int slice_bytes, int row, int j, const double (&v)[8],
-                                             double sc) {
-  int d[8][XR_SL];
-#pragma unroll
-  for (int u = 0; u < 8; ++u) digits7(llrint(v[u] * sc), d[u]);
   const int off = row * 128 + ((j ^ (row & 7)) << 4);
 #pragma unroll
   for (int p = 0; p < XR_SL; ++p) {
+    uint32_t f[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      if (p == 0) f[u] = __float_as_uint(__uint_as_float(0x4B400000u | (hi[u] >> 16)) - 12583040.0f);
+      else if (p <= 2) f[u] = digit_f32(hi[u], (uint32_t)(2 - p));
+      else f[u] = digit_f32(lo[u], (uint32_t)(6 - p));
+    }
     uint4 q;
-    q.x = bf16_pair(d[0][p], d[1][p]);
-    q.y = bf16_pair(d[2][p], d[3][p]);
-    q.z = bf16_pair(d[4][p], d[5][p]);
-    q.w = bf16_pair(d[6][p], d[7][p]);
+    q.x = __byte_perm(f[0], f[1], 0x7632);
+    q.y = __byte_perm(f[2], f[3], 0x7632);
+    q.z = __byte_perm(f[4], f[5], 0x7632);
+    q.w = __byte_perm(f[6], f[7], 0x7632);
     *reinterpret_cast<uint4*>(base + p * slice_bytes + off) = q;
   }
 }
@@ -743,10 +782,10 @@ __global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(E
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(xr_smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* sA = smem;
   uint8_t* sX = smem + XR_A_BYTES;
-  double* amax = reinterpret_cast<double*>(sX + XR_X_BYTES);  // [2][128]
-  double* xmax = amax + 2 * XR_ROWS;                            // [4][64]
-  int* ea_s = reinterpret_cast<int*>(xmax + 4 * XR_COLS);       // [128]
-  int* eb_s = ea_s + XR_ROWS;                                   // [64]
+  double* xraw = reinterpret_cast<double*>(sX + XR_X_BYTES);   // [64 columns][XR_XRP]
+  int* ebits = reinterpret_cast<int*>(xraw + XR_COLS * XR_XRP);  // [4][128] partial row maxima of the exponent field
+  int* ea_s = ebits + 4 * XR_ROWS;                               // [128]
+  int* eb_s = ea_s + XR_ROWS;                                    // [64]
   uint64_t* mma_bar = reinterpret_cast<uint64_t*>(eb_s + XR_COLS);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_bar + 1);
   __shared__ volatile int s_abort;
@@ -756,173 +795,206 @@ __global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(E
   const nla_batch_desc d = a.descs[g.sys];
   const int n = (int)d.n, r0 = tile.r0, c0 = tile.c0;
   const int ncols = min(XR_COLS, g.ncols - c0);
+  const int kend = min(n, r0 + XR_ROWS);  // k <= row
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int64_t dk = (a.rev ? -1 : 1) * (a.tA ? 1 : d.lda);  // step of canonical k within a row of A
+  const int64_t sk = a.rev ? -1 : 1;                          // step of canonical k within a column of X
+  const double* xbase = a.X64 + b_at(d, a.rev, 0, g.c0 + c0);  // canonical row 0 of the tile's first column
+  // Fixed point of the per-element sums: headroom for the tile's blocks.
+  const int lg = tile.nkb > 1 ? 32 - __clz(tile.nkb - 1) : 0;
+  const int sa_bits = 18 - lg, sl_bits = 24 - sa_bits;
 
   if (t == 0) {
     s_abort = 0;
     umma::mbar_init(umma::smem_u32(mma_bar), 1);
     umma::fence_barrier_init();
   }
-  if (warp == 8) umma::tmem_alloc(umma::smem_u32(tmem_slot), 512);
+  if (warp == 0) umma::tmem_alloc(umma::smem_u32(tmem_slot), 512);
+
+  // Scale exponents over the tile's K range: rows of L (thread -> row t % 128,
+  // every fourth k) and columns of X (warp w: columns w, w + 16, w + 32,
+  // w + 48, lanes along k).
+  {
+    const int row = t & 127, part = t >> 7, r = r0 + row;
+    const double* arow = a.A64 + a_at(d, a.tA, a.rev, min(r, n - 1), 0);
+    const int kr = r < n ? r + 1 : 0;
+    int bm = 0;
+#pragma unroll 8
+    for (int k = part; k < kr; k += 4) bm = max(bm, exp_field(__ldg(arow + (int64_t)k * dk)));
+    ebits[part * XR_ROWS + row] = bm;
+    int bx[4] = {0, 0, 0, 0};
+#pragma unroll 2
+    for (int k = lane; k < kend; k += 32) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (warp + 16 * c < ncols)
+          bx[c] = max(bx[c], exp_field(__ldcg(xbase + (int64_t)k * sk + (int64_t)(warp + 16 * c) * d.ldb)));
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int v = __reduce_max_sync(0xffffffffu, bx[c]);
+      if (lane == 0) eb_s[warp + 16 * c] = scale_exp(v);
+    }
+  }
   umma::fence_before_sync();
   __syncthreads();
   umma::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
+  if (t < XR_ROWS)
+    ea_s[t] = scale_exp(max(max(ebits[t], ebits[XR_ROWS + t]), max(ebits[2 * XR_ROWS + t], ebits[3 * XR_ROWS + t])));
+  __syncthreads();
 
-  // Epilogue role of a worker: rows q * 32 + lane, columns h * 32 .. + 32.
-  const int q = warp & 3, h = (warp >> 2) & 1;
-  double acc[32];
+  // Drain role: rows q * 32 + lane (the warp's TMEM lane quarter), columns
+  // h * 16 .. + 16.
+  const int q = warp & 3, h = warp >> 2;
+  long long acc[16];
 #pragma unroll
-  for (int j = 0; j < 32; ++j) acc[j] = 0.0;
+  for (int j = 0; j < 16; ++j) acc[j] = 0;
   bool ok = true;
+  // Split roles: A row t % 128 with the block's k values 16 (t / 128) ..
+  // + 16; X column t % 64 with k values 8 (t / 64) .. + 8, read back from the
+  // raw block, which threads load along k (thread -> k t % 64, columns
+  // t / 64 + 8 j): coalesced.
+  const int arow_i = t & 127, apart = t >> 7, ar = r0 + arow_i;
+  const double* arow = a.A64 + a_at(d, a.tA, a.rev, min(ar, n - 1), 0);
+  const int xk = t & 63, xc8 = t >> 6;
 
-  for (int kb = 0; kb < tile.nkb && ok; ++kb) {
+  int kb = 0;
+  for (; kb < tile.nkb && ok; ++kb) {
     const int k0 = kb * XR_KB;
-    // Two passes over the block: the largest magnitudes first, then the
-    // values again (from L1 / L2) to split them, so that no block of values
-    // stays in registers across the barrier.
-    if (warp < 8) {
-      // A: thread -> row t % 128, half t / 128 of the block's 64 values of k.
-      const int row = t & 127, half = t >> 7, r = r0 + row;
-      const double* arow = a.A64 + a_at(d, a.tA, a.rev, min(r, n - 1), 0);
-      double m = 0.0;
-#pragma unroll 8
-      for (int u = 0; u < 32; ++u) {
-        const int k = k0 + half * 32 + u;
-        if (r < n && k <= r) m = fmax(m, fabs(arow[(int64_t)k * dk]));
-      }
-      amax[half * XR_ROWS + row] = m;
-      // X: thread -> column t % 64, quarter t / 64 of the block's rows.
-      const int col = t & 63, qu = t >> 6;
-      double mx = 0.0;
-#pragma unroll 8
-      for (int u = 0; u < 16; ++u) {
-        const int k = k0 + qu * 16 + u;
-        if (k < n && col < ncols) mx = fmax(mx, fabs(__ldcg(a.X64 + b_at(d, a.rev, k, g.c0 + c0 + col))));
-      }
-      xmax[qu * XR_COLS + col] = mx;
-    }
-    __syncthreads();
-    if (warp < 8) {
-      const int row = t & 127, half = t >> 7, r = r0 + row;
-      const double* arow = a.A64 + a_at(d, a.tA, a.rev, min(r, n - 1), 0);
-      const int ea = block_exp(fmax(amax[row], amax[XR_ROWS + row]));
-      if (half == 0) ea_s[row] = ea;
-      const double sca = ldexp(1.0, 56 - ea);
-#pragma unroll 1
-      for (int c = 0; c < 4; ++c) {
-        double v[8];
+    {
+      double va[8], vx[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int k = k0 + half * 32 + c * 8 + u;
-          v[u] = r < n && k <= r ? arow[(int64_t)k * dk] : 0.0;
-        }
-        store_chunks(sA, XR_ROWS * 128, row, half * 4 + c, v, sca);
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + apart * 16 + u;
+        va[u] = ar < n && k <= ar ? __ldg(arow + (int64_t)k * dk) : 0.0;
       }
-      const int col = t & 63, qu = t >> 6;
-      const int eb = block_exp(fmax(fmax(xmax[col], xmax[XR_COLS + col]),
-                                    fmax(xmax[2 * XR_COLS + col], xmax[3 * XR_COLS + col])));
-      if (qu == 0) eb_s[col] = eb;
-      const double scx = ldexp(1.0, 56 - eb);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int k = k0 + xk, col = xc8 + 8 * j;
+        vx[j] = k < kend && col < ncols ? __ldcg(xbase + (int64_t)k * sk + (int64_t)col * d.ldb) : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) xraw[(xc8 + 8 * j) * XR_XRP + xk] = vx[j];
+      const int ea = ea_s[arow_i];
 #pragma unroll 1
       for (int c = 0; c < 2; ++c) {
-        double v[8];
+        long long y[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int k = k0 + qu * 16 + c * 8 + u;
-          v[u] = k < n && col < ncols ? __ldcg(a.X64 + b_at(d, a.rev, k, g.c0 + c0 + col)) : 0.0;
+        for (int u = 0; u < 8; ++u) y[u] = fixed56(va[u], ea);
+        if (c == 0) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int k = k0 + apart * 16 + 8 + u;
+            va[u] = ar < n && k <= ar ? __ldg(arow + (int64_t)k * dk) : 0.0;
+          }
         }
-        store_chunks(sX, XR_COLS * 128, col, qu * 2 + c, v, scx);
+        store_chunks(sA, XR_ROWS * 128, arow_i, apart * 2 + c, y);
       }
-      // The tensor cores read shared memory through the async proxy.
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
+    __syncthreads();  // the raw X block is in shared memory
+    {
+      const int col = t & 63, kc = t >> 6;
+      const int eb = eb_s[col];
+      long long y[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) y[u] = fixed56(xraw[col * XR_XRP + kc * 8 + u], eb);
+      store_chunks(sX, XR_COLS * 128, col, kc, y);
+    }
+    // The tensor cores read shared memory through the async proxy.
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
-    if (warp == 8 && lane == 0) {
+    if (t == 0) {
       const uint32_t idesc = umma::idesc_f16(XR_ROWS, XR_COLS, true);
       const uint32_t a0 = umma::smem_u32(sA), x0 = umma::smem_u32(sX);
 #pragma unroll 1
       for (int w = 0; w < XR_SL; ++w) {
-        const int p0 = w > XR_SL - 1 ? w - (XR_SL - 1) : 0;
-        for (int p = p0; p <= w && p < XR_SL; ++p) {
+        for (int p = 0; p <= w; ++p) {
           const int qq = w - p;
 #pragma unroll
           for (int kk = 0; kk < XR_KB / 16; ++kk)
             umma::mma_f16(tmem + (uint32_t)(w * XR_COLS),
                           umma::desc_kmajor_sw128(a0 + p * XR_ROWS * 128 + kk * 32),
                           umma::desc_kmajor_sw128(x0 + qq * XR_COLS * 128 + kk * 32), idesc,
-                          (p > p0 || kk > 0) ? 1u : 0u);
+                          (p > 0 || kk > 0) ? 1u : 0u);
         }
       }
       umma::mma_commit(umma::smem_u32(mma_bar));
     }
-    if (warp < 8) {
-      ok = __all_sync(0xffffffffu, umma::mbar_wait(umma::smem_u32(mma_bar), (uint32_t)kb & 1u, &s_abort, a.err, 21));
-      umma::fence_after_sync();
-      if (ok) {
-        const int row = q * 32 + lane;
-        const double sa = ldexp(1.0, ea_s[row] - 24);
+    __syncwarp();
+    ok = __all_sync(0xffffffffu, umma::mbar_wait(umma::smem_u32(mma_bar), (uint32_t)kb & 1u, &s_abort, a.err, 21));
+    umma::fence_after_sync();
+    if (ok) {
+      const long long lround = 1ll << (sl_bits - 1);
+      const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 16);
+      long long S[16];
+      // H: weights 0..3.
 #pragma unroll
-        for (int j0 = 0; j0 < 32; j0 += 16) {
-          // Two exact integer parts per element: weights 0..3 (H, in units of
-          // 2^72 of the digit products) and 4..6 (L, units of 2^48); each fits
-          // a double exactly, so nothing is rounded before the accumulator.
+      for (int j = 0; j < 16; ++j) S[j] = 0;
 #pragma unroll
-          for (int part = 0; part < 2; ++part) {
-            const int w0 = part == 0 ? 0 : 4, w1 = part == 0 ? 4 : XR_SL;
-            long long S[16];
+      for (int w = 0; w < 4; ++w) {
+        uint32_t rr[16];
+        umma::tmem_ld16(tq + (uint32_t)(w * XR_COLS), rr);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) S[j] = 0;
-#pragma unroll
-            for (int w = w0; w < w1; ++w) {
-              uint32_t rr[16];
-              umma::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(w * XR_COLS + h * 32 + j0), rr);
-              const int sh = 8 * (w1 - 1 - w);
-#pragma unroll
-              for (int j = 0; j < 16; ++j) S[j] += (long long)__float2int_rn(__uint_as_float(rr[j])) << sh;
-            }
-            const double sp = sa * (part == 0 ? 256.0 : 1.0 / 65536.0);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) acc[j0 + j] += (double)S[j] * sp * ldexp(1.0, eb_s[h * 32 + j0 + j] - 24);
-          }
-        }
+        for (int j = 0; j < 16; ++j) S[j] += (long long)__float2int_rn(__uint_as_float(rr[j])) << (24 - 8 * w);
       }
-    } else if (lane == 0) {
-      // Keep the MMA warp in step with the workers' view of the barrier.
-      umma::mbar_wait(umma::smem_u32(mma_bar), (uint32_t)kb & 1u, &s_abort, a.err, 22, false);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        acc[j] += S[j] << sa_bits;
+        S[j] = 0;
+      }
+      // L: weights 4..6, rounded to the fixed point.
+#pragma unroll
+      for (int w = 4; w < XR_SL; ++w) {
+        uint32_t rr[16];
+        umma::tmem_ld16(tq + (uint32_t)(w * XR_COLS), rr);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) S[j] += (long long)__float2int_rn(__uint_as_float(rr[j])) << (48 - 8 * w);
+      }
+#pragma unroll
+      for (int j = 0; j < 16; ++j) acc[j] += (S[j] + lround) >> sl_bits;
     }
     umma::fence_before_sync();
     __syncthreads();
     ok = ok && !s_abort;
   }
+  if (!ok && t == 0 && kb > 0) {
+    // A wait gave up: let the tensor cores finish the last block's MMAs (a
+    // drain with the default limit) before the tensor memory is released.
+    umma::mbar_wait(umma::smem_u32(mma_bar), (uint32_t)(kb - 1) & 1u, &s_abort, a.err, 22, false);
+  }
 
-  if (warp < 8 && ok) {
+  if (ok) {
     const int row = q * 32 + lane, r = r0 + row;
     if (r < n) {
-      // Loads of a half before its stores (the pools may alias as far as
-      // the compiler knows).
+      const int ea = ea_s[row];
+      // All loads before the stores (the pools may alias as far as the
+      // compiler knows).
+      double rv[16];
+      const int64_t rbase = b_at(d, a.rev, r, g.c0 + c0 + h * 16);
 #pragma unroll
-      for (int j0 = 0; j0 < 32; j0 += 16) {
-        double rv[16];
+      for (int j = 0; j < 16; ++j) {
+        const int col = h * 16 + j;
+        rv[j] = col < ncols ? a.R64[rbase + (int64_t)j * d.ldb] : 0.0;
+      }
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int col = h * 32 + j0 + j;
-          rv[j] = col < ncols ? a.R64[b_at(d, a.rev, r, g.c0 + c0 + col)] : 0.0;
-        }
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int col = h * 32 + j0 + j;
-          if (col < ncols) a.D32[b_at(d, a.rev, r, g.c0 + c0 + col)] = (float)(rv[j] - acc[j0 + j]);
+      for (int j = 0; j < 16; ++j) {
+        const int col = h * 16 + j;
+        if (col < ncols) {
+          const int eb = eb_s[col];
+          const float res = ea == XR_NONFINITE || eb == XR_NONFINITE
+                                ? __int_as_float(0x7FC00000)
+                                : (float)(rv[j] - ldexp((double)acc[j], ea + eb - 40 - sa_bits));
+          a.D32[rbase + (int64_t)j * d.ldb] = res;
         }
       }
     }
   }
   umma::fence_before_sync();
   __syncthreads();
-  if (warp == 8) {
+  if (warp == 0) {
     umma::fence_after_sync();
     umma::tmem_dealloc(tmem, 512);
   }

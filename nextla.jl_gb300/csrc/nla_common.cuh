@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/nextla_gb300.h"
 
@@ -134,8 +135,11 @@ int launch_scale_complex(int dtype, int64_t rows, int64_t cols, double alpha_re,
 // Tensor-core update on staged slices (nla_umma.cu).  C (M x N) += alpha *
 // op(A) (M x K) * op(B) (K x N); in_dtype NLA_F64 (split into S BF16/FP16
 // slices) or NLA_F16 (one unscaled slice); out_dtype NLA_F64 or NLA_F16.
+// With overwrite (exact 7-slice products only) C := alpha * op(A) op(B); C may
+// then be the same matrix as B (both operands are staged before C is written).
 int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat& A, const Mat& B, const Mat& C,
-                       int in_dtype, int out_dtype, int S, bool bf16, void* ws, size_t ws_bytes, cudaStream_t s);
+                       int in_dtype, int out_dtype, int S, bool bf16, void* ws, size_t ws_bytes, cudaStream_t s,
+                       bool overwrite = false);
 size_t sliced_workspace_bytes(int64_t M, int64_t N, int64_t K, int S);
 
 // An operand staged for the tensor cores: S K-major 16-bit slices of a
@@ -170,13 +174,30 @@ struct ResidualTerm {
 // fixed_buf (A.rows_pad x N int64, or null) lets a plain update leave its
 // fixed-point sums there for a separate finishing pass over C.
 int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat& C, bool trans_out,
-                      cudaStream_t s, const ResidualTerm* res = nullptr, long long* fixed_buf = nullptr);
+                      cudaStream_t s, const ResidualTerm* res = nullptr, long long* fixed_buf = nullptr,
+                      bool overwrite = false);
 constexpr int EXACT_SLICES = 7;
 int workspace_get(cudaStream_t s, size_t bytes, void** out);
 int device_status(cudaStream_t s);
 int set_wait_limit(uint64_t ns);
 uint64_t wait_limit_ns();  // the limit last set (default 2 s), for kernels that take it as a parameter
 int batch_device_error();  // the batched kernel's error word (read and cleared), or 0
+
+// Inverses of the diagonal blocks (leaves) of a mixed solve's recursion,
+// W = inv(T) for each leaf block T (lower or upper as the recursion sees it),
+// one 64 x 64 slot each in w.  A leaf is then X := W X on the tensor cores
+// with the exact slice products.  Upfront: every leaf's inverse is
+// formed before the recursion, slot j for the j-th leaf offset in k.  Lazy
+// (the host-buffer path, where A arrives block by block): each leaf inverts
+// its block into slot 0 just before its product.
+constexpr int LEAF_INV_N = 64;
+struct LeafInverses {
+  const double* a_base = nullptr;  // A as the recursion indexes it
+  int64_t lda = 0;
+  double* w = nullptr;
+  std::vector<int64_t> k;  // leaf offsets, increasing
+  bool lazy = false;
+};
 
 // The recursion of unified_rec (src/rectrxm.jl:101-198) with a choice of
 // update kernel.
@@ -190,9 +211,24 @@ struct RecPlan {
   int mode;
   int S;
   bool bf16;
-  bool unit = false;  // unit diagonal (plain path only)
+  bool unit = false;  // unit diagonal
+  const LeafInverses* inv = nullptr;  // leaves through their inverses (mixed exact solves)
 };
 int recurse(const RecPlan& c, const Mat& A, int64_t n, const Mat& B);
+// Mixed exact solves: whether the leaves go through inverses (a 7-slice solve
+// with leaves of at most LEAF_INV_N rows, unless NLA_MIXED_INV_LEAF=0), the
+// upfront and lazy set-ups, and the leaf itself.
+bool leaf_inverses_wanted(const RecPlan& c);
+int leaf_inverses_upfront(const RecPlan& c, const Mat& A, int64_t n, LeafInverses* out);
+int leaf_inverses_lazy(const RecPlan& c, LeafInverses* out);
+int leaf_inverse_apply(const RecPlan& c, const Mat& A, int64_t n, const Mat& B);
+// Launches inside the scope are traced under kernel class kclass (the leaf
+// products of a mixed solve run the update kernels but are leaf work).
+struct TraceClassScope {
+  int prev;
+  explicit TraceClassScope(int kclass);
+  ~TraceClassScope();
+};
 // One node of the recursion: which half goes first, which off-diagonal block
 // the update between the halves reads, and that update.
 bool rec_forward(const RecPlan& c);

@@ -344,6 +344,14 @@ int nla_trxm_mixed_host(char side, char uplo, char trans, double alpha, char fun
   h.Bd = reinterpret_cast<char*>(B_dev);
   h.ldbd = ldb_dev;
   const bool whole = func == 'S' && o.sweeps > 0;
+  // The staged walk brings A in block by block, so each leaf inverts its own
+  // block just before its product (the whole-array form inverts them all
+  // inside trxm_mixed_impl).
+  LeafInverses lazy;
+  if (!whole && leaf_inverses_wanted(h.c)) {
+    NLA_TRY(leaf_inverses_lazy(h.c, &lazy));
+    h.c.inv = &lazy;
+  }
   return host_run(h, n, host_levels(levels), whole, [&] {
     return trxm_mixed_impl(side, uplo, trans, alpha, func, n, m, A_dev, lda_dev, B_dev, ldb_dev, &o, s);
   });

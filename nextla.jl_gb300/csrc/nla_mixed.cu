@@ -8,8 +8,11 @@
 // wins back the accuracy the split loses.
 #include <cmath>
 #include <cstdlib>
+#include <algorithm>
+#include <climits>
 #include <mutex>
 #include <unordered_map>
+#include <vector>
 
 #include "nla_common.cuh"
 
@@ -163,6 +166,195 @@ int default_mixed_cutoff() {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Leaves of a mixed exact solve through their inverses.  GB300 runs FP64 FMAs
+// at 2 per clock per SM, so the substitution leaf (n^2 m / 2 FMAs per block)
+// is a large share of a solve whose updates run on the tensor cores.  Here
+// each leaf block T (at most 64 rows) is inverted once in FP64, and the leaf
+// becomes X := inv(T) X, an exact 7-slice product on the tensor cores
+// rounded once per element.  (X + (inv(T) - I) X, which needs no overwrite,
+// loses digits to cancellation when T's diagonal is large: x ~ b / d from
+// b - (1 - 1/d) b.)
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int INV_MAX = 1900;  // leaves per launch (the table rides in the kernel parameters)
+
+struct LeafInvArgs {
+  const double* A;  // leaf j's block starts at A + k[j] * (lda + 1)
+  int64_t lda;
+  int tA, upper, unit;
+  double* W;  // slot first_slot + j at W + (first_slot + j) * 64 * 64, leading dimension 64
+  int first_slot;
+  int count;
+  int k[INV_MAX];
+  int nl[INV_MAX];
+};
+
+// One CTA per leaf.  The block is read in canonical lower orientation (an
+// upper block with its indices reversed), the inverse formed column by
+// column by right-looking substitution (four threads per column, in one
+// warp, rows split by residue mod 4), and written back in the block's own
+// orientation.
+constexpr int INV_SMEM = (2 * LEAF_INV_N * (LEAF_INV_N + 1) + LEAF_INV_N) * (int)sizeof(double);
+
+__global__ void __launch_bounds__(256) leaf_inverse_kernel(const __grid_constant__ LeafInvArgs g) {
+  extern __shared__ double inv_smem[];
+  auto T = reinterpret_cast<double (*)[LEAF_INV_N + 1]>(inv_smem);
+  auto S = reinterpret_cast<double (*)[LEAF_INV_N + 1]>(inv_smem + LEAF_INV_N * (LEAF_INV_N + 1));
+  double* dinv = inv_smem + 2 * LEAF_INV_N * (LEAF_INV_N + 1);
+  const int b = blockIdx.x, t = threadIdx.x, n = g.nl[b];
+  const double* Ab = g.A + (int64_t)g.k[b] * (g.lda + 1);
+  for (int idx = t; idx < n * n; idx += blockDim.x) {
+    const int i = idx % n, j = idx / n;
+    double v = 0.0;
+    if (j <= i) {
+      const int ri = g.upper ? n - 1 - i : i, rj = g.upper ? n - 1 - j : j;
+      v = g.tA ? Ab[rj + (int64_t)ri * g.lda] : Ab[ri + (int64_t)rj * g.lda];
+    }
+    T[i][j] = v;
+    S[i][j] = i == j ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  if (t < n) dinv[t] = g.unit ? 1.0 : 1.0 / T[t][t];
+  __syncthreads();
+  const int j = t >> 2, rg = t & 3;
+  for (int i = 0; i < n; ++i) {
+    double x = 0.0;
+    if (j < n && i >= j) x = S[i][j] * dinv[i];
+    __syncwarp();
+    if (j < n && i >= j) {
+      if (rg == (i & 3)) S[i][j] = x;
+      for (int r = i + 1 + ((rg - i - 1) & 3); r < n; r += 4) S[r][j] -= T[r][i] * x;
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  double* W = g.W + (int64_t)(g.first_slot + b) * LEAF_INV_N * LEAF_INV_N;
+  for (int idx = t; idx < n * n; idx += blockDim.x) {
+    const int i = idx % n, jj = idx / n;
+    const double v = jj <= i ? S[i][jj] : 0.0;
+    const int ri = g.upper ? n - 1 - i : i, rj = g.upper ? n - 1 - jj : jj;
+    W[ri + (int64_t)rj * LEAF_INV_N] = v;
+  }
+}
+
+std::mutex g_inv_mu;
+std::unordered_map<uint64_t, Buf> g_inv_bufs;
+
+// The inverses' slots, one buffer per (device, stream), grown on demand.
+int inverse_buffer(cudaStream_t s, size_t bytes, double** out) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t key = ((uint64_t)(uint32_t)dev << 48) ^ (uint64_t)reinterpret_cast<uintptr_t>(s);
+  std::lock_guard<std::mutex> lk(g_inv_mu);
+  Buf& b = g_inv_bufs[key];
+  if (b.n < bytes) {
+    if (b.p) cudaFreeAsync(b.p, s);
+    b.p = nullptr;
+    b.n = 0;
+    cudaError_t e = cudaMallocAsync(&b.p, bytes, s);
+    if (e != cudaSuccess) {
+      b.p = nullptr;
+      return cuda_status(e, "leaf inverse buffer");
+    }
+    b.n = bytes;
+  }
+  *out = static_cast<double*>(b.p);
+  return NLA_OK;
+}
+
+void collect_leaves(int64_t k, int64_t n, int64_t thr, std::vector<int64_t>* ks, std::vector<int>* ns) {
+  if (n <= thr) {
+    ks->push_back(k);
+    ns->push_back((int)n);
+    return;
+  }
+  const int64_t mid = split_point(n);
+  collect_leaves(k, mid, thr, ks, ns);
+  collect_leaves(k + mid, n - mid, thr, ks, ns);
+}
+
+int launch_inverses(const RecPlan& c, const double* A, int64_t lda, int tA, const std::vector<int64_t>& ks,
+                    const std::vector<int>& ns, double* W, int first) {
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [] {
+    attr = cudaFuncSetAttribute(leaf_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, INV_SMEM);
+  });
+  if (attr != cudaSuccess) return cuda_status(attr, "cudaFuncSetAttribute(leaf_inverse_kernel)");
+  TraceScope trace(NLA_K_LEAF_SOLVE, c.s, 0.0, 0.0);
+  for (size_t j0 = 0; j0 < ks.size(); j0 += INV_MAX) {
+    LeafInvArgs g{};
+    g.A = A;
+    g.lda = lda;
+    g.tA = tA;
+    g.upper = c.uplo == 'U';
+    g.unit = c.unit ? 1 : 0;
+    g.W = W;
+    g.first_slot = first + (int)j0;
+    g.count = (int)std::min<size_t>(INV_MAX, ks.size() - j0);
+    for (int j = 0; j < g.count; ++j) {
+      g.k[j] = (int)ks[j0 + j];
+      g.nl[j] = ns[j0 + j];
+    }
+    leaf_inverse_kernel<<<(unsigned)g.count, 256, INV_SMEM, c.s>>>(g);
+    NLA_CHECK_LAUNCH("leaf_inverse_kernel");
+  }
+  return NLA_OK;
+}
+
+}  // namespace
+
+bool leaf_inverses_wanted(const RecPlan& c) {
+  if (c.mode != GEMM_MIXED || c.S != EXACT_SLICES || !c.bf16 || c.func != 'S' || c.dtype != NLA_F64) return false;
+  if (c.threshold > LEAF_INV_N) return false;
+  // The leaf overwrites X from the finishing pass (NLA_EXACT_FINISH=0 removes it).
+  const char* f = std::getenv("NLA_EXACT_FINISH");
+  if (f && f[0] == '0') return false;
+  const char* v = std::getenv("NLA_MIXED_INV_LEAF");
+  return !(v && v[0] == '0');
+}
+
+int leaf_inverses_upfront(const RecPlan& c, const Mat& A, int64_t n, LeafInverses* out) {
+  out->a_base = static_cast<const double*>(A.p);
+  out->lda = A.ld;
+  out->lazy = false;
+  out->k.clear();
+  std::vector<int> ns;
+  collect_leaves(0, n, c.threshold, &out->k, &ns);
+  if (n > INT32_MAX) return fail(NLA_ERR_UNSUPPORTED, "leaf inverses: n too large");
+  NLA_TRY(inverse_buffer(c.s, out->k.size() * LEAF_INV_N * LEAF_INV_N * sizeof(double), &out->w));
+  return launch_inverses(c, out->a_base, A.ld, A.t, out->k, ns, out->w, 0);
+}
+
+int leaf_inverses_lazy(const RecPlan& c, LeafInverses* out) {
+  out->lazy = true;
+  out->k.clear();
+  return inverse_buffer(c.s, LEAF_INV_N * LEAF_INV_N * sizeof(double), &out->w);
+}
+
+int leaf_inverse_apply(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
+  if (n <= 0 || c.m <= 0) return NLA_OK;
+  const LeafInverses& L = *c.inv;
+  TraceClassScope cls(NLA_K_LEAF_SOLVE);
+  int64_t slot = 0;
+  if (L.lazy) {
+    NLA_TRY(launch_inverses(c, static_cast<const double*>(A.p), A.ld, A.t, std::vector<int64_t>{0},
+                            std::vector<int>{(int)n}, L.w, 0));
+  } else {
+    const int64_t k = (static_cast<const double*>(A.p) - L.a_base) / (L.lda + 1);
+    const auto it = std::lower_bound(L.k.begin(), L.k.end(), k);
+    if (it == L.k.end() || *it != k) return fail(NLA_ERR_ARG, "leaf inverses: no inverse for this block");
+    slot = it - L.k.begin();
+  }
+  const Mat W{L.w + slot * LEAF_INV_N * LEAF_INV_N, LEAF_INV_N, 0};
+  // X := inv(T) X  (side L)  or  X inv(T)  (side R).
+  if (c.side == 'L')
+    return launch_sliced_gemm(n, c.m, n, 1.0, W, B, B, NLA_F64, NLA_F64, EXACT_SLICES, true, nullptr, 0, c.s, true);
+  return launch_sliced_gemm(c.m, n, n, 1.0, B, W, B, NLA_F64, NLA_F64, EXACT_SLICES, true, nullptr, 0, c.s, true);
+}
+
 // Stage the strict triangle of op(A) as the row operand of the residual
 // product: op(A) itself for side L, op(A)^T for side R.
 int stage_triangle(const Mat& Am, int64_t n, char side, char uplo, void* buf, Staged* out, cudaStream_t s) {
@@ -244,6 +436,11 @@ int trxm_mixed_impl(char side, char uplo, char trans, double alpha, char func, i
   if (func == 'M') {
     NLA_TRY(recurse(mixed, Am, n, Bm));
     return launch_scale(NLA_F64, rows, cols, alpha, Bm, s);  // src/rectrxm.jl:72
+  }
+  LeafInverses inv;
+  if (leaf_inverses_wanted(mixed)) {
+    NLA_TRY(leaf_inverses_upfront(mixed, Am, n, &inv));
+    mixed.inv = &inv;
   }
 
   NLA_TRY(launch_scale(NLA_F64, rows, cols, alpha, Bm, s));  // src/rectrxm.jl:64

@@ -97,3 +97,35 @@ def test_refinement_residual_modes(pkg, oracle, workloads, cuda, residual):
         ref = oracle.rectrxm(side, uplo, trans, 0.5, "S", A, B, nthreads=os.cpu_count() or 1)
         X = _mixed(pkg, cuda, side, uplo, trans, 0.5, "S", A, B, split_terms=2, sweeps=3, residual=residual)
         assert oracle.rel_err(X, ref) < 1e-14, (side, uplo, trans)
+
+
+@pytest.mark.parametrize("diag", ["N", "U"])
+def test_inverse_leaves_match_substitution(pkg, oracle, workloads, cuda, diag, monkeypatch):
+    """Exact 7-slice solves apply each leaf block through its FP64 inverse on
+    the tensor cores (X += (inv(T) - I) X).  Over every side, uplo and trans,
+    sizes with ragged leaves (n = 1, 65, 1000, 1500) and a unit diagonal,
+    the result matches the substitution leaves (NLA_MIXED_INV_LEAF=0) and
+    the oracle at the Float64 tolerance."""
+    import torch
+
+    nthreads = os.cpu_count() or 1
+    for k, (n, side, uplo, trans) in enumerate(itertools.product([1, 65, 1000], "LR", "LU", "NT")):
+        A, B = workloads.problem(n, 37, side, uplo, seed=300 + k)
+        if diag == "U":
+            A = np.array(A) / max(n, 1)  # well conditioned with a unit diagonal too
+            A[np.diag_indices(n)] = 1.0  # what the unit solve assumes; the device copy gets NaNs there
+        out = {}
+        for inv in ("1", "0"):
+            monkeypatch.setenv("NLA_MIXED_INV_LEAF", inv)
+            An = np.array(A)
+            if diag == "U":
+                An[np.diag_indices(n)] = np.nan
+            Ad, Bd = to_dev(An, np.float64, cuda), to_dev(B, np.float64, cuda)
+            pkg.trsm(side, uplo, trans, diag, Ad, Bd, 0.5, mixed=True)
+            pkg.device_status(Bd)
+            torch.cuda.synchronize()
+            out[inv] = to_host(Bd)
+        ref = oracle.rectrxm(side, uplo, trans, 0.5, "S", A, B, nthreads=nthreads)
+        assert np.isfinite(out["1"]).all(), (n, side, uplo, trans)
+        assert oracle.rel_err(out["1"], ref) < 1e-13, (n, side, uplo, trans)
+        assert oracle.rel_err(out["1"], out["0"]) < 1e-13, (n, side, uplo, trans)
