@@ -715,6 +715,10 @@ struct ExactResArgs {
   float* D32;
   int tA, rev;
   int* err;
+  const int* row_exp;        // scale exponent of each system row of A's triangle
+  const int64_t* row_base;   // first row_exp entry of each system
+  const int* col_exp;        // scale exponent of each group column of X
+  const int64_t* col_base;   // first col_exp entry of each group
 };
 
 // Biased exponent field of a double.
@@ -725,6 +729,61 @@ __device__ __forceinline__ int exp_field(double v) { return (__double2hiint(v) >
 // subnormal, XR_NONFINITE when one is Inf or NaN).
 __device__ __forceinline__ int scale_exp(int bmax) {
   return bmax == 0x7FF ? XR_NONFINITE : (bmax == 0 ? 0 : bmax - 1021);
+}
+
+// Scale exponents of the rows of A's canonical lower triangles (k <= r), one
+// CTA per band of 128 rows of a system, two threads per row.  A does not
+// change between sweeps, so this runs once per mixed solve.
+struct RowExpArgs {
+  const nla_batch_desc* descs;
+  const int2* bands;  // (system, first row of the band)
+  const int64_t* row_base;
+  const double* A64;
+  int tA, rev;
+  int* out;
+};
+
+__global__ void __launch_bounds__(256) batched_row_exp_kernel(RowExpArgs a) {
+  __shared__ int part_max[256];
+  const int2 b = a.bands[blockIdx.x];
+  const nla_batch_desc d = a.descs[b.x];
+  const int n = (int)d.n, t = threadIdx.x, row = t & 127, part = t >> 7, r = b.y + row;
+  const int64_t dk = (a.rev ? -1 : 1) * (a.tA ? 1 : d.lda);
+  int bm = 0;
+  if (r < n) {
+    const double* arow = a.A64 + a_at(d, a.tA, a.rev, r, 0);
+#pragma unroll 8
+    for (int k = part; k <= r; k += 2) bm = max(bm, exp_field(__ldg(arow + (int64_t)k * dk)));
+  }
+  part_max[t] = bm;
+  __syncthreads();
+  if (t < 128 && r < n) a.out[a.row_base[b.x] + r] = scale_exp(max(part_max[t], part_max[t + 128]));
+}
+
+// Scale exponents of the columns of X (over all n rows of the system), one
+// CTA per group, a warp per column with its lanes along the column.
+struct ColExpArgs {
+  const nla_batch_desc* descs;
+  const Group* groups;
+  const int64_t* col_base;
+  const double* X64;
+  int rev;
+  int* out;
+};
+
+__global__ void __launch_bounds__(256) batched_col_exp_kernel(ColExpArgs a) {
+  const Group g = a.groups[blockIdx.x];
+  const nla_batch_desc d = a.descs[g.sys];
+  const int n = (int)d.n, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t sk = a.rev ? -1 : 1;
+  for (int c = warp; c < g.ncols; c += 8) {
+    const double* xc = a.X64 + b_at(d, a.rev, 0, g.c0 + c);
+    int bx = 0;
+#pragma unroll 4
+    for (int k = lane; k < n; k += 32) bx = max(bx, exp_field(__ldcg(xc + (int64_t)k * sk)));
+    bx = __reduce_max_sync(0xffffffffu, bx);
+    if (lane == 0) a.out[a.col_base[blockIdx.x] + c] = scale_exp(bx);
+  }
 }
 
 // y = round(v 2^(56 - e)) from the bits of v (|v| < 2^(e - 1), so |y| < 2^55;
@@ -783,8 +842,7 @@ __global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(E
   uint8_t* sA = smem;
   uint8_t* sX = smem + XR_A_BYTES;
   double* xraw = reinterpret_cast<double*>(sX + XR_X_BYTES);   // [64 columns][XR_XRP]
-  int* ebits = reinterpret_cast<int*>(xraw + XR_COLS * XR_XRP);  // [4][128] partial row maxima of the exponent field
-  int* ea_s = ebits + 4 * XR_ROWS;                               // [128]
+  int* ea_s = reinterpret_cast<int*>(xraw + XR_COLS * XR_XRP);  // [128]
   int* eb_s = ea_s + XR_ROWS;                                    // [64]
   uint64_t* mma_bar = reinterpret_cast<uint64_t*>(eb_s + XR_COLS);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_bar + 1);
@@ -811,38 +869,17 @@ __global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(E
   }
   if (warp == 0) umma::tmem_alloc(umma::smem_u32(tmem_slot), 512);
 
-  // Scale exponents over the tile's K range: rows of L (thread -> row t % 128,
-  // every fourth k) and columns of X (warp w: columns w, w + 16, w + 32,
-  // w + 48, lanes along k).
-  {
-    const int row = t & 127, part = t >> 7, r = r0 + row;
-    const double* arow = a.A64 + a_at(d, a.tA, a.rev, min(r, n - 1), 0);
-    const int kr = r < n ? r + 1 : 0;
-    int bm = 0;
-#pragma unroll 8
-    for (int k = part; k < kr; k += 4) bm = max(bm, exp_field(__ldg(arow + (int64_t)k * dk)));
-    ebits[part * XR_ROWS + row] = bm;
-    int bx[4] = {0, 0, 0, 0};
-#pragma unroll 2
-    for (int k = lane; k < kend; k += 32) {
-#pragma unroll
-      for (int c = 0; c < 4; ++c)
-        if (warp + 16 * c < ncols)
-          bx[c] = max(bx[c], exp_field(__ldcg(xbase + (int64_t)k * sk + (int64_t)(warp + 16 * c) * d.ldb)));
-    }
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const int v = __reduce_max_sync(0xffffffffu, bx[c]);
-      if (lane == 0) eb_s[warp + 16 * c] = scale_exp(v);
-    }
+  // Scale exponents (per row of A's triangle and per column of X, formed by
+  // batched_row_exp_kernel and batched_col_exp_kernel).
+  if (t < XR_ROWS) ea_s[t] = r0 + t < n ? a.row_exp[a.row_base[g.sys] + r0 + t] : 0;
+  else if (t < XR_ROWS + XR_COLS) {
+    const int c = t - XR_ROWS;
+    eb_s[c] = c < ncols ? a.col_exp[a.col_base[tile.group] + c0 + c] : 0;
   }
   umma::fence_before_sync();
   __syncthreads();
   umma::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
-  if (t < XR_ROWS)
-    ea_s[t] = scale_exp(max(max(ebits[t], ebits[XR_ROWS + t]), max(ebits[2 * XR_ROWS + t], ebits[3 * XR_ROWS + t])));
-  __syncthreads();
 
   // Drain role: rows q * 32 + lane (the warp's TMEM lane quarter), columns
   // h * 16 .. + 16.
@@ -859,23 +896,33 @@ __global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(E
   const double* arow = a.A64 + a_at(d, a.tA, a.rev, min(ar, n - 1), 0);
   const int xk = t & 63, xc8 = t >> 6;
 
+  // One block ahead: the raw X block goes to shared memory by asynchronous
+  // copies (zero-filled outside the system), and the first eight values of
+  // A into registers, so that both latencies pass during the previous
+  // block's MMAs and drain.
+  double va[8];
+  auto load_ahead = [&](int k0) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int k = k0 + xk, col = xc8 + 8 * j;
+      const bool in = k < kend && col < ncols;
+      const double* src = in ? xbase + (int64_t)k * sk + (int64_t)col * d.ldb : a.X64;
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(umma::smem_u32(xraw + (xc8 + 8 * j) * XR_XRP + xk)),
+                   "l"(src), "r"(in ? 8 : 0)
+                   : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int k = k0 + apart * 16 + u;
+      va[u] = ar < n && k <= ar ? __ldg(arow + (int64_t)k * dk) : 0.0;
+    }
+  };
+  load_ahead(0);
   int kb = 0;
   for (; kb < tile.nkb && ok; ++kb) {
     const int k0 = kb * XR_KB;
     {
-      double va[8], vx[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int k = k0 + apart * 16 + u;
-        va[u] = ar < n && k <= ar ? __ldg(arow + (int64_t)k * dk) : 0.0;
-      }
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int k = k0 + xk, col = xc8 + 8 * j;
-        vx[j] = k < kend && col < ncols ? __ldcg(xbase + (int64_t)k * sk + (int64_t)col * d.ldb) : 0.0;
-      }
-#pragma unroll
-      for (int j = 0; j < 8; ++j) xraw[(xc8 + 8 * j) * XR_XRP + xk] = vx[j];
       const int ea = ea_s[arow_i];
 #pragma unroll 1
       for (int c = 0; c < 2; ++c) {
@@ -892,6 +939,7 @@ __global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(E
         store_chunks(sA, XR_ROWS * 128, arow_i, apart * 2 + c, y);
       }
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();  // the raw X block is in shared memory
     {
       const int col = t & 63, kc = t >> 6;
@@ -924,6 +972,7 @@ __global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(E
       umma::mma_commit(umma::smem_u32(mma_bar));
     }
     __syncwarp();
+    if (kb + 1 < tile.nkb) load_ahead(k0 + XR_KB);  // the X split above has read the raw block
     ok = __all_sync(0xffffffffu, umma::mbar_wait(umma::smem_u32(mma_bar), (uint32_t)kb & 1u, &s_abort, a.err, 21));
     umma::fence_after_sync();
     if (ok) {
@@ -960,6 +1009,7 @@ __global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(E
     __syncthreads();
     ok = ok && !s_abort;
   }
+  asm volatile("cp.async.wait_all;" ::: "memory");  // no copy into shared memory outlives the loop
   if (!ok && t == 0 && kb > 0) {
     // A wait gave up: let the tensor cores finish the last block's MMAs (a
     // drain with the default limit) before the tensor memory is released.
@@ -1035,9 +1085,16 @@ struct nla_batch_plan_s {
   float* a32;
   float* x32;
   double* r64;
-  // Tiles of the tensor-core residual (built on first use).
+  // Tensor-core residual (built on first use): tiles, row bands, the
+  // exponents' indexing and the exponents, in one allocation.
   void* d_xtiles;
   int nxtiles;
+  int2* d_bands;
+  int nbands;
+  int64_t* d_row_base;
+  int64_t* d_col_base;
+  int* d_row_exp;
+  int* d_col_exp;
 };
 
 namespace nla {
@@ -1315,6 +1372,10 @@ int plan_create(nla_batch_plan* out, int dtype, char uplo, char trans, int64_t c
   p->r64 = nullptr;
   p->d_xtiles = nullptr;
   p->nxtiles = 0;
+  p->d_bands = nullptr;
+  p->nbands = 0;
+  p->d_row_base = p->d_col_base = nullptr;
+  p->d_row_exp = p->d_col_exp = nullptr;
   p->exec = nullptr;
   p->d_descs = p->d_groups = p->d_nodes = nullptr;
   p->d_counters = nullptr;
@@ -1406,8 +1467,9 @@ int plan_create(nla_batch_plan* out, int dtype, char uplo, char trans, int64_t c
 }
 
 // Tiles of the tensor-core residual: 128 rows x 64 right-hand sides of a
-// group, with their blocks of K (k <= row), longest first; and the kernel's
-// shared-memory limit.
+// group, with their blocks of K (k <= row), longest first; the 128-row bands
+// of every system for the row exponents; the exponents' indexing; and the
+// kernel's shared-memory limit.  One device allocation holds them all.
 int exact_residual_setup(nla_batch_plan p) {
   static std::once_flag once;
   static cudaError_t st = cudaSuccess;
@@ -1418,8 +1480,12 @@ int exact_residual_setup(nla_batch_plan p) {
   if (st != cudaSuccess) return cuda_status(st, "cudaFuncSetAttribute(batched_exact_residual_kernel)");
   if (p->d_xtiles) return NLA_OK;
   std::vector<bat::ExactTile> tiles;
+  std::vector<int64_t> col_base(p->h_groups.size());
+  int64_t ncol = 0;
   for (int gi = 0; gi < (int)p->h_groups.size(); ++gi) {
     const bat::Group& g = p->h_groups[gi];
+    col_base[gi] = ncol;
+    ncol += g.ncols;
     for (int r0 = 0; r0 < g.n; r0 += bat::XR_ROWS)
       for (int c0 = 0; c0 < g.ncols; c0 += bat::XR_COLS) {
         const int kend = std::min(g.n, r0 + bat::XR_ROWS);
@@ -1429,15 +1495,42 @@ int exact_residual_setup(nla_batch_plan p) {
   std::stable_sort(tiles.begin(), tiles.end(),
                    [](const bat::ExactTile& x, const bat::ExactTile& y) { return x.nkb > y.nkb; });
   if (tiles.empty()) return NLA_OK;  // nothing to launch
-  cudaError_t e = cudaMalloc(&p->d_xtiles, sizeof(bat::ExactTile) * tiles.size());
-  if (e == cudaSuccess)
-    e = cudaMemcpy(p->d_xtiles, tiles.data(), sizeof(bat::ExactTile) * tiles.size(), cudaMemcpyHostToDevice);
+  std::vector<int2> bands;
+  std::vector<int64_t> row_base(p->h_descs.size());
+  int64_t nrow = 0;
+  for (size_t i = 0; i < p->h_descs.size(); ++i) {
+    row_base[i] = nrow;
+    nrow += p->h_descs[i].n;
+    for (int64_t r0 = 0; r0 < p->h_descs[i].n; r0 += bat::XR_ROWS) bands.push_back(make_int2((int)i, (int)r0));
+  }
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t o_bands = up(sizeof(bat::ExactTile) * tiles.size());
+  const size_t o_rb = o_bands + up(sizeof(int2) * std::max<size_t>(bands.size(), 1));
+  const size_t o_cb = o_rb + up(sizeof(int64_t) * row_base.size());
+  const size_t o_re = o_cb + up(sizeof(int64_t) * std::max<size_t>(col_base.size(), 1));
+  const size_t o_ce = o_re + up(sizeof(int) * (size_t)std::max<int64_t>(nrow, 1));
+  const size_t total = o_ce + up(sizeof(int) * (size_t)std::max<int64_t>(ncol, 1));
+  uint8_t* base = nullptr;
+  cudaError_t e = cudaMalloc(&base, total);
+  if (e == cudaSuccess) e = cudaMemcpy(base, tiles.data(), sizeof(bat::ExactTile) * tiles.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !bands.empty())
+    e = cudaMemcpy(base + o_bands, bands.data(), sizeof(int2) * bands.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !row_base.empty())
+    e = cudaMemcpy(base + o_rb, row_base.data(), sizeof(int64_t) * row_base.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !col_base.empty())
+    e = cudaMemcpy(base + o_cb, col_base.data(), sizeof(int64_t) * col_base.size(), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
-    cudaFree(p->d_xtiles);
-    p->d_xtiles = nullptr;
+    cudaFree(base);
     return cuda_status(e, "residual tiles");
   }
+  p->d_xtiles = base;
   p->nxtiles = (int)tiles.size();
+  p->d_bands = reinterpret_cast<int2*>(base + o_bands);
+  p->nbands = (int)bands.size();
+  p->d_row_base = reinterpret_cast<int64_t*>(base + o_rb);
+  p->d_col_base = reinterpret_cast<int64_t*>(base + o_cb);
+  p->d_row_exp = reinterpret_cast<int*>(base + o_re);
+  p->d_col_exp = reinterpret_cast<int*>(base + o_ce);
   return NLA_OK;
 }
 
@@ -1598,11 +1691,23 @@ int nla_batch_solve_mixed_ex(nla_batch_plan p, double alpha, const void* A_pool,
   void* errp = nullptr;
   cudaError_t ee = cudaGetSymbolAddress(&errp, bat::g_batch_error);
   if (ee != cudaSuccess) return cuda_status(ee, "batch error word");
-  const bat::ExactResArgs xr{descs, groups, static_cast<const bat::ExactTile*>(p->d_xtiles), A64, B64, p->r64,
-                             p->x32, p->tA, p->rev, static_cast<int*>(errp)};
+  const bat::ExactResArgs xr{descs,         groups,        static_cast<const bat::ExactTile*>(p->d_xtiles),
+                             A64,           B64,           p->r64,
+                             p->x32,        p->tA,         p->rev,
+                             static_cast<int*>(errp), p->d_row_exp, p->d_row_base,
+                             p->d_col_exp,  p->d_col_base};
+  if (sweeps > 0 && residual == NLA_RESIDUAL_SPLIT && p->nbands > 0) {
+    // Row exponents of A once: A does not change between sweeps.
+    const bat::RowExpArgs re{descs, p->d_bands, p->d_row_base, A64, p->tA, p->rev, p->d_row_exp};
+    bat::batched_row_exp_kernel<<<(unsigned)p->nbands, 256, 0, s>>>(re);
+    NLA_CHECK_LAUNCH("batched_row_exp_kernel");
+  }
+  const bat::ColExpArgs ce{descs, groups, p->d_col_base, B64, p->rev, p->d_col_exp};
   for (int k = 0; k < sweeps; ++k) {
     if (residual == NLA_RESIDUAL_SPLIT) {
       if (p->nxtiles == 0) return fail(NLA_ERR_UNSUPPORTED, "mixed batch: no residual tiles");
+      bat::batched_col_exp_kernel<<<(unsigned)p->ngroups, 256, 0, s>>>(ce);
+      NLA_CHECK_LAUNCH("batched_col_exp_kernel");
       bat::batched_exact_residual_kernel<<<(unsigned)p->nxtiles, bat::XR_THREADS, bat::XR_SMEM, s>>>(xr);
       NLA_CHECK_LAUNCH("batched_exact_residual_kernel");
     } else {
