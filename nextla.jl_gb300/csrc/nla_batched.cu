@@ -41,6 +41,7 @@
 #include <vector>
 
 #include "nla_common.cuh"
+#include "nla_split7.cuh"
 #include "nla_umma.cuh"
 
 namespace nla {
@@ -696,7 +697,11 @@ constexpr int XR_X_BYTES = XR_SL * XR_COLS * 128;  // 7 slices x 64 columns x 64
 constexpr int XR_XRP = XR_KB + 1;                  // row pitch (doubles) of the raw X block, per column
 constexpr int XR_XRAW_BYTES = XR_COLS * XR_XRP * 8;
 constexpr int XR_SMEM = XR_A_BYTES + XR_X_BYTES + XR_XRAW_BYTES + 1024 + 4096;  // + alignment, exponents, barrier
-constexpr int XR_NONFINITE = 0x7FFFFFFF;  // exponent marker of a row or column holding Inf or NaN
+constexpr int XR_NONFINITE = split7::NONFINITE;  // exponent marker of a row or column holding Inf or NaN
+using split7::exp_field;
+using split7::fixed56;
+using split7::scale_exp;
+using split7::store_chunks;
 
 struct ExactTile {
   int group;
@@ -720,16 +725,6 @@ struct ExactResArgs {
   const int* col_exp;        // scale exponent of each group column of X
   const int64_t* col_base;   // first col_exp entry of each group
 };
-
-// Biased exponent field of a double.
-__device__ __forceinline__ int exp_field(double v) { return (__double2hiint(v) >> 20) & 0x7FF; }
-
-// Scale exponent e of a row or column from the largest biased exponent of
-// its elements: |v| < 2^(e - 1) for all of them (0 when all are zero or
-// subnormal, XR_NONFINITE when one is Inf or NaN).
-__device__ __forceinline__ int scale_exp(int bmax) {
-  return bmax == 0x7FF ? XR_NONFINITE : (bmax == 0 ? 0 : bmax - 1021);
-}
 
 // Scale exponents of the rows of A's canonical lower triangles (k <= r), one
 // CTA per band of 128 rows of a system, two threads per row.  A does not
@@ -783,56 +778,6 @@ __global__ void __launch_bounds__(256) batched_col_exp_kernel(ColExpArgs a) {
     for (int k = lane; k < n; k += 32) bx = max(bx, exp_field(__ldcg(xc + (int64_t)k * sk)));
     bx = __reduce_max_sync(0xffffffffu, bx);
     if (lane == 0) a.out[a.col_base[blockIdx.x] + c] = scale_exp(bx);
-  }
-}
-
-// y = round(v 2^(56 - e)) from the bits of v (|v| < 2^(e - 1), so |y| < 2^55;
-// subnormals, Inf and NaN give 0).
-__device__ __forceinline__ long long fixed56(double v, int e) {
-  const long long b = __double_as_longlong(v);
-  const int be = (int)((b >> 52) & 0x7FF);
-  if (be == 0 || be == 0x7FF || e == XR_NONFINITE) return 0;
-  const long long m = (b & 0xFFFFFFFFFFFFFll) | (1ll << 52);
-  const int s = be - 1019 - e;  // y = m 2^s, s <= 2
-  const long long y = s >= 0 ? (m << s) : (s > -62 ? ((m + (1ll << (-s - 1))) >> (-s)) : 0ll);
-  return b < 0 ? -y : y;
-}
-
-// FP32 bit pattern of byte `sel` of w minus 128, an exact small integer:
-// 0x4B4000uu is 2^23 + 2^22 + uu as a float.
-__device__ __forceinline__ uint32_t digit_f32(uint32_t w, uint32_t sel) {
-  return __float_as_uint(__uint_as_float(__byte_perm(w, 0x4B4000u, 0x6540u + sel)) - 12583040.0f);
-}
-
-// 8 values (k = 8 j .. 8 j + 7 of a row), as fixed-point integers y, stored
-// as 7 BF16 slices of one 16-byte chunk each.  The balanced digits are the
-// bytes of y + 0x0080808080808080 minus 128 (the top digit: bits 48 and up),
-// so no carries need propagating; an integer |d| <= 256 is exact in BF16,
-// which is the upper half of its FP32 pattern.
-__device__ __forceinline__ void store_chunks(uint8_t* base, int slice_bytes, int row, int j, const long long (&y)[8]) {
-  uint32_t lo[8], hi[8];
-#pragma unroll
-  for (int u = 0; u < 8; ++u) {
-    const unsigned long long o = (unsigned long long)y[u] + 0x0080808080808080ull;
-    lo[u] = (uint32_t)o;
-    hi[u] = (uint32_t)(o >> 32);
-  }
-  const int off = row * 128 + ((j ^ (row & 7)) << 4);
-#pragma unroll
-  for (int p = 0; p < XR_SL; ++p) {
-    uint32_t f[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      if (p == 0) f[u] = __float_as_uint(__uint_as_float(0x4B400000u | (hi[u] >> 16)) - 12583040.0f);
-      else if (p <= 2) f[u] = digit_f32(hi[u], (uint32_t)(2 - p));
-      else f[u] = digit_f32(lo[u], (uint32_t)(6 - p));
-    }
-    uint4 q;
-    q.x = __byte_perm(f[0], f[1], 0x7632);
-    q.y = __byte_perm(f[2], f[3], 0x7632);
-    q.z = __byte_perm(f[4], f[5], 0x7632);
-    q.w = __byte_perm(f[6], f[7], 0x7632);
-    *reinterpret_cast<uint4*>(base + p * slice_bytes + off) = q;
   }
 }
 

@@ -179,6 +179,7 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
 constexpr int EXACT_SLICES = 7;
 int workspace_get(cudaStream_t s, size_t bytes, void** out);
 int device_status(cudaStream_t s);
+int* device_error_word();  // device address of the error word nla_device_status reads (null on failure)
 int set_wait_limit(uint64_t ns);
 uint64_t wait_limit_ns();  // the limit last set (default 2 s), for kernels that take it as a parameter
 int batch_device_error();  // the batched kernel's error word (read and cleared), or 0
@@ -197,6 +198,7 @@ struct LeafInverses {
   double* w = nullptr;
   std::vector<int64_t> k;  // leaf offsets, increasing
   bool lazy = false;
+  int* err = nullptr;  // the device error word of the bounded waits
 };
 
 // The recursion of unified_rec (src/rectrxm.jl:101-198) with a choice of

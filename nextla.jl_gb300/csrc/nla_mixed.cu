@@ -15,6 +15,8 @@
 #include <vector>
 
 #include "nla_common.cuh"
+#include "nla_split7.cuh"
+#include "nla_umma.cuh"
 
 namespace nla {
 namespace {
@@ -239,6 +241,182 @@ __global__ void __launch_bounds__(256) leaf_inverse_kernel(const __grid_constant
   }
 }
 
+// X := W X (side L, X n x m) or X W (side R, X m x n) for one leaf, W the
+// leaf's FP64 inverse (n <= 64), in one kernel: each CTA takes 128
+// right-hand sides (M of the MMA: D^T = X^T W^T), loads its block of X and
+// W, scales every right-hand side and every row of W by a power of two,
+// splits both into 7 BF16 digit slices in shared memory (nla_split7.cuh),
+// multiplies the 28 slice pairs with p + q <= 6 on the tensor cores (one
+// FP32 TMEM accumulator per weight p + q, exact: 7 x 64 x 2^14 < 2^24),
+// combines the weights exactly in int64 and writes the result over X with one
+// rounding.  Each CTA reads and writes only its own right-hand sides.
+constexpr int LP_COLS = 128;                            // right-hand sides per CTA
+constexpr int LP_THREADS = 512;                         // 16 warps: load, split, drain; one thread issues MMAs
+constexpr int LP_A_BYTES = split7::SLICES * LP_COLS * 128;   // X^T slices: 128 rows x 64 K
+constexpr int LP_B_BYTES = split7::SLICES * LEAF_INV_N * 128;  // W slices: 64 rows x 64 K
+constexpr int LP_SMEM = LP_A_BYTES + LP_B_BYTES + 1024 + 8192;
+
+struct LeafProdArgs {
+  const double* W;  // column-major, leading dimension LEAF_INV_N
+  double* X;
+  int64_t ldx;
+  int64_t m;
+  int n;
+  int side_r;
+  int* err;
+};
+
+__global__ void __launch_bounds__(LP_THREADS, 1) leaf_product_kernel(const LeafProdArgs a) {
+  using namespace split7;
+  extern __shared__ uint8_t lp_smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(lp_smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + LP_A_BYTES;
+  int* xpart = reinterpret_cast<int*>(sB + LP_B_BYTES);  // [4][128] exponent-field maxima of X
+  int* wpart = xpart + 4 * LP_COLS;                        // [8][64] of W
+  int* ex_s = wpart + 8 * LEAF_INV_N;                      // [128] scale exponents of the right-hand sides
+  int* ew_s = ex_s + LP_COLS;                              // [64] of W's rows
+  uint64_t* mma_bar = reinterpret_cast<uint64_t*>(ew_s + LEAF_INV_N);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_bar + 1);
+  __shared__ volatile int s_abort;
+
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31, n = a.n;
+  const int64_t j0 = (int64_t)blockIdx.x * LP_COLS;
+  // Element (k, j) of the right-hand sides (k < n, j < m) and (i, k) of the
+  // W operand (W itself for side L, W^T for side R).
+  auto xat = [&](int k, int64_t j) -> int64_t { return a.side_r ? j + (int64_t)k * a.ldx : k + j * a.ldx; };
+  auto wat = [&](int i, int k) -> int { return a.side_r ? k + i * LEAF_INV_N : i + k * LEAF_INV_N; };
+
+  if (t == 0) {
+    s_abort = 0;
+    umma::mbar_init(umma::smem_u32(mma_bar), 1);
+    umma::fence_barrier_init();
+  }
+  if (warp == 0) umma::tmem_alloc(umma::smem_u32(tmem_slot), 512);
+
+  // Loads: right-hand side jr = t % 128 with k = 16 (t / 128) .. + 16; row
+  // i = t % 64 of W with k = 8 (t / 64) .. + 8.
+  const int jr = t & (LP_COLS - 1), xp = t >> 7;
+  const int wi = t & (LEAF_INV_N - 1), wp = t >> 6;
+  const int64_t j = j0 + jr;
+  double vx[16], vw[8];
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int k = xp * 16 + u;
+    vx[u] = k < n && j < a.m ? a.X[xat(k, j)] : 0.0;
+  }
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int k = wp * 8 + u;
+    vw[u] = wi < n && k < n ? a.W[wat(wi, k)] : 0.0;
+  }
+  int bx = 0, bw = 0;
+#pragma unroll
+  for (int u = 0; u < 16; ++u) bx = max(bx, exp_field(vx[u]));
+#pragma unroll
+  for (int u = 0; u < 8; ++u) bw = max(bw, exp_field(vw[u]));
+  xpart[xp * LP_COLS + jr] = bx;
+  wpart[wp * LEAF_INV_N + wi] = bw;
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  if (t < LP_COLS) {
+    ex_s[t] = scale_exp(max(max(xpart[t], xpart[LP_COLS + t]), max(xpart[2 * LP_COLS + t], xpart[3 * LP_COLS + t])));
+  } else if (t < LP_COLS + LEAF_INV_N) {
+    const int i = t - LP_COLS;
+    int m8 = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) m8 = max(m8, wpart[q * LEAF_INV_N + i]);
+    ew_s[i] = scale_exp(m8);
+  }
+  __syncthreads();
+  {
+    const int ex = ex_s[jr], ew = ew_s[wi];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      long long y[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) y[u] = fixed56(vx[c * 8 + u], ex);
+      store_chunks(sA, LP_COLS * 128, jr, xp * 2 + c, y);
+    }
+    long long y[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) y[u] = fixed56(vw[u], ew);
+    store_chunks(sB, LEAF_INV_N * 128, wi, wp, y);
+  }
+  // The tensor cores read shared memory through the async proxy.
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  if (t == 0) {
+    const uint32_t idesc = umma::idesc_f16(LP_COLS, LEAF_INV_N, true);
+    const uint32_t a0 = umma::smem_u32(sA), b0 = umma::smem_u32(sB);
+#pragma unroll 1
+    for (int w = 0; w < SLICES; ++w)
+      for (int p = 0; p <= w; ++p) {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+          umma::mma_f16(tmem + (uint32_t)(w * LEAF_INV_N), umma::desc_kmajor_sw128(a0 + p * LP_COLS * 128 + kk * 32),
+                        umma::desc_kmajor_sw128(b0 + (w - p) * LEAF_INV_N * 128 + kk * 32), idesc,
+                        (p > 0 || kk > 0) ? 1u : 0u);
+      }
+    umma::mma_commit(umma::smem_u32(mma_bar));
+  }
+  __syncwarp();
+  bool ok = __all_sync(0xffffffffu, umma::mbar_wait(umma::smem_u32(mma_bar), 0u, &s_abort, a.err, 41));
+  umma::fence_after_sync();
+  if (!ok && t == 0) {
+    // Let the MMAs finish (a drain with the default limit) before the tensor
+    // memory is released.
+    umma::mbar_wait(umma::smem_u32(mma_bar), 0u, &s_abort, a.err, 42, false);
+  }
+  if (ok) {
+    // Drain: right-hand side q * 32 + lane (the warp's TMEM lane quarter),
+    // output rows h * 16 .. + 16.  One block of K: S = H 2^18 + round(L 2^-6)
+    // (H = sum_{w<4} T_w 2^(24 - 8 w), L = sum_{4<=w<7} T_w 2^(48 - 8 w)),
+    // and the product is S 2^(e_x + e_w - 58).
+    const int q = warp & 3, h = warp >> 2;
+    const int jd = q * 32 + lane;
+    const int64_t jj = j0 + jd;
+    const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 16);
+    long long S[16], L[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) S[c] = L[c] = 0;
+#pragma unroll
+    for (int w = 0; w < SLICES; ++w) {
+      uint32_t rr[16];
+      umma::tmem_ld16(tq + (uint32_t)(w * LEAF_INV_N), rr);
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const long long v = (long long)__float2int_rn(__uint_as_float(rr[c]));
+        if (w < 4) S[c] += v << (24 - 8 * w);
+        else L[c] += v << (48 - 8 * w);
+      }
+    }
+    const int ex = ex_s[jd];
+    if (jj < a.m) {
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int i = h * 16 + c;
+        if (i < n) {
+          const int ew = ew_s[i];
+          const long long tot = (S[c] << 18) + ((L[c] + (1ll << 5)) >> 6);
+          a.X[xat(i, jj)] = ex == NONFINITE || ew == NONFINITE ? __longlong_as_double(0x7ff8000000000000ll)
+                                                               : ldexp((double)tot, ex + ew - 58);
+        }
+      }
+    }
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    umma::fence_after_sync();
+    umma::tmem_dealloc(tmem, 512);
+  }
+}
+
 std::mutex g_inv_mu;
 std::unordered_map<uint64_t, Buf> g_inv_bufs;
 
@@ -320,6 +498,8 @@ int leaf_inverses_upfront(const RecPlan& c, const Mat& A, int64_t n, LeafInverse
   out->a_base = static_cast<const double*>(A.p);
   out->lda = A.ld;
   out->lazy = false;
+  out->err = device_error_word();
+  if (!out->err) return fail(NLA_ERR_UNSUPPORTED, "leaf inverses: no device error word");
   out->k.clear();
   std::vector<int> ns;
   collect_leaves(0, n, c.threshold, &out->k, &ns);
@@ -331,6 +511,8 @@ int leaf_inverses_upfront(const RecPlan& c, const Mat& A, int64_t n, LeafInverse
 int leaf_inverses_lazy(const RecPlan& c, LeafInverses* out) {
   out->lazy = true;
   out->k.clear();
+  out->err = device_error_word();
+  if (!out->err) return fail(NLA_ERR_UNSUPPORTED, "leaf inverses: no device error word");
   return inverse_buffer(c.s, LEAF_INV_N * LEAF_INV_N * sizeof(double), &out->w);
 }
 
@@ -348,11 +530,22 @@ int leaf_inverse_apply(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) 
     if (it == L.k.end() || *it != k) return fail(NLA_ERR_ARG, "leaf inverses: no inverse for this block");
     slot = it - L.k.begin();
   }
-  const Mat W{L.w + slot * LEAF_INV_N * LEAF_INV_N, LEAF_INV_N, 0};
-  // X := inv(T) X  (side L)  or  X inv(T)  (side R).
-  if (c.side == 'L')
-    return launch_sliced_gemm(n, c.m, n, 1.0, W, B, B, NLA_F64, NLA_F64, EXACT_SLICES, true, nullptr, 0, c.s, true);
-  return launch_sliced_gemm(c.m, n, n, 1.0, B, W, B, NLA_F64, NLA_F64, EXACT_SLICES, true, nullptr, 0, c.s, true);
+  // X := inv(T) X  (side L)  or  X inv(T)  (side R), one kernel.
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [] {
+    attr = cudaFuncSetAttribute(leaf_product_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, LP_SMEM);
+  });
+  if (attr != cudaSuccess) return cuda_status(attr, "cudaFuncSetAttribute(leaf_product_kernel)");
+  if (B.t) return fail(NLA_ERR_UNSUPPORTED, "leaf product: transposed B view");
+  LeafProdArgs g{L.w + slot * LEAF_INV_N * LEAF_INV_N, static_cast<double*>(B.p), B.ld, c.m, (int)n,
+                 c.side == 'R' ? 1 : 0, L.err};
+  const int64_t grid = (c.m + LP_COLS - 1) / LP_COLS;
+  if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "leaf product: too many right-hand sides");
+  TraceScope trace(NLA_K_LEAF_SOLVE, c.s, 2.0 * (double)n * n * (double)c.m, 16.0 * (double)n * (double)c.m);
+  leaf_product_kernel<<<(unsigned)grid, LP_THREADS, LP_SMEM, c.s>>>(g);
+  NLA_CHECK_LAUNCH("leaf_product_kernel");
+  return NLA_OK;
 }
 
 // Stage the strict triangle of op(A) as the row operand of the residual

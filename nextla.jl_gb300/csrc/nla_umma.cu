@@ -1750,6 +1750,11 @@ int set_wait_limit(uint64_t ns) {
 uint64_t wait_limit_ns() { return g_wait_limit_host.load(); }
 
 // Reads and clears the device error word after synchronising the stream.
+int* device_error_word() {
+  void* p = nullptr;
+  return cudaGetSymbolAddress(&p, g_device_error) == cudaSuccess ? static_cast<int*>(p) : nullptr;
+}
+
 int device_status(cudaStream_t s) {
   cudaError_t e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_status(e, "stream synchronize");
