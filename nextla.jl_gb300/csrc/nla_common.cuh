@@ -186,18 +186,17 @@ int batch_device_error();  // the batched kernel's error word (read and cleared)
 
 // Inverses of the diagonal blocks (leaves) of a mixed solve's recursion,
 // W = inv(T) for each leaf block T (lower or upper as the recursion sees it),
-// one 64 x 64 slot each in w.  A leaf is then X := W X on the tensor cores
-// with the exact slice products.  Upfront: every leaf's inverse is
-// formed before the recursion, slot j for the j-th leaf offset in k.  Lazy
-// (the host-buffer path, where A arrives block by block): each leaf inverts
-// its block into slot 0 just before its product.
+// one 64 x 64 slot each in w, slot j for the j-th leaf offset in k (relative
+// to a_base).  A leaf is then X := W X on the tensor cores with the exact
+// slice products.  The device path inverts every leaf before the recursion;
+// the host-buffer path, where A arrives block by block, inverts the leaves of
+// each block when the block arrives.
 constexpr int LEAF_INV_N = 64;
 struct LeafInverses {
-  const double* a_base = nullptr;  // A as the recursion indexes it
+  const double* a_base = nullptr;  // A (or the block) as the recursion indexes it
   int64_t lda = 0;
   double* w = nullptr;
   std::vector<int64_t> k;  // leaf offsets, increasing
-  bool lazy = false;
   int* err = nullptr;  // the device error word of the bounded waits
 };
 
@@ -219,10 +218,9 @@ struct RecPlan {
 int recurse(const RecPlan& c, const Mat& A, int64_t n, const Mat& B);
 // Mixed exact solves: whether the leaves go through inverses (a 7-slice solve
 // with leaves of at most LEAF_INV_N rows, unless NLA_MIXED_INV_LEAF=0), the
-// upfront and lazy set-ups, and the leaf itself.
+// inversion of every leaf of the n x n block A (one launch), and the leaf.
 bool leaf_inverses_wanted(const RecPlan& c);
 int leaf_inverses_upfront(const RecPlan& c, const Mat& A, int64_t n, LeafInverses* out);
-int leaf_inverses_lazy(const RecPlan& c, LeafInverses* out);
 int leaf_inverse_apply(const RecPlan& c, const Mat& A, int64_t n, const Mat& B);
 // Launches inside the scope are traced under kernel class kclass (the leaf
 // products of a mixed solve run the update kernels but are leaf work).

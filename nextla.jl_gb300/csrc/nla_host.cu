@@ -197,6 +197,9 @@ int staged(HostRun& h, int64_t k, int64_t n, int levels, bool emit) {
   if (levels == 0 || n <= c.threshold) {
     NLA_TRY(copy_a(h, k, k, n, n));
     NLA_TRY(acquire_b(h, k, n));
+    // The block's leaves through their inverses: all of them inverted in one
+    // launch once the block is on the device.
+    if (c.inv) NLA_TRY(leaf_inverses_upfront(c, a_view(h, k, k), n, const_cast<LeafInverses*>(c.inv)));
     NLA_TRY(recurse(c, a_view(h, k, k), n, b_view(h, k)));
     return emit ? release_b(h, k, n) : NLA_OK;
   }
@@ -344,14 +347,11 @@ int nla_trxm_mixed_host(char side, char uplo, char trans, double alpha, char fun
   h.Bd = reinterpret_cast<char*>(B_dev);
   h.ldbd = ldb_dev;
   const bool whole = func == 'S' && o.sweeps > 0;
-  // The staged walk brings A in block by block, so each leaf inverts its own
-  // block just before its product (the whole-array form inverts them all
-  // inside trxm_mixed_impl).
-  LeafInverses lazy;
-  if (!whole && leaf_inverses_wanted(h.c)) {
-    NLA_TRY(leaf_inverses_lazy(h.c, &lazy));
-    h.c.inv = &lazy;
-  }
+  // The staged walk brings A in block by block, so the leaves of each block
+  // are inverted when the block arrives (the whole-array form inverts them
+  // all inside trxm_mixed_impl).
+  LeafInverses blockinv;
+  if (!whole && leaf_inverses_wanted(h.c)) h.c.inv = &blockinv;
   return host_run(h, n, host_levels(levels), whole, [&] {
     return trxm_mixed_impl(side, uplo, trans, alpha, func, n, m, A_dev, lda_dev, B_dev, ldb_dev, &o, s);
   });

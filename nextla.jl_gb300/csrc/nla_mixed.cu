@@ -497,7 +497,6 @@ bool leaf_inverses_wanted(const RecPlan& c) {
 int leaf_inverses_upfront(const RecPlan& c, const Mat& A, int64_t n, LeafInverses* out) {
   out->a_base = static_cast<const double*>(A.p);
   out->lda = A.ld;
-  out->lazy = false;
   out->err = device_error_word();
   if (!out->err) return fail(NLA_ERR_UNSUPPORTED, "leaf inverses: no device error word");
   out->k.clear();
@@ -508,28 +507,14 @@ int leaf_inverses_upfront(const RecPlan& c, const Mat& A, int64_t n, LeafInverse
   return launch_inverses(c, out->a_base, A.ld, A.t, out->k, ns, out->w, 0);
 }
 
-int leaf_inverses_lazy(const RecPlan& c, LeafInverses* out) {
-  out->lazy = true;
-  out->k.clear();
-  out->err = device_error_word();
-  if (!out->err) return fail(NLA_ERR_UNSUPPORTED, "leaf inverses: no device error word");
-  return inverse_buffer(c.s, LEAF_INV_N * LEAF_INV_N * sizeof(double), &out->w);
-}
-
 int leaf_inverse_apply(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
   if (n <= 0 || c.m <= 0) return NLA_OK;
   const LeafInverses& L = *c.inv;
-  TraceClassScope cls(NLA_K_LEAF_SOLVE);
-  int64_t slot = 0;
-  if (L.lazy) {
-    NLA_TRY(launch_inverses(c, static_cast<const double*>(A.p), A.ld, A.t, std::vector<int64_t>{0},
-                            std::vector<int>{(int)n}, L.w, 0));
-  } else {
-    const int64_t k = (static_cast<const double*>(A.p) - L.a_base) / (L.lda + 1);
-    const auto it = std::lower_bound(L.k.begin(), L.k.end(), k);
-    if (it == L.k.end() || *it != k) return fail(NLA_ERR_ARG, "leaf inverses: no inverse for this block");
-    slot = it - L.k.begin();
-  }
+  const int64_t k = (static_cast<const double*>(A.p) - L.a_base) / (L.lda + 1);
+  const auto it = std::lower_bound(L.k.begin(), L.k.end(), k);
+  if (L.a_base == nullptr || it == L.k.end() || *it != k)
+    return fail(NLA_ERR_ARG, "leaf inverses: no inverse for this block");
+  const int64_t slot = it - L.k.begin();
   // X := inv(T) X  (side L)  or  X inv(T)  (side R), one kernel.
   static std::once_flag once;
   static cudaError_t attr = cudaSuccess;
