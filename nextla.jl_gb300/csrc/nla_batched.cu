@@ -981,7 +981,7 @@ __global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(E
           const int eb = eb_s[col];
           const float res = ea == XR_NONFINITE || eb == XR_NONFINITE
                                 ? __int_as_float(0x7FC00000)
-                                : (float)(rv[j] - ldexp((double)acc[j], ea + eb - 40 - sa_bits));
+                                : (float)(rv[j] - split7::scaled_i64_to_f64(acc[j], ea + eb - 40 - sa_bits));
           a.D32[rbase + (int64_t)j * d.ldb] = res;
         }
       }

@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(LP_THREADS, 1) leaf_product_kernel(const LeafP
           const int ew = ew_s[i];
           const long long tot = (S[c] << 18) + ((L[c] + (1ll << 5)) >> 6);
           a.X[xat(i, jj)] = ex == NONFINITE || ew == NONFINITE ? __longlong_as_double(0x7ff8000000000000ll)
-                                                               : ldexp((double)tot, ex + ew - 58);
+                                                               : scaled_i64_to_f64(tot, ex + ew - 58);
         }
       }
     }

@@ -78,5 +78,32 @@ __device__ __forceinline__ void store_chunks(uint8_t* base, int slice_bytes, int
   }
 }
 
+// (double)v * 2^s rounded to nearest even, with integer operations only (the
+// FP64 pipe runs 2 operations per clock per SM on GB300, and a conversion plus
+// ldexp per output element made it the busiest pipe of the kernels that write
+// these products); results outside the normal range go through ldexp.
+__device__ __forceinline__ double scaled_i64_to_f64(long long v, int s) {
+  if (v == 0) return 0.0;
+  const unsigned long long sign = v < 0 ? (1ull << 63) : 0ull;
+  const unsigned long long u = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  int msb = 63 - __clzll((long long)u);
+  unsigned long long m;
+  if (msb > 52) {
+    const int sh = msb - 52;
+    const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    m = u >> sh;
+    if (rem > half || (rem == half && (m & 1ull))) ++m;
+    if (m >> 53) {
+      m >>= 1;
+      ++msb;
+    }
+  } else {
+    m = u << (52 - msb);
+  }
+  const int biased = msb + s + 1023;
+  if (biased <= 0 || biased >= 2047) return ldexp((double)v, s);
+  return __longlong_as_double((long long)(sign | ((unsigned long long)biased << 52) | (m & 0xFFFFFFFFFFFFFull)));
+}
+
 }  // namespace split7
 }  // namespace nla
