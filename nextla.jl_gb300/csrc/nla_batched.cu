@@ -96,6 +96,8 @@ struct Args {
   int tA, rev;
   double alpha;
   uint64_t limit_ns;
+  float alpha_f;      // alpha as a float, and whether that is exact: the float
+  int alpha_f_exact;  // product is then the double product rounded once
 };
 
 __device__ int g_batch_error = 0;
@@ -150,6 +152,15 @@ __device__ __forceinline__ float to_c(__half v) { return __half2float(v); }
 template <typename T> __device__ __forceinline__ typename Elem<T>::compute scaled(T b, double alpha);
 template <> __device__ __forceinline__ double scaled<double>(double b, double alpha) { return alpha * b; }
 template <> __device__ __forceinline__ float scaled<float>(float b, double alpha) { return (float)(alpha * (double)b); }
+// The same for a node's first touch of B, without FP64 work when alpha is a
+// float (24 x 24 bits are exact in a double, so one float rounding gives the
+// same value).
+template <typename T> __device__ __forceinline__ typename Elem<T>::compute scaled_node(T b, const Args& a) {
+  return scaled<T>(b, a.alpha);
+}
+template <> __device__ __forceinline__ float scaled_node<float>(float b, const Args& a) {
+  return a.alpha_f_exact ? b * a.alpha_f : scaled<float>(b, a.alpha);
+}
 template <> __device__ __forceinline__ float scaled<__half>(__half b, double alpha) {
   return __half2float(__double2half(alpha * (double)__half2float(b)));
 }
@@ -358,12 +369,19 @@ __device__ bool run_update(const Args& a, const Node& nd, const Group& g, const 
     const int c = cb + u * CSTEP;
     bv[u] = r < rows && c < ncols ? ldcg(Bt + (int64_t)c * d.ldb) : T(0);
   }
+  // A node-uniform branch: with a select the compiler formed alpha * b (FP64
+  // work, slow on this part) for every node.
+  if (first) {
 #pragma unroll
-  for (int u = 0; u < PER; ++u) {
-    const int c = cb + u * CSTEP;
-    if (r < rows && c < ncols) {
-      const Tc base = first ? scaled<T>(bv[u], a.alpha) : to_c(bv[u]);
-      Elem<T>::store(Bt + (int64_t)c * d.ldb, base - Ts[c * TP + r]);
+    for (int u = 0; u < PER; ++u) {
+      const int c = cb + u * CSTEP;
+      if (r < rows && c < ncols) Elem<T>::store(Bt + (int64_t)c * d.ldb, scaled_node<T>(bv[u], a) - Ts[c * TP + r]);
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int c = cb + u * CSTEP;
+      if (r < rows && c < ncols) Elem<T>::store(Bt + (int64_t)c * d.ldb, to_c(bv[u]) - Ts[c * TP + r]);
     }
   }
   return true;
@@ -398,7 +416,8 @@ __device__ bool run_leaf(const Args& a, const Node& nd, const Group& g, const nl
   const int64_t dr = sgn * (a.tA ? d.lda : 1), dk = sgn * (a.tA ? 1 : d.lda);
   const T* A0 = A + a_at(d, a.tA, a.rev, nd.r0, nd.r0);
   constexpr int A_PER = MAX_ROWS * MAX_ROWS / NT, X_PER = MAX_ROWS * W / NT;
-  Tc va[A_PER], vx[X_PER];
+  Tc va[A_PER];
+  T vx[X_PER];
 #pragma unroll
   for (int u = 0; u < A_PER; ++u) {
     const int idx = t + u * NT;
@@ -411,12 +430,7 @@ __device__ bool run_leaf(const Args& a, const Node& nd, const Group& g, const nl
 #pragma unroll
   for (int u = 0; u < X_PER; ++u) {
     const int c = (t + u * NT) / MAX_ROWS;
-    Tc x = Tc(0);
-    if (xr < rows && c < ncols) {
-      const T b = ldcg(X0 + xr * sgn + (int64_t)c * d.ldb);
-      x = first ? scaled<T>(b, a.alpha) : to_c(b);
-    }
-    vx[u] = x;
+    vx[u] = xr < rows && c < ncols ? ldcg(X0 + xr * sgn + (int64_t)c * d.ldb) : T(0);
   }
 #pragma unroll
   for (int u = 0; u < A_PER; ++u) {
@@ -425,10 +439,18 @@ __device__ bool run_leaf(const Args& a, const Node& nd, const Group& g, const nl
     if (r < rows && k < r) Ls[r * LP + k] = va[u];
     else if (r < rows && k == r) inv[r] = Tc(1) / va[u];
   }
+  if (first) {  // node-uniform (see the update's epilogue)
 #pragma unroll
-  for (int u = 0; u < X_PER; ++u) {
-    const int c = (t + u * NT) / MAX_ROWS;
-    if (xr < rows) Xs[xr * XP + c] = vx[u];
+    for (int u = 0; u < X_PER; ++u) {
+      const int c = (t + u * NT) / MAX_ROWS;
+      if (xr < rows) Xs[xr * XP + c] = scaled_node<T>(vx[u], a);
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < X_PER; ++u) {
+      const int c = (t + u * NT) / MAX_ROWS;
+      if (xr < rows) Xs[xr * XP + c] = to_c(vx[u]);
+    }
   }
   __syncthreads();
 
@@ -1267,7 +1289,7 @@ int launch_nodes(nla_batch_plan p, double alpha, const void* A, void* B, cudaStr
   int* c = p->d_counters;  // next, abort, solved[ngroups], applied[nleaves]
   bat::Args a{static_cast<const nla_batch_desc*>(p->d_descs), static_cast<const Group*>(p->d_groups),
               static_cast<const Node*>(p->d_nodes), p->nnodes, c, c + 2, c + 2 + p->ngroups, c + 1, nullptr, A, B,
-              p->tA, p->rev, alpha, wait_limit_ns()};
+              p->tA, p->rev, alpha, wait_limit_ns(), (float)alpha, (double)(float)alpha == alpha ? 1 : 0};
   void* errp = nullptr;
   cudaError_t e = cudaGetSymbolAddress(&errp, bat::g_batch_error);
   if (e != cudaSuccess) return cuda_status(e, "batch error word");
