@@ -458,18 +458,22 @@ __device__ bool run_leaf(const Args& a, const Node& nd, const Group& g, const nl
   for (int p0 = 0; p0 < rows; p0 += PANEL) {
     const int pw = min(PANEL, rows - p0);
     // The panel's triangle: one right-hand side per thread (warps whose
-    // right-hand sides all lie past the group's skip it).
+    // right-hand sides all lie past the group's skip it), right-looking: as
+    // soon as x_j is known it is subtracted from every later row.  Each row
+    // sees the same FMAs in the same order (j increasing) as a row-by-row
+    // dot product, so the bits are the same, but the dependent chain is one
+    // FMA and one multiply per row instead of a whole dot product.
     if (t < W && (t & ~31) < ncols) {
-      Tc x[PANEL];
+      Tc y[PANEL];
 #pragma unroll
-      for (int i = 0; i < PANEL; ++i) {
-        if (i < pw) {
-          Tc y = Xs[(p0 + i) * XP + t];
+      for (int i = 0; i < PANEL; ++i) y[i] = i < pw ? Xs[(p0 + i) * XP + t] : Tc(0);
 #pragma unroll
-          for (int j = 0; j < i; ++j) y = fma(-Ls[(p0 + i) * LP + p0 + j], x[j], y);
-          y *= inv[p0 + i];
-          x[i] = y;
-          Xs[(p0 + i) * XP + t] = y;
+      for (int j = 0; j < PANEL; ++j) {
+        if (j < pw) {
+          const Tc xj = y[j] * inv[p0 + j];
+          Xs[(p0 + j) * XP + t] = xj;
+#pragma unroll
+          for (int r = j + 1; r < PANEL; ++r) y[r] = fma(-Ls[(p0 + r) * LP + p0 + j], xj, y[r]);
         }
       }
     }
