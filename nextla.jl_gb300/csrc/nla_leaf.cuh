@@ -286,9 +286,9 @@ __device__ __forceinline__ void trailing_update_wide(const Tc* __restrict__ slab
 
 // Canonical lower-left solve for wide column blocks (CW in {16, 32, 64, 128}):
 // the same panels as solve_block, but each panel's 32 x 32 triangle is solved
-// with one right-hand side per thread (threads < CW), as a fully unrolled
-// dot product against the panel's already-solved values in registers, so
-// every lane does useful work and no value has to cross lanes.
+// with one right-hand side per thread (threads < CW), fully unrolled over the
+// panel's values in registers, so every lane does useful work and no value
+// has to cross lanes.
 template <typename T, int CW>
 __device__ __forceinline__ void solve_block_wide(const LeafArgs& g, int64_t c0, int ncols, unsigned char* smem_raw,
                                                  typename Elem<T>::compute alpha) {
@@ -318,16 +318,20 @@ __device__ __forceinline__ void solve_block_wide(const LeafArgs& g, int64_t c0, 
     const int rot = std::is_same<Tc, double>::value ? 32 * (int)((p0 / PANEL + blockIdx.x) % (LEAF_THREADS / 32)) : 0;
     const int tt = (t - rot + LEAF_THREADS) % LEAF_THREADS;
     if (tt < CW) {
-      Tc x[PANEL];
+      // Right-looking: x_j is subtracted from every later row as soon as it
+      // is known.  Each row sees the same FMAs in the same order (j
+      // increasing) as a row-by-row dot product, so the bits are the same,
+      // and the dependent chain is one FMA and one multiply per row.
+      Tc y[PANEL];
 #pragma unroll
-      for (int r = 0; r < PANEL; ++r) {
-        if (r < pw) {
-          Tc y = X[(p0 + r) * CW + tt];
+      for (int r = 0; r < PANEL; ++r) y[r] = r < pw ? X[(p0 + r) * CW + tt] : Tc(0);
 #pragma unroll
-          for (int j = 0; j < r; ++j) y = fma(-diag[r * SLAB_PAD + j], x[j], y);
-          y *= inv_d[p0 + r];
-          x[r] = y;
-          X[(p0 + r) * CW + tt] = y;
+      for (int j = 0; j < PANEL; ++j) {
+        if (j < pw) {
+          const Tc xj = y[j] * inv_d[p0 + j];
+          X[(p0 + j) * CW + tt] = xj;
+#pragma unroll
+          for (int r = j + 1; r < PANEL; ++r) y[r] = fma(-diag[r * SLAB_PAD + j], xj, y[r]);
         }
       }
     }
