@@ -1029,6 +1029,8 @@ __global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(E
 struct nla_batch_plan_s {
   int dtype;
   int tA, rev;
+  char uplo0, trans0;  // the flags the plan was created with
+  nla_batch_plan p32;  // mixed batches: a Float32 plan of the same systems (built on first use)
   int64_t count;
   std::vector<nla_batch_desc> h_descs;
   std::vector<nla::bat::Group> h_groups;
@@ -1330,6 +1332,9 @@ int plan_create(nla_batch_plan* out, int dtype, char uplo, char trans, int64_t c
   }
   nla_batch_plan p = new nla_batch_plan_s();
   p->dtype = dtype;
+  p->uplo0 = uplo;
+  p->trans0 = trans;
+  p->p32 = nullptr;
   p->tA = (trans == 'T' || trans == 'C') ? 1 : 0;
   const char up = p->tA ? (uplo == 'L' ? 'U' : 'L') : uplo;
   p->rev = up == 'U';
@@ -1636,8 +1641,16 @@ int nla_batch_solve_mixed_ex(nla_batch_plan p, double alpha, const void* A_pool,
       return cuda_status(e, "mixed batch buffers");
     }
   }
+  // The Float32 solves run on a Float32 plan of the same systems: its groups
+  // take up to 128 right-hand sides (a Float64 plan's at most 64), so it has
+  // fewer, wider nodes; its pools share the Float64 pools' offsets.
+  if (!p->p32) {
+    nla_batch_tuning t32;
+    default_tuning(NLA_F32, &t32);
+    NLA_TRY(plan_create(&p->p32, NLA_F32, p->uplo0, p->trans0, p->count, p->h_descs.data(), t32));
+  }
   int per_sm = 0;
-  NLA_TRY(node_kernel_setup<float>(p->smem, &per_sm));
+  NLA_TRY(node_kernel_setup<float>(p->p32->smem, &per_sm));
   const auto* descs = static_cast<const nla_batch_desc*>(p->d_descs);
   const auto* groups = static_cast<const Group*>(p->d_groups);
   double* B64 = static_cast<double*>(B_pool);
@@ -1646,12 +1659,10 @@ int nla_batch_solve_mixed_ex(nla_batch_plan p, double alpha, const void* A_pool,
   bat::MapArgs m{descs, groups, A64, p->a32, B64, p->r64, p->x32, alpha, bat::MAP_INIT};
   bat::batched_map_kernel<<<p->ngroups, 256, 0, s>>>(m);
   NLA_CHECK_LAUNCH("batched_map_kernel");
-  // The Float32 solves run on the same node queue (the plan's Float64 layout
-  // of nodes and shared memory covers the Float32 kernel).
   auto solve32 = [&]() -> int {
-    cudaError_t e = cudaMemsetAsync(p->d_counters, 0, p->counter_bytes, s);
+    cudaError_t e = cudaMemsetAsync(p->p32->d_counters, 0, p->p32->counter_bytes, s);
     if (e != cudaSuccess) return cuda_status(e, "batch counter reset");
-    return launch_nodes<float>(p, 1.0, p->a32, p->x32, s);
+    return launch_nodes<float>(p->p32, 1.0, p->a32, p->x32, s);
   };
   NLA_TRY(solve32());
   m.op = bat::MAP_SET;
@@ -1698,6 +1709,7 @@ int nla_batch_solve_mixed_ex(nla_batch_plan p, double alpha, const void* A_pool,
 int nla_batch_plan_destroy(nla_batch_plan p) {
   clear_error();
   if (!p) return NLA_OK;
+  if (p->p32) nla_batch_plan_destroy(p->p32);
   cudaFree(p->a32);
   cudaFree(p->x32);
   cudaFree(p->r64);
