@@ -353,12 +353,8 @@ __device__ bool run_update(const Args& a, const Node& nd, const Group& g, const 
   // may alias a later load of it, which would otherwise wait for it).
   constexpr int TP = MAX_ROWS + 4;
   static_assert(RT == 4 && TP * W <= KC * (AP + XP) + MAX_ROWS * (MAX_ROWS + LEAF_PAD), "tile fits the node's smem");
-  Tc* Ts = As;
-  __syncthreads();  // the last chunk is no longer read
-#pragma unroll
-  for (int c = 0; c < CT; ++c)
-    sts4(Ts + (tc * CT + c) * TP + RT * tr, acc[0][c], acc[1][c], acc[2][c], acc[3][c]);
-  __syncthreads();
+  // The tile's loads of B are issued first, so that their latency passes
+  // while the products go to shared memory.
   constexpr int PER = MAX_ROWS * W / NT, CSTEP = NT / MAX_ROWS;
   const int r = t % MAX_ROWS, cb = t / MAX_ROWS;
   T* const Bt = static_cast<T*>(a.B) + b_at(d, a.rev, nd.r0, g.c0) + sgn * r;
@@ -369,6 +365,12 @@ __device__ bool run_update(const Args& a, const Node& nd, const Group& g, const 
     const int c = cb + u * CSTEP;
     bv[u] = r < rows && c < ncols ? ldcg(Bt + (int64_t)c * d.ldb) : T(0);
   }
+  Tc* Ts = As;
+  __syncthreads();  // the last chunk is no longer read
+#pragma unroll
+  for (int c = 0; c < CT; ++c)
+    sts4(Ts + (tc * CT + c) * TP + RT * tr, acc[0][c], acc[1][c], acc[2][c], acc[3][c]);
+  __syncthreads();
   // A node-uniform branch: with a select the compiler formed alpha * b (FP64
   // work, slow on this part) for every node.
   if (first) {
