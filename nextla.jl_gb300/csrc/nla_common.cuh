@@ -155,8 +155,10 @@ struct Staged {
   int tri;  // 0 full, 1 k <= row, 2 k >= row, 3 k < row, 4 k > row
 };
 size_t staged_bytes(int64_t rows, int64_t K, int S);
+// want_nrm: also the row-magnitude sums the exact kernel reads for its A
+// operand (nrm is null in *out otherwise).
 int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bool bf16, int tri, void* buf,
-                  Staged* out, cudaStream_t s);
+                  Staged* out, cudaStream_t s, bool want_nrm = true);
 // The diagonal term and final rounding of a residual computed by the exact
 // update: C := C - P - d_i * X(pos), with d_i = d[i * dstride] (i the row of
 // the staged A operand) and X at the position of C's element.

@@ -549,11 +549,11 @@ int split_residual(const Mat& Am, const Staged& As, char side, int64_t n, int64_
   // diagonal term from R (= alpha*B on entry) and rounds once.
   const ResidualTerm term{static_cast<const double*>(Xm.p), Xm.ld, static_cast<const double*>(Am.p), Am.ld + 1};
   if (side == 'L') {  // op(A) (n x n) times X (n x m): B-operand rows are X's columns
-    NLA_TRY(stage_operand(transposed(Xm), m, n, NLA_F64, EXACT_SLICES, true, 0, xbuf, Xs, s));
+    NLA_TRY(stage_operand(transposed(Xm), m, n, NLA_F64, EXACT_SLICES, true, 0, xbuf, Xs, s, false));
     return launch_exact_gemm(As, *Xs, -1.0, Rm, false, s, &term);
   }
   // (X op(A))^T = op(A)^T X^T: B-operand rows are X's rows; written transposed
-  NLA_TRY(stage_operand(Xm, m, n, NLA_F64, EXACT_SLICES, true, 0, xbuf, Xs, s));
+  NLA_TRY(stage_operand(Xm, m, n, NLA_F64, EXACT_SLICES, true, 0, xbuf, Xs, s, false));
   return launch_exact_gemm(As, *Xs, -1.0, Rm, true, s, &term);
 }
 

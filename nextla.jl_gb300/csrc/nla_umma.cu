@@ -1086,7 +1086,7 @@ __device__ __forceinline__ void store_tile(double (*tile)[65], int t, const doub
 template <typename Sl, int NS>
 __device__ __forceinline__ void split_tile(const double (*tile)[65], int64_t i0, int64_t k0, int64_t rows,
                                            const int* ex_rows, Sl* __restrict__ out, int64_t cols_pad,
-                                           float (&mag)[4]) {
+                                           float (&mag)[4], bool with_mag) {
   constexpr int BETA = std::is_same<Sl, __nv_bfloat16>::value ? 8 : 11;
   constexpr int NSL = NS == 0 ? 1 : NS;
   // One row per warp and pass (idx >> 5 is warp-uniform), two K values per lane.
@@ -1127,9 +1127,10 @@ __device__ __forceinline__ void split_tile(const double (*tile)[65], int64_t i0,
         const float f1 = __int_as_float(0x4B400000 + d1) - 12582912.0f;
         o[sl * (128 * cols_pad / 2)] = pack_slices<Sl>(f0, f1);
         // 2^(-beta (sl + 1)) built from its exponent bits (exact).
-        m += (fabsf(f0) + fabsf(f1)) * __int_as_float((127 - BETA * (sl + 1)) << 23);
+        if (with_mag) m += (fabsf(f0) + fabsf(f1)) * __int_as_float((127 - BETA * (sl + 1)) << 23);
       }
-      for (int off = 16; off > 0; off >>= 1) m += __shfl_xor_sync(0xffffffffu, m, off);
+      if (with_mag)  // uniform over the launch
+        for (int off = 16; off > 0; off >>= 1) m += __shfl_xor_sync(0xffffffffu, m, off);
       mag[pass] = m;
     }
   }
@@ -1155,7 +1156,7 @@ __global__ void __launch_bounds__(256) split_kernel(const T* __restrict__ X, int
   store_tile(tile, t, v);
   __syncthreads();
   float mag[4];
-  split_tile<Sl, NS>(tile, i0, k0, rows, e ? e + i0 : nullptr, out, cols_pad, mag);
+  split_tile<Sl, NS>(tile, i0, k0, rows, e ? e + i0 : nullptr, out, cols_pad, mag, nrm != nullptr);
   if (NS != 0 && nrm && (threadIdx.x & 31) == 0) {
 #pragma unroll
     for (int pass = 0; pass < 4; ++pass) {
@@ -1248,11 +1249,11 @@ __global__ void __launch_bounds__(256, 3) stage_pair_kernel(const StageJob a, co
     store_tile(tile[kt & 1], j.t, v);
     __syncthreads();
     float mag[4];
-    split_tile<Sl, NS>(tile[kt & 1], i0, kt * 64, j.rows, sexp, out, j.cols_pad, mag);
+    split_tile<Sl, NS>(tile[kt & 1], i0, kt * 64, j.rows, sexp, out, j.cols_pad, mag, j.nrm != nullptr);
 #pragma unroll
     for (int pass = 0; pass < 4; ++pass) acc[pass] += mag[pass];
   }
-  if (lane == 0) {
+  if (lane == 0 && j.nrm) {
 #pragma unroll
     for (int pass = 0; pass < 4; ++pass) j.nrm[i0 + warp + 8 * pass] = i0 + warp + 8 * pass < j.rows ? acc[pass] : 0.0f;
   }
@@ -1444,7 +1445,7 @@ void staged_layout(void* buf, int64_t rows, int64_t K, int S, bool bf16, bool co
 }
 
 int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bool bf16, int tri, void* buf,
-                  Staged* out, cudaStream_t s) {
+                  Staged* out, cudaStream_t s, bool want_nrm) {
   const bool copy = in_dtype == NLA_F16;
   const int beta = bf16 ? 8 : 11;
   if (copy) S = 1;
@@ -1461,7 +1462,10 @@ int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bo
     return NLA_OK;
   }
   cudaMemsetAsync(out->e, 0x80, (size_t)Rp * sizeof(int), s);
-  cudaMemsetAsync(out->nrm, 0, (size_t)Rp * sizeof(float), s);
+  // The row-magnitude sums bound the exact kernel's fixed point for its A
+  // operand; nothing reads them for a B operand or in the fast mode.
+  if (want_nrm) cudaMemsetAsync(out->nrm, 0, (size_t)Rp * sizeof(float), s);
+  else out->nrm = nullptr;
   const dim3 ge((unsigned)((rows + 63) / 64), (unsigned)((K + 63) / 64));
   row_exp_kernel<double><<<ge, 256, 0, s>>>((const double*)X.p, X.ld, X.t, rows, K, tri, out->e);
   NLA_CHECK_LAUNCH("row_exp_kernel");
@@ -1516,7 +1520,13 @@ int stage_pair(const Mat& A, int64_t M, const Mat& Bt, int64_t N, int64_t K, int
     j.blocks = (int)(st.rows_pad / 32);
     return j;
   };
-  const StageJob ja = job(A, *As), jb = job(Bt, *Bs);
+  StageJob ja = job(A, *As), jb = job(Bt, *Bs);
+  jb.nrm = nullptr;  // only the A operand's row-magnitude sums are read (exact kernel)
+  Bs->nrm = nullptr;
+  if (S != EXACT_SLICES) {
+    ja.nrm = nullptr;
+    As->nrm = nullptr;
+  }
   const int64_t grid = (int64_t)ja.blocks + jb.blocks;
   if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "operand too large");
   TraceScope trace(NLA_K_SPLIT, s, 0.0,
@@ -1581,7 +1591,8 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
       NLA_TRY(stage_pair(A, M, transposed(B), N, K, S, true, base, static_cast<uint8_t*>(base) + sa, &As, &Bs, s));
     } else {
       NLA_TRY(stage_operand(A, M, K, NLA_F64, S, true, 0, base, &As, s));
-      NLA_TRY(stage_operand(transposed(B), N, K, NLA_F64, S, true, 0, static_cast<uint8_t*>(base) + sa, &Bs, s));
+      NLA_TRY(stage_operand(transposed(B), N, K, NLA_F64, S, true, 0, static_cast<uint8_t*>(base) + sa, &Bs, s,
+                            false));
     }
     return launch_exact_gemm(As, Bs, alpha, C, false, s, nullptr, fixed, overwrite);
   }
@@ -1602,9 +1613,9 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
     NLA_TRY(stage_pair(A, M, transposed(B), N, K, S, bf16, base, static_cast<uint8_t*>(base) + staged_bytes(M, K, S),
                        &As, &Bs, s));
   } else {
-    NLA_TRY(stage_operand(A, M, K, in_dtype, S, bf16, 0, base, &As, s));
+    NLA_TRY(stage_operand(A, M, K, in_dtype, S, bf16, 0, base, &As, s, false));
     NLA_TRY(stage_operand(transposed(B), N, K, in_dtype, S, bf16, 0,
-                          static_cast<uint8_t*>(base) + staged_bytes(M, K, S), &Bs, s));
+                          static_cast<uint8_t*>(base) + staged_bytes(M, K, S), &Bs, s, false));
   }
 
   const bool use_bf16 = As.bf16;
