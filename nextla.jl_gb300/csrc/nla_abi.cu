@@ -258,6 +258,7 @@ int rec_update(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
 }
 
 int recurse(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
+  if (c.inv && leaf_pair_wanted(c, n)) return leaf_pair_apply(c, A, n, B);
   if (n <= c.threshold) {
     if (c.inv) return leaf_inverse_apply(c, A, n, B);
     return launch_leaf(c.func, c.side, c.uplo, c.dtype, n, c.m, A, B, c.s, c.unit);

@@ -224,6 +224,10 @@ int recurse(const RecPlan& c, const Mat& A, int64_t n, const Mat& B);
 bool leaf_inverses_wanted(const RecPlan& c);
 int leaf_inverses_upfront(const RecPlan& c, const Mat& A, int64_t n, LeafInverses* out);
 int leaf_inverse_apply(const RecPlan& c, const Mat& A, int64_t n, const Mat& B);
+// A recursion node whose two halves are both leaves, solved with the update
+// between them in one launch (nla_mixed.cu).
+bool leaf_pair_wanted(const RecPlan& c, int64_t n);
+int leaf_pair_apply(const RecPlan& c, const Mat& A, int64_t n, const Mat& B);
 // Launches inside the scope are traced under kernel class kclass (the leaf
 // products of a mixed solve run the update kernels but are leaf work).
 struct TraceClassScope {

@@ -256,6 +256,157 @@ constexpr int LP_A_BYTES = split7::SLICES * LP_COLS * 128;   // X^T slices: 128 
 constexpr int LP_B_BYTES = split7::SLICES * LEAF_INV_N * 128;  // W slices: 64 rows x 64 K
 constexpr int LP_SMEM = LP_A_BYTES + LP_B_BYTES + 1024 + 8192;
 
+// Shared memory of the leaf product kernels.  Thread t holds, for every
+// product, rows k = 16 (t / 128) + u (u < 16) of right-hand side t % 128 and
+// row t % 64 of the W operand at k = 8 (t / 64) + u (u < 8); the drain gives
+// it output rows 16 (t / 128) + c of right-hand side t % 128, the same
+// positions, so one product's result is the next one's right-hand sides
+// without an exchange.
+struct LpShared {
+  uint8_t* sA;         // 7 slices of the right-hand sides: 128 rows x 64 K
+  uint8_t* sB;         // 7 slices of W: 64 rows x 64 K
+  int* xpart;          // [4][128] exponent-field maxima of the right-hand sides
+  int* wpart;          // [8][64] of W's rows
+  int* ex_s;           // [128] scale exponents of the right-hand sides
+  int* ew_s;           // [64] of W's rows
+  uint64_t* bar;       // MMA completion
+  uint32_t* tmem_slot;
+};
+
+__device__ __forceinline__ LpShared lp_shared(uint8_t* raw) {
+  LpShared s;
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(raw) + 1023) & ~uintptr_t(1023));
+  s.sA = smem;
+  s.sB = smem + LP_A_BYTES;
+  s.xpart = reinterpret_cast<int*>(s.sB + LP_B_BYTES);
+  s.wpart = s.xpart + 4 * LP_COLS;
+  s.ex_s = s.wpart + 8 * LEAF_INV_N;
+  s.ew_s = s.ex_s + LP_COLS;
+  s.bar = reinterpret_cast<uint64_t*>(s.ew_s + LEAF_INV_N);
+  s.tmem_slot = reinterpret_cast<uint32_t*>(s.bar + 1);
+  return s;
+}
+
+// The scale exponents (per right-hand side and per row of W) and the 7
+// digit slices of one product's operands, ending with the slices visible to
+// the tensor cores.  Every thread of the CTA takes part.
+__device__ __forceinline__ void lp_stage(const LpShared& s, const double (&vx)[16], const double (&vw)[8]) {
+  using namespace split7;
+  const int t = threadIdx.x;
+  const int jr = t & (LP_COLS - 1), xp = t >> 7;
+  const int wi = t & (LEAF_INV_N - 1), wp = t >> 6;
+  int bx = 0, bw = 0;
+#pragma unroll
+  for (int u = 0; u < 16; ++u) bx = max(bx, exp_field(vx[u]));
+#pragma unroll
+  for (int u = 0; u < 8; ++u) bw = max(bw, exp_field(vw[u]));
+  s.xpart[xp * LP_COLS + jr] = bx;
+  s.wpart[wp * LEAF_INV_N + wi] = bw;
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  if (t < LP_COLS) {
+    s.ex_s[t] =
+        scale_exp(max(max(s.xpart[t], s.xpart[LP_COLS + t]), max(s.xpart[2 * LP_COLS + t], s.xpart[3 * LP_COLS + t])));
+  } else if (t < LP_COLS + LEAF_INV_N) {
+    const int i = t - LP_COLS;
+    int m8 = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) m8 = max(m8, s.wpart[q * LEAF_INV_N + i]);
+    s.ew_s[i] = scale_exp(m8);
+  }
+  __syncthreads();
+  {
+    const int ex = s.ex_s[jr], ew = s.ew_s[wi];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      long long y[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) y[u] = fixed56(vx[c * 8 + u], ex);
+      store_chunks(s.sA, LP_COLS * 128, jr, xp * 2 + c, y);
+    }
+    long long y[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) y[u] = fixed56(vw[u], ew);
+    store_chunks(s.sB, LEAF_INV_N * 128, wi, wp, y);
+  }
+  // The tensor cores read shared memory through the async proxy.
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+}
+
+// The 28 slice pairs with p + q <= 6 (weight w = p + q into accumulator w),
+// issued by one thread, with their completion committed to s.bar.
+__device__ __forceinline__ void lp_issue(const LpShared& s, uint32_t tmem) {
+  using namespace split7;
+  const uint32_t idesc = umma::idesc_f16(LP_COLS, LEAF_INV_N, true);
+  const uint32_t a0 = umma::smem_u32(s.sA), b0 = umma::smem_u32(s.sB);
+#pragma unroll 1
+  for (int w = 0; w < SLICES; ++w)
+    for (int p = 0; p <= w; ++p) {
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+        umma::mma_f16(tmem + (uint32_t)(w * LEAF_INV_N), umma::desc_kmajor_sw128(a0 + p * LP_COLS * 128 + kk * 32),
+                      umma::desc_kmajor_sw128(b0 + (w - p) * LEAF_INV_N * 128 + kk * 32), idesc,
+                      (p > 0 || kk > 0) ? 1u : 0u);
+    }
+  umma::mma_commit(umma::smem_u32(s.bar));
+}
+
+// Waits for the products committed in phase `parity`, with one answer for
+// the whole CTA.  After a wait that gave up, thread 0 lets the MMAs finish
+// (a drain with the default limit) so that the tensor memory can be
+// released.
+__device__ __forceinline__ bool lp_wait(const LpShared& s, uint32_t parity, volatile int* abort, int* err,
+                                        int site) {
+  __syncwarp();
+  bool ok = __all_sync(0xffffffffu, umma::mbar_wait(umma::smem_u32(s.bar), parity, abort, err, site));
+  umma::fence_after_sync();
+  ok = __syncthreads_and(ok ? 1 : 0) != 0;
+  if (!ok && threadIdx.x == 0) umma::mbar_wait(umma::smem_u32(s.bar), parity, abort, err, site + 1, false);
+  return ok;
+}
+
+// Drain: right-hand side t % 128 (the warp's TMEM lane quarter), output rows
+// 16 (t / 128) + c.  One block of K: S = H 2^18 + round(L 2^-6), with
+// H = sum_{w<4} T_w 2^(24 - 8 w) and L = sum_{4<=w<7} T_w 2^(48 - 8 w); the
+// product is S 2^(e_x + e_w - 58).  L is rounded first and H 2^18 added as
+// the exact integer sum_{w<4} T_w 2^(42 - 8 w), which keeps one int64 per
+// element live.
+__device__ __forceinline__ void lp_drain(uint32_t tmem, long long (&tot)[16]) {
+  using namespace split7;
+  const int warp = threadIdx.x >> 5;
+  const uint32_t tq = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((warp >> 2) * 16);
+#pragma unroll
+  for (int c = 0; c < 16; ++c) tot[c] = 0;
+#pragma unroll
+  for (int w = 4; w < SLICES; ++w) {
+    uint32_t rr[16];
+    umma::tmem_ld16(tq + (uint32_t)(w * LEAF_INV_N), rr);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) tot[c] += (long long)__float2int_rn(__uint_as_float(rr[c])) << (48 - 8 * w);
+  }
+#pragma unroll
+  for (int c = 0; c < 16; ++c) tot[c] = (tot[c] + (1ll << 5)) >> 6;
+#pragma unroll
+  for (int w = 0; w < 4; ++w) {
+    uint32_t rr[16];
+    umma::tmem_ld16(tq + (uint32_t)(w * LEAF_INV_N), rr);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) tot[c] += (long long)__float2int_rn(__uint_as_float(rr[c])) << (42 - 8 * w);
+  }
+}
+
+// One element of a product from its int64 sum and the operands' scale
+// exponents (NaN when either operand held a non-finite value).
+__device__ __forceinline__ double lp_value(long long tot, int ex, int ew) {
+  using namespace split7;
+  return ex == NONFINITE || ew == NONFINITE ? __longlong_as_double(0x7ff8000000000000ll)
+                                            : scaled_i64_to_f64(tot, ex + ew - 58);
+}
+
 struct LeafProdArgs {
   const double* W;  // column-major, leading dimension LEAF_INV_N
   double* X;
@@ -267,20 +418,11 @@ struct LeafProdArgs {
 };
 
 __global__ void __launch_bounds__(LP_THREADS, 1) leaf_product_kernel(const LeafProdArgs a) {
-  using namespace split7;
   extern __shared__ uint8_t lp_smem_raw[];
-  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(lp_smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* sA = smem;
-  uint8_t* sB = smem + LP_A_BYTES;
-  int* xpart = reinterpret_cast<int*>(sB + LP_B_BYTES);  // [4][128] exponent-field maxima of X
-  int* wpart = xpart + 4 * LP_COLS;                        // [8][64] of W
-  int* ex_s = wpart + 8 * LEAF_INV_N;                      // [128] scale exponents of the right-hand sides
-  int* ew_s = ex_s + LP_COLS;                              // [64] of W's rows
-  uint64_t* mma_bar = reinterpret_cast<uint64_t*>(ew_s + LEAF_INV_N);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_bar + 1);
+  const LpShared s = lp_shared(lp_smem_raw);
   __shared__ volatile int s_abort;
 
-  const int t = threadIdx.x, warp = t >> 5, lane = t & 31, n = a.n;
+  const int t = threadIdx.x, warp = t >> 5, n = a.n;
   const int64_t j0 = (int64_t)blockIdx.x * LP_COLS;
   // Element (k, j) of the right-hand sides (k < n, j < m) and (i, k) of the
   // W operand (W itself for side L, W^T for side R).
@@ -289,13 +431,11 @@ __global__ void __launch_bounds__(LP_THREADS, 1) leaf_product_kernel(const LeafP
 
   if (t == 0) {
     s_abort = 0;
-    umma::mbar_init(umma::smem_u32(mma_bar), 1);
+    umma::mbar_init(umma::smem_u32(s.bar), 1);
     umma::fence_barrier_init();
   }
-  if (warp == 0) umma::tmem_alloc(umma::smem_u32(tmem_slot), 512);
+  if (warp == 0) umma::tmem_alloc(umma::smem_u32(s.tmem_slot), 512);
 
-  // Loads: right-hand side jr = t % 128 with k = 16 (t / 128) .. + 16; row
-  // i = t % 64 of W with k = 8 (t / 64) .. + 8.
   const int jr = t & (LP_COLS - 1), xp = t >> 7;
   const int wi = t & (LEAF_INV_N - 1), wp = t >> 6;
   const int64_t j = j0 + jr;
@@ -310,101 +450,235 @@ __global__ void __launch_bounds__(LP_THREADS, 1) leaf_product_kernel(const LeafP
     const int k = wp * 8 + u;
     vw[u] = wi < n && k < n ? a.W[wat(wi, k)] : 0.0;
   }
-  int bx = 0, bw = 0;
+  lp_stage(s, vx, vw);
+  const uint32_t tmem = *s.tmem_slot;
+  if (t == 0) lp_issue(s, tmem);
+  if (lp_wait(s, 0u, &s_abort, a.err, 41)) {
+    long long tot[16];
+    lp_drain(tmem, tot);
+    const int ex = s.ex_s[jr];
+    if (j < a.m) {
 #pragma unroll
-  for (int u = 0; u < 16; ++u) bx = max(bx, exp_field(vx[u]));
-#pragma unroll
-  for (int u = 0; u < 8; ++u) bw = max(bw, exp_field(vw[u]));
-  xpart[xp * LP_COLS + jr] = bx;
-  wpart[wp * LEAF_INV_N + wi] = bw;
-  umma::fence_before_sync();
-  __syncthreads();
-  umma::fence_after_sync();
-  const uint32_t tmem = *tmem_slot;
-  if (t < LP_COLS) {
-    ex_s[t] = scale_exp(max(max(xpart[t], xpart[LP_COLS + t]), max(xpart[2 * LP_COLS + t], xpart[3 * LP_COLS + t])));
-  } else if (t < LP_COLS + LEAF_INV_N) {
-    const int i = t - LP_COLS;
-    int m8 = 0;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) m8 = max(m8, wpart[q * LEAF_INV_N + i]);
-    ew_s[i] = scale_exp(m8);
-  }
-  __syncthreads();
-  {
-    const int ex = ex_s[jr], ew = ew_s[wi];
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      long long y[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) y[u] = fixed56(vx[c * 8 + u], ex);
-      store_chunks(sA, LP_COLS * 128, jr, xp * 2 + c, y);
+      for (int c = 0; c < 16; ++c) {
+        const int i = xp * 16 + c;
+        if (i < n) a.X[xat(i, j)] = lp_value(tot[c], ex, s.ew_s[i]);
+      }
     }
-    long long y[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) y[u] = fixed56(vw[u], ew);
-    store_chunks(sB, LEAF_INV_N * 128, wi, wp, y);
   }
-  // The tensor cores read shared memory through the async proxy.
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   umma::fence_before_sync();
   __syncthreads();
-  umma::fence_after_sync();
-  if (t == 0) {
-    const uint32_t idesc = umma::idesc_f16(LP_COLS, LEAF_INV_N, true);
-    const uint32_t a0 = umma::smem_u32(sA), b0 = umma::smem_u32(sB);
+  if (warp == 0) {
+    umma::fence_after_sync();
+    umma::tmem_dealloc(tmem, 512);
+  }
+}
+
+// Two sibling leaves of the recursion and the update between them in one
+// kernel: for the node of n <= 128 rows whose halves f (solved first) and s
+// are both leaves,
+//     X_f := W_f X_f,   C := X_s - G X_f,   X_s := W_s C
+// with G the node's off-diagonal block (A21 or A12 of the recursion's update,
+// read through the caller's strides).  Each step is the exact 7-slice product
+// of leaf_product_kernel, rounded once per element as in the separate
+// launches (the update's result is X_s - round(G X_f)); X_f and C stay in
+// registers between the steps, in the positions the next step loads them
+// from.  This replaces a leaf launch, the update's staging, product and
+// finishing launches and the second leaf launch of every such node.
+struct LeafPairArgs {
+  const double* Wf;  // inverses of the two leaves, column-major, leading dimension LEAF_INV_N
+  const double* Ws;
+  const double* G;   // G(i, k) = G[i * gsi + k * gsk], i < ns, k < nf
+  int64_t gsi, gsk;
+  double* Xf;        // the halves' right-hand sides: element (k, j) at k + j ldx (side L) or j + k ldx (side R)
+  double* Xs;
+  int64_t ldx;
+  int64_t m;
+  int nf, ns;
+  int* err;
+};
+
+// Side L: a block of right-hand sides (rows k < 64 of the CTA's 128
+// columns; column j at X + j ldx) passes through a shared-memory tile, so
+// that global loads and stores run along the contiguous rows (a thread's own
+// 16 rows of one column would touch 32 cache lines per warp instruction).
+// Row r of the tile is right-hand side r, padded to LP_TP doubles.
+constexpr int LP_TP = 65;
+static_assert(LP_COLS * LP_TP * 8 <= LP_A_BYTES, "the staging tile lives in the slice buffer");
+
+// Asynchronous copy of the block into the tile: warp w takes columns w + 16 q
+// (q < 8), lane l rows l and l + 32; rows >= nk and columns >= m read as 0.
+__device__ __forceinline__ void lp_tile_fetch(double* tile, const double* X, int64_t ldx, int64_t j0, int64_t m,
+                                              int nk) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll 1
-    for (int w = 0; w < SLICES; ++w)
-      for (int p = 0; p <= w; ++p) {
+  for (int q = 0; q < 8; ++q) {
+    const int r = warp + 16 * q;
+    const int64_t j = j0 + r;
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
-          umma::mma_f16(tmem + (uint32_t)(w * LEAF_INV_N), umma::desc_kmajor_sw128(a0 + p * LP_COLS * 128 + kk * 32),
-                        umma::desc_kmajor_sw128(b0 + (w - p) * LEAF_INV_N * 128 + kk * 32), idesc,
-                        (p > 0 || kk > 0) ? 1u : 0u);
-      }
-    umma::mma_commit(umma::smem_u32(mma_bar));
+    for (int h = 0; h < 2; ++h) {
+      const int k = lane + 32 * h;
+      const bool in = j < m && k < nk;
+      const double* src = in ? X + k + j * ldx : X;
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(umma::smem_u32(tile + r * LP_TP + k)),
+                   "l"(src), "r"(in ? 8 : 0)
+                   : "memory");
+    }
   }
-  __syncwarp();
-  bool ok = __all_sync(0xffffffffu, umma::mbar_wait(umma::smem_u32(mma_bar), 0u, &s_abort, a.err, 41));
-  umma::fence_after_sync();
-  if (!ok && t == 0) {
-    // Let the MMAs finish (a drain with the default limit) before the tensor
-    // memory is released.
-    umma::mbar_wait(umma::smem_u32(mma_bar), 0u, &s_abort, a.err, 42, false);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void lp_tile_arrived() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  __syncthreads();
+}
+
+// Stores rows k < nk of the tile's columns j < m back to X (after a barrier
+// that follows the tile's writes).
+__device__ __forceinline__ void lp_tile_store(const double* tile, double* X, int64_t ldx, int64_t j0, int64_t m,
+                                              int nk) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int r = warp + 16 * q;
+    const int64_t j = j0 + r;
+    if (j >= m) break;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = lane + 32 * h;
+      if (k < nk) X[k + j * ldx] = tile[r * LP_TP + k];
+    }
   }
+}
+
+template <bool SIDE_R>
+__global__ void __launch_bounds__(LP_THREADS, 1) leaf_pair_kernel(const LeafPairArgs a) {
+  extern __shared__ uint8_t lp_smem_raw[];
+  const LpShared s = lp_shared(lp_smem_raw);
+  __shared__ volatile int s_abort;
+
+  const int t = threadIdx.x, warp = t >> 5;
+  const int jr = t & (LP_COLS - 1), xp = t >> 7;
+  const int wi = t & (LEAF_INV_N - 1), wp = t >> 6;
+  const int64_t j0 = (int64_t)blockIdx.x * LP_COLS;
+  const int64_t j = j0 + jr;
+  const bool jin = j < a.m;
+  // Side R: X(k, j) at j + k ldx, so a thread's loads and stores are already
+  // coalesced across the warp (consecutive j); side L goes through `tile`.
+  double* tile = reinterpret_cast<double*>(s.sA);
+  double* trow = tile + jr * LP_TP + xp * 16;
+  auto wat = [&](int i, int k) -> int { return SIDE_R ? k + i * LEAF_INV_N : i + k * LEAF_INV_N; };
+
+  if (t == 0) {
+    s_abort = 0;
+    umma::mbar_init(umma::smem_u32(s.bar), 1);
+    umma::fence_barrier_init();
+  }
+  if (warp == 0) umma::tmem_alloc(umma::smem_u32(s.tmem_slot), 512);
+
+  // X_f := W_f X_f.
+  double vx[16], vw[8];
+  if constexpr (!SIDE_R) lp_tile_fetch(tile, a.Xf, a.ldx, j0, a.m, a.nf);
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int k = wp * 8 + u;
+    vw[u] = wi < a.nf && k < a.nf ? a.Wf[wat(wi, k)] : 0.0;
+  }
+  if constexpr (!SIDE_R) {
+    lp_tile_arrived();
+#pragma unroll
+    for (int u = 0; u < 16; ++u) vx[u] = trow[u];
+  } else {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int k = xp * 16 + u;
+      vx[u] = k < a.nf && jin ? a.Xf[j + k * a.ldx] : 0.0;
+    }
+  }
+  lp_stage(s, vx, vw);
+  const uint32_t tmem = *s.tmem_slot;
+  if (t == 0) lp_issue(s, tmem);
+  // G's block, in flight during the products.
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int k = wp * 8 + u;
+    vw[u] = wi < a.ns && k < a.nf ? a.G[wi * a.gsi + k * a.gsk] : 0.0;
+  }
+  bool ok = lp_wait(s, 0u, &s_abort, a.err, 43);
   if (ok) {
-    // Drain: right-hand side q * 32 + lane (the warp's TMEM lane quarter),
-    // output rows h * 16 .. + 16.  One block of K: S = H 2^18 + round(L 2^-6)
-    // (H = sum_{w<4} T_w 2^(24 - 8 w), L = sum_{4<=w<7} T_w 2^(48 - 8 w)),
-    // and the product is S 2^(e_x + e_w - 58).
-    const int q = warp & 3, h = warp >> 2;
-    const int jd = q * 32 + lane;
-    const int64_t jj = j0 + jd;
-    const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 16);
-    long long S[16], L[16];
-#pragma unroll
-    for (int c = 0; c < 16; ++c) S[c] = L[c] = 0;
-#pragma unroll
-    for (int w = 0; w < SLICES; ++w) {
-      uint32_t rr[16];
-      umma::tmem_ld16(tq + (uint32_t)(w * LEAF_INV_N), rr);
+    long long tot[16];
+    lp_drain(tmem, tot);
+    const int ex = s.ex_s[jr];
+    if constexpr (!SIDE_R) {
+      // The values wait in the tile (not in registers) while it is stored.
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
-        const long long v = (long long)__float2int_rn(__uint_as_float(rr[c]));
-        if (w < 4) S[c] += v << (24 - 8 * w);
-        else L[c] += v << (48 - 8 * w);
+        const int i = xp * 16 + c;
+        trow[c] = i < a.nf ? lp_value(tot[c], ex, s.ew_s[i]) : 0.0;
+      }
+      __syncthreads();
+      lp_tile_store(tile, a.Xf, a.ldx, j0, a.m, a.nf);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) vx[u] = trow[u];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int i = xp * 16 + c;
+        vx[c] = i < a.nf ? lp_value(tot[c], ex, s.ew_s[i]) : 0.0;
+        if (jin && i < a.nf) a.Xf[j + i * a.ldx] = vx[c];
       }
     }
-    const int ex = ex_s[jd];
-    if (jj < a.m) {
+
+    // C := X_s - G X_f.
+    lp_stage(s, vx, vw);
+    if (t == 0) lp_issue(s, tmem);
+    if constexpr (!SIDE_R) {
+      // X_s's block into L2 while the products run (one 128-byte line per
+      // thread); it comes into the tile once they are done.
+      const int r = t >> 2, k = (t & 3) * 16;
+      if (j0 + r < a.m && k < a.ns)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Xs + k + (j0 + r) * a.ldx));
+    }
+    ok = lp_wait(s, 1u, &s_abort, a.err, 43);
+    if (ok) {
+      if constexpr (!SIDE_R) lp_tile_fetch(tile, a.Xs, a.ldx, j0, a.m, a.ns);
+      lp_drain(tmem, tot);
+      const int ex2 = s.ex_s[jr];
+      if constexpr (!SIDE_R) lp_tile_arrived();
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
-        const int i = h * 16 + c;
-        if (i < n) {
-          const int ew = ew_s[i];
-          const long long tot = (S[c] << 18) + ((L[c] + (1ll << 5)) >> 6);
-          a.X[xat(i, jj)] = ex == NONFINITE || ew == NONFINITE ? __longlong_as_double(0x7ff8000000000000ll)
-                                                               : scaled_i64_to_f64(tot, ex + ew - 58);
+        const int i = xp * 16 + c;
+        double bs;
+        if constexpr (!SIDE_R) bs = trow[c];
+        else bs = i < a.ns && jin ? a.Xs[j + i * a.ldx] : 0.0;
+        vx[c] = i < a.ns ? bs - lp_value(tot[c], ex2, s.ew_s[i]) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = wp * 8 + u;
+        vw[u] = wi < a.ns && k < a.ns ? a.Ws[wat(wi, k)] : 0.0;
+      }
+
+      // X_s := W_s C.
+      lp_stage(s, vx, vw);
+      if (t == 0) lp_issue(s, tmem);
+      ok = lp_wait(s, 0u, &s_abort, a.err, 43);
+      if (ok) {
+        lp_drain(tmem, tot);
+        const int ex3 = s.ex_s[jr];
+        if constexpr (!SIDE_R) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const int i = xp * 16 + c;
+            trow[c] = i < a.ns ? lp_value(tot[c], ex3, s.ew_s[i]) : 0.0;
+          }
+          __syncthreads();
+          lp_tile_store(tile, a.Xs, a.ldx, j0, a.m, a.ns);
+        } else if (jin) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const int i = xp * 16 + c;
+            if (i < a.ns) a.Xs[j + i * a.ldx] = lp_value(tot[c], ex3, s.ew_s[i]);
+          }
         }
       }
     }
@@ -507,21 +781,37 @@ int leaf_inverses_upfront(const RecPlan& c, const Mat& A, int64_t n, LeafInverse
   return launch_inverses(c, out->a_base, A.ld, A.t, out->k, ns, out->w, 0);
 }
 
-int leaf_inverse_apply(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
-  if (n <= 0 || c.m <= 0) return NLA_OK;
-  const LeafInverses& L = *c.inv;
-  const int64_t k = (static_cast<const double*>(A.p) - L.a_base) / (L.lda + 1);
+namespace {
+
+// Slot of the inverse of the leaf whose diagonal block starts at row k of the
+// solve's A.
+int leaf_slot(const LeafInverses& L, int64_t k, int64_t* slot) {
   const auto it = std::lower_bound(L.k.begin(), L.k.end(), k);
   if (L.a_base == nullptr || it == L.k.end() || *it != k)
     return fail(NLA_ERR_ARG, "leaf inverses: no inverse for this block");
-  const int64_t slot = it - L.k.begin();
-  // X := inv(T) X  (side L)  or  X inv(T)  (side R), one kernel.
+  *slot = it - L.k.begin();
+  return NLA_OK;
+}
+
+// The shared-memory opt-in of one leaf product kernel, once per process
+// (one flag per kernel: the template argument is the kernel itself).
+template <auto Kernel>
+int allow_smem(const char* name) {
   static std::once_flag once;
   static cudaError_t attr = cudaSuccess;
-  std::call_once(once, [] {
-    attr = cudaFuncSetAttribute(leaf_product_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, LP_SMEM);
-  });
-  if (attr != cudaSuccess) return cuda_status(attr, "cudaFuncSetAttribute(leaf_product_kernel)");
+  std::call_once(once, [] { attr = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, LP_SMEM); });
+  return attr == cudaSuccess ? NLA_OK : cuda_status(attr, name);
+}
+
+}  // namespace
+
+int leaf_inverse_apply(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
+  if (n <= 0 || c.m <= 0) return NLA_OK;
+  const LeafInverses& L = *c.inv;
+  int64_t slot = 0;
+  NLA_TRY(leaf_slot(L, (static_cast<const double*>(A.p) - L.a_base) / (L.lda + 1), &slot));
+  // X := inv(T) X  (side L)  or  X inv(T)  (side R), one kernel.
+  NLA_TRY(allow_smem<leaf_product_kernel>("cudaFuncSetAttribute(leaf_product_kernel)"));
   if (B.t) return fail(NLA_ERR_UNSUPPORTED, "leaf product: transposed B view");
   LeafProdArgs g{L.w + slot * LEAF_INV_N * LEAF_INV_N, static_cast<double*>(B.p), B.ld, c.m, (int)n,
                  c.side == 'R' ? 1 : 0, L.err};
@@ -530,6 +820,62 @@ int leaf_inverse_apply(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) 
   TraceScope trace(NLA_K_LEAF_SOLVE, c.s, 2.0 * (double)n * n * (double)c.m, 16.0 * (double)n * (double)c.m);
   leaf_product_kernel<<<(unsigned)grid, LP_THREADS, LP_SMEM, c.s>>>(g);
   NLA_CHECK_LAUNCH("leaf_product_kernel");
+  return NLA_OK;
+}
+
+bool leaf_pair_wanted(const RecPlan& c, int64_t n) {
+  if (!c.inv || c.func != 'S' || n <= c.threshold) return false;
+  const int64_t mid = split_point(n);
+  if (mid > c.threshold || n - mid > c.threshold) return false;
+  const char* v = std::getenv("NLA_LEAF_PAIR");
+  return !(v && v[0] == '0');
+}
+
+int leaf_pair_apply(const RecPlan& c, const Mat& A, int64_t n, const Mat& B) {
+  if (c.m <= 0) return NLA_OK;
+  const LeafInverses& L = *c.inv;
+  if (B.t) return fail(NLA_ERR_UNSUPPORTED, "leaf pair: transposed B view");
+  // The halves in the recursion's order (src/rectrxm.jl:104-124): f is solved
+  // first, then s is updated from it and solved.
+  const int64_t mid = split_point(n), rem = n - mid;
+  const bool fwd = rec_forward(c), R = c.side == 'R';
+  const int64_t of = fwd ? 0 : mid, nf = fwd ? mid : rem, os = fwd ? mid : 0, ns = fwd ? rem : mid;
+  const double* Ap = static_cast<const double*>(A.p);
+  const int64_t k0 = (Ap - L.a_base) / (L.lda + 1);
+  int64_t slot_f = 0, slot_s = 0;
+  NLA_TRY(leaf_slot(L, k0 + of, &slot_f));
+  NLA_TRY(leaf_slot(L, k0 + os, &slot_s));
+  NLA_TRY(R ? allow_smem<leaf_pair_kernel<true>>("cudaFuncSetAttribute(leaf_pair_kernel)")
+            : allow_smem<leaf_pair_kernel<false>>("cudaFuncSetAttribute(leaf_pair_kernel)"));
+  LeafPairArgs g{};
+  g.Wf = L.w + slot_f * LEAF_INV_N * LEAF_INV_N;
+  g.Ws = L.w + slot_s * LEAF_INV_N * LEAF_INV_N;
+  // G(i, k) = op(A)(os + i, of + k) for side L (B_s -= A_sf X_f) and
+  // op(A)(of + k, os + i) for side R (X_s -= X_f A_fs), read through A's view.
+  if (!R) {
+    g.G = Ap + mat_off(os, of, A.ld, A.t);
+    g.gsi = A.t ? A.ld : 1;
+    g.gsk = A.t ? 1 : A.ld;
+  } else {
+    g.G = Ap + mat_off(of, os, A.ld, A.t);
+    g.gsi = A.t ? 1 : A.ld;
+    g.gsk = A.t ? A.ld : 1;
+  }
+  double* Bp = static_cast<double*>(B.p);
+  g.Xf = Bp + (R ? of * B.ld : of);
+  g.Xs = Bp + (R ? os * B.ld : os);
+  g.ldx = B.ld;
+  g.m = c.m;
+  g.nf = (int)nf;
+  g.ns = (int)ns;
+  g.err = L.err;
+  const int64_t grid = (c.m + LP_COLS - 1) / LP_COLS;
+  if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "leaf pair: too many right-hand sides");
+  TraceScope trace(NLA_K_LEAF_SOLVE, c.s, 2.0 * (double)(nf * nf + ns * ns + nf * ns) * (double)c.m,
+                   8.0 * (double)(2 * n + ns) * (double)c.m);
+  if (R) leaf_pair_kernel<true><<<(unsigned)grid, LP_THREADS, LP_SMEM, c.s>>>(g);
+  else leaf_pair_kernel<false><<<(unsigned)grid, LP_THREADS, LP_SMEM, c.s>>>(g);
+  NLA_CHECK_LAUNCH("leaf_pair_kernel");
   return NLA_OK;
 }
 

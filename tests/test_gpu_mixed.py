@@ -102,7 +102,7 @@ def test_refinement_residual_modes(pkg, oracle, workloads, cuda, residual):
 @pytest.mark.parametrize("diag", ["N", "U"])
 def test_inverse_leaves_match_substitution(pkg, oracle, workloads, cuda, diag, monkeypatch):
     """Exact 7-slice solves apply each leaf block through its FP64 inverse on
-    the tensor cores (X += (inv(T) - I) X).  Over every side, uplo and trans,
+    the tensor cores (X := inv(T) X).  Over every side, uplo and trans,
     sizes with ragged leaves (n = 1, 65, 1000, 1500) and a unit diagonal,
     the result matches the substitution leaves (NLA_MIXED_INV_LEAF=0) and
     the oracle at the Float64 tolerance."""
@@ -129,3 +129,57 @@ def test_inverse_leaves_match_substitution(pkg, oracle, workloads, cuda, diag, m
         assert np.isfinite(out["1"]).all(), (n, side, uplo, trans)
         assert oracle.rel_err(out["1"], ref) < 1e-13, (n, side, uplo, trans)
         assert oracle.rel_err(out["1"], out["0"]) < 1e-13, (n, side, uplo, trans)
+
+
+def test_leaf_pairs_match_separate_leaves(pkg, oracle, workloads, cuda, monkeypatch):
+    """A recursion node whose two halves are both leaves runs as one launch
+    (leaf, update, leaf: leaf_pair_kernel).  Over every side, uplo and trans,
+    nodes of 64 + 1, 64 + 36 and 64 + 64 rows and the nodes inside n = 1000,
+    with right-hand-side counts that leave a partial block of 128, the result
+    matches the separate launches (NLA_LEAF_PAIR=0) to a few rounding errors
+    and the oracle at the Float64 tolerance.  A NaN or an infinity in B
+    spreads over its own right-hand side only, as in the separate launches."""
+    import torch
+
+    nthreads = os.cpu_count() or 1
+    cases = [(65, 37), (100, 300), (128, 129), (1000, 257)]
+    for k, ((n, m), side, uplo, trans) in enumerate(itertools.product(cases, "LR", "LU", "NT")):
+        A, B = workloads.problem(n, m, side, uplo, seed=500 + k)
+        out = {}
+        for pair in ("1", "0"):
+            monkeypatch.setenv("NLA_LEAF_PAIR", pair)
+            Ad, Bd = to_dev(A, np.float64, cuda), to_dev(B, np.float64, cuda)
+            pkg.trsm(side, uplo, trans, "N", Ad, Bd, -1.5, mixed=True)
+            pkg.device_status(Bd)
+            torch.cuda.synchronize()
+            out[pair] = to_host(Bd)
+        ref = oracle.rectrxm(side, uplo, trans, -1.5, "S", A, B, nthreads=nthreads)
+        assert np.isfinite(out["1"]).all(), (n, m, side, uplo, trans)
+        assert oracle.rel_err(out["1"], ref) < 1e-13, (n, m, side, uplo, trans)
+        assert oracle.rel_err(out["1"], out["0"]) < 1e-14, (n, m, side, uplo, trans)
+
+    n, m = 100, 300
+    for side in "LR":
+        A, B = workloads.problem(n, m, side, "L", seed=77)
+        B = np.array(B)
+        if side == "L":
+            B[5, 3], B[70, 200] = np.nan, np.inf
+        else:
+            B[3, 5], B[200, 70] = np.nan, np.inf
+        out = {}
+        for pair in ("1", "0"):
+            monkeypatch.setenv("NLA_LEAF_PAIR", pair)
+            Ad, Bd = to_dev(A, np.float64, cuda), to_dev(B, np.float64, cuda)
+            pkg.trsm(side, "L", "N", "N", Ad, Bd, 1.0, mixed=True)
+            pkg.device_status(Bd)
+            torch.cuda.synchronize()
+            out[pair] = to_host(Bd)
+        bad = ~np.isfinite(out["0"])
+        assert bad.any(), side
+        assert np.array_equal(bad, ~np.isfinite(out["1"])), side
+        rhs_axis = 0 if side == "L" else 1  # right-hand sides are B's columns (L) or rows (R)
+        touched = bad.any(axis=rhs_axis)
+        assert touched.sum() == 2, side
+        good = out["0"][:, ~touched] if side == "L" else out["0"][~touched, :]
+        good1 = out["1"][:, ~touched] if side == "L" else out["1"][~touched, :]
+        assert oracle.rel_err(good1, good) < 1e-14, side
