@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(LP_THREADS, 1) leaf_pair_kernel(const LeafPair
   }
   if (warp == 0) umma::tmem_alloc(umma::smem_u32(s.tmem_slot), 512);
 
-  // X_f := W_f X_f.
+  // The first product's operands: X_f and W_f.
   double vx[16], vw[8];
   if constexpr (!SIDE_R) lp_tile_fetch(tile, a.Xf, a.ldx, j0, a.m, a.nf);
 #pragma unroll
@@ -594,92 +594,63 @@ __global__ void __launch_bounds__(LP_THREADS, 1) leaf_pair_kernel(const LeafPair
       vx[u] = k < a.nf && jin ? a.Xf[j + k * a.ldx] : 0.0;
     }
   }
-  lp_stage(s, vx, vw);
-  const uint32_t tmem = *s.tmem_slot;
-  if (t == 0) lp_issue(s, tmem);
-  // G's block, in flight during the products.
-#pragma unroll
-  for (int u = 0; u < 8; ++u) {
-    const int k = wp * 8 + u;
-    vw[u] = wi < a.ns && k < a.nf ? a.G[wi * a.gsi + k * a.gsk] : 0.0;
-  }
-  bool ok = lp_wait(s, 0u, &s_abort, a.err, 43);
-  if (ok) {
-    long long tot[16];
-    lp_drain(tmem, tot);
-    const int ex = s.ex_s[jr];
-    if constexpr (!SIDE_R) {
-      // The values wait in the tile (not in registers) while it is stored.
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        const int i = xp * 16 + c;
-        trow[c] = i < a.nf ? lp_value(tot[c], ex, s.ew_s[i]) : 0.0;
-      }
-      __syncthreads();
-      lp_tile_store(tile, a.Xf, a.ldx, j0, a.m, a.nf);
-#pragma unroll
-      for (int u = 0; u < 16; ++u) vx[u] = trow[u];
-    } else {
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        const int i = xp * 16 + c;
-        vx[c] = i < a.nf ? lp_value(tot[c], ex, s.ew_s[i]) : 0.0;
-        if (jin && i < a.nf) a.Xf[j + i * a.ldx] = vx[c];
-      }
-    }
+  uint32_t tmem = 0;
 
-    // C := X_s - G X_f.
+  // Step 0: X_f := W_f X_f;  step 1: C := X_s - G X_f;  step 2: X_s := W_s C.
+  // One body for the three steps, so that its code is fetched once and hits
+  // the instruction cache in the later steps.
+#pragma unroll 1
+  for (int st = 0; st < 3; ++st) {
     lp_stage(s, vx, vw);
+    if (st == 0) tmem = *s.tmem_slot;
     if (t == 0) lp_issue(s, tmem);
-    if constexpr (!SIDE_R) {
+    if (st == 0) {
+      // G's block, in flight during the products.
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = wp * 8 + u;
+        vw[u] = wi < a.ns && k < a.nf ? a.G[wi * a.gsi + k * a.gsk] : 0.0;
+      }
+    } else if (st == 1 && !SIDE_R) {
       // X_s's block into L2 while the products run (one 128-byte line per
       // thread); it comes into the tile once they are done.
       const int r = t >> 2, k = (t & 3) * 16;
-      if (j0 + r < a.m && k < a.ns)
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Xs + k + (j0 + r) * a.ldx));
+      if (j0 + r < a.m && k < a.ns) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Xs + k + (j0 + r) * a.ldx));
     }
-    ok = lp_wait(s, 1u, &s_abort, a.err, 43);
-    if (ok) {
-      if constexpr (!SIDE_R) lp_tile_fetch(tile, a.Xs, a.ldx, j0, a.m, a.ns);
-      lp_drain(tmem, tot);
-      const int ex2 = s.ex_s[jr];
-      if constexpr (!SIDE_R) lp_tile_arrived();
+    if (!lp_wait(s, (uint32_t)(st & 1), &s_abort, a.err, 43)) break;
+    if (st == 1 && !SIDE_R) lp_tile_fetch(tile, a.Xs, a.ldx, j0, a.m, a.ns);
+    long long tot[16];
+    lp_drain(tmem, tot);
+    const int ex = s.ex_s[jr];
+    const int nout = st == 0 ? a.nf : a.ns;
+    if (st == 1 && !SIDE_R) lp_tile_arrived();
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        const int i = xp * 16 + c;
-        double bs;
-        if constexpr (!SIDE_R) bs = trow[c];
-        else bs = i < a.ns && jin ? a.Xs[j + i * a.ldx] : 0.0;
-        vx[c] = i < a.ns ? bs - lp_value(tot[c], ex2, s.ew_s[i]) : 0.0;
+    for (int c = 0; c < 16; ++c) {
+      const int i = xp * 16 + c;
+      double v = 0.0;
+      if (i < nout) {
+        v = lp_value(tot[c], ex, s.ew_s[i]);
+        if (st == 1) v = (SIDE_R ? (jin ? a.Xs[j + i * a.ldx] : 0.0) : trow[c]) - v;
       }
+      vx[c] = v;
+    }
+    if (st != 1) {
+      double* Xo = st == 0 ? a.Xf : a.Xs;
+      if constexpr (!SIDE_R) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) trow[c] = vx[c];
+        __syncthreads();
+        lp_tile_store(tile, Xo, a.ldx, j0, a.m, nout);
+      } else if (jin) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          if (xp * 16 + c < nout) Xo[j + (xp * 16 + c) * a.ldx] = vx[c];
+      }
+    } else {
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int k = wp * 8 + u;
         vw[u] = wi < a.ns && k < a.ns ? a.Ws[wat(wi, k)] : 0.0;
-      }
-
-      // X_s := W_s C.
-      lp_stage(s, vx, vw);
-      if (t == 0) lp_issue(s, tmem);
-      ok = lp_wait(s, 0u, &s_abort, a.err, 43);
-      if (ok) {
-        lp_drain(tmem, tot);
-        const int ex3 = s.ex_s[jr];
-        if constexpr (!SIDE_R) {
-#pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const int i = xp * 16 + c;
-            trow[c] = i < a.ns ? lp_value(tot[c], ex3, s.ew_s[i]) : 0.0;
-          }
-          __syncthreads();
-          lp_tile_store(tile, a.Xs, a.ldx, j0, a.m, a.ns);
-        } else if (jin) {
-#pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const int i = xp * 16 + c;
-            if (i < a.ns) a.Xs[j + i * a.ldx] = lp_value(tot[c], ex3, s.ew_s[i]);
-          }
-        }
       }
     }
   }

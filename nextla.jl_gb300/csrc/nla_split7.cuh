@@ -78,6 +78,11 @@ __device__ __forceinline__ void store_chunks(uint8_t* base, int slice_bytes, int
   }
 }
 
+// The out-of-range case of scaled_i64_to_f64, out of line: inlined, ldexp's
+// code at every call site crowded the instruction cache of the kernels that
+// convert many elements in straight-line code.
+static __device__ __noinline__ double scaled_i64_to_f64_ldexp(long long v, int s) { return ldexp((double)v, s); }
+
 // (double)v * 2^s rounded to nearest even, with integer operations only (the
 // FP64 pipe runs 2 operations per clock per SM on GB300, and a conversion plus
 // ldexp per output element made it the busiest pipe of the kernels that write
@@ -101,7 +106,7 @@ __device__ __forceinline__ double scaled_i64_to_f64(long long v, int s) {
     m = u << (52 - msb);
   }
   const int biased = msb + s + 1023;
-  if (biased <= 0 || biased >= 2047) return ldexp((double)v, s);
+  if (biased <= 0 || biased >= 2047) return scaled_i64_to_f64_ldexp(v, s);
   return __longlong_as_double((long long)(sign | ((unsigned long long)biased << 52) | (m & 0xFFFFFFFFFFFFFull)));
 }
 
