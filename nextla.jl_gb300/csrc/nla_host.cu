@@ -176,9 +176,16 @@ int release_b(HostRun& h, int64_t k, int64_t len) {
   return NLA_OK;
 }
 
+// Where the staged walk stops: after `levels` levels, at a leaf, or at a node
+// whose two leaves and update run as one launch (the device-resident solve
+// runs that node the same way, and its results match bit for bit).
+bool walk_stops(const RecPlan& c, int64_t n, int levels) {
+  return levels == 0 || n <= c.threshold || leaf_pair_wanted(c, n);
+}
+
 // The blocks of B: the diagonal blocks where the staged walk stops.
 void plan_blocks(const RecPlan& c, int64_t k, int64_t n, int levels, std::vector<BlockB>* out) {
-  if (levels == 0 || n <= c.threshold) {
+  if (walk_stops(c, n, levels)) {
     out->push_back(BlockB{k, n, false, false});
     return;
   }
@@ -194,7 +201,7 @@ void plan_blocks(const RecPlan& c, int64_t k, int64_t n, int levels, std::vector
 // after the update.
 int staged(HostRun& h, int64_t k, int64_t n, int levels, bool emit) {
   const RecPlan& c = h.c;
-  if (levels == 0 || n <= c.threshold) {
+  if (walk_stops(c, n, levels)) {
     NLA_TRY(copy_a(h, k, k, n, n));
     NLA_TRY(acquire_b(h, k, n));
     // The block's leaves through their inverses: all of them inverted in one

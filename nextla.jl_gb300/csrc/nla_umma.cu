@@ -32,6 +32,7 @@
 #include <unordered_map>
 
 #include "nla_common.cuh"
+#include "nla_split7.cuh"
 #include "nla_umma.cuh"
 
 namespace nla {
@@ -447,8 +448,11 @@ __global__ void __launch_bounds__(256) exact_finish_kernel(const ExactParams p) 
       const int64_t col = cbase + c0 + c;
       if (col >= p.N) continue;
       double out = __longlong_as_double(0x7ff8000000000000ll);
+      // The sum as FP64 by integer operations (the same rounding as a
+      // conversion followed by an exact scaling), which leaves the FMA as
+      // the only work on GB300's FP64 pipe (2 operations per clock per SM).
       if (!row_nan && ej[c] != NONFINITE_EXP)
-        out = fma(p.alpha, scale_pow2(__ll2double_rn(v[c]), er + max(ej[c], -4000)), cv[c]);
+        out = fma(p.alpha, split7::scaled_i64_to_f64(v[c], er + max(ej[c], -4000)), cv[c]);
       static_cast<double*>(p.C)[(int64_t)i + col * p.ldc] = out;
     }
   }
