@@ -337,21 +337,31 @@ __device__ __forceinline__ void lp_stage(const LpShared& s, const double (&vx)[1
   umma::fence_after_sync();
 }
 
-// The 28 slice pairs with p + q <= 6 (weight w = p + q into accumulator w),
-// issued by one thread, with their completion committed to s.bar.
+// The 28 slice pairs with p + q <= 6 (weight w = p + q into accumulator w,
+// TMEM columns 64 w ..), issued by one thread, with their completion
+// committed to s.bar.  W's slices lie one after another in shared memory and
+// the accumulators side by side in TMEM, so slice p of the right-hand sides
+// meets W's slices q = 0 .. 6 - p in MMAs as wide as N = 256 allows: rows
+// 64 q of the stacked slices feed accumulator p + q.  That is 10 MMAs per
+// 16-wide K step instead of 28, each reading the right-hand-side slice from
+// shared memory once (the 28 narrow MMAs were bound by shared-memory reads).
+// The accumulators hold exact integers, so the order of the sums is free.
 __device__ __forceinline__ void lp_issue(const LpShared& s, uint32_t tmem) {
   using namespace split7;
-  const uint32_t idesc = umma::idesc_f16(LP_COLS, LEAF_INV_N, true);
   const uint32_t a0 = umma::smem_u32(s.sA), b0 = umma::smem_u32(s.sB);
 #pragma unroll 1
-  for (int w = 0; w < SLICES; ++w)
-    for (int p = 0; p <= w; ++p) {
+  for (int p = 0; p < SLICES; ++p) {
+    const int rows = LEAF_INV_N * (SLICES - p);
+#pragma unroll 1
+    for (int r0 = 0; r0 < rows; r0 += 256) {
+      const int nn = min(256, rows - r0);
+      const uint32_t idesc = umma::idesc_f16(LP_COLS, nn, true);
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk)
-        umma::mma_f16(tmem + (uint32_t)(w * LEAF_INV_N), umma::desc_kmajor_sw128(a0 + p * LP_COLS * 128 + kk * 32),
-                      umma::desc_kmajor_sw128(b0 + (w - p) * LEAF_INV_N * 128 + kk * 32), idesc,
-                      (p > 0 || kk > 0) ? 1u : 0u);
+        umma::mma_f16(tmem + (uint32_t)(p * LEAF_INV_N + r0), umma::desc_kmajor_sw128(a0 + p * LP_COLS * 128 + kk * 32),
+                      umma::desc_kmajor_sw128(b0 + r0 * 128 + kk * 32), idesc, (p > 0 || kk > 0) ? 1u : 0u);
     }
+  }
   umma::mma_commit(umma::smem_u32(s.bar));
 }
 
@@ -732,9 +742,6 @@ int launch_inverses(const RecPlan& c, const double* A, int64_t lda, int tA, cons
 bool leaf_inverses_wanted(const RecPlan& c) {
   if (c.mode != GEMM_MIXED || c.S != EXACT_SLICES || !c.bf16 || c.func != 'S' || c.dtype != NLA_F64) return false;
   if (c.threshold > LEAF_INV_N) return false;
-  // The leaf overwrites X from the finishing pass (NLA_EXACT_FINISH=0 removes it).
-  const char* f = std::getenv("NLA_EXACT_FINISH");
-  if (f && f[0] == '0') return false;
   const char* v = std::getenv("NLA_MIXED_INV_LEAF");
   return !(v && v[0] == '0');
 }
