@@ -928,18 +928,22 @@ __global__ void __launch_bounds__(XR_THREADS, 1) batched_exact_residual_kernel(E
     __syncthreads();
     umma::fence_after_sync();
     if (t == 0) {
-      const uint32_t idesc = umma::idesc_f16(XR_ROWS, XR_COLS, true);
+      // Slice p of A against X's slices q = 0 .. 6 - p, stacked in shared
+      // memory, into the adjacent accumulators p + q: MMAs up to N = 256
+      // wide, 10 per 16-wide K step instead of 28 (exact integer sums, so
+      // the order is free).
       const uint32_t a0 = umma::smem_u32(sA), x0 = umma::smem_u32(sX);
 #pragma unroll 1
-      for (int w = 0; w < XR_SL; ++w) {
-        for (int p = 0; p <= w; ++p) {
-          const int qq = w - p;
+      for (int p = 0; p < XR_SL; ++p) {
+        const int rows = XR_COLS * (XR_SL - p);
+#pragma unroll 1
+        for (int q0 = 0; q0 < rows; q0 += 256) {
+          const int nn = min(256, rows - q0);
+          const uint32_t idesc = umma::idesc_f16(XR_ROWS, nn, true);
 #pragma unroll
           for (int kk = 0; kk < XR_KB / 16; ++kk)
-            umma::mma_f16(tmem + (uint32_t)(w * XR_COLS),
-                          umma::desc_kmajor_sw128(a0 + p * XR_ROWS * 128 + kk * 32),
-                          umma::desc_kmajor_sw128(x0 + qq * XR_COLS * 128 + kk * 32), idesc,
-                          (p > 0 || kk > 0) ? 1u : 0u);
+            umma::mma_f16(tmem + (uint32_t)(p * XR_COLS + q0), umma::desc_kmajor_sw128(a0 + p * XR_ROWS * 128 + kk * 32),
+                          umma::desc_kmajor_sw128(x0 + q0 * 128 + kk * 32), idesc, (p > 0 || kk > 0) ? 1u : 0u);
         }
       }
       umma::mma_commit(umma::smem_u32(mma_bar));

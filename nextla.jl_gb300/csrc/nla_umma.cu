@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t idesc = umma::idesc_f16(BM, BN, true);
+      const uint32_t idesc = umma::idesc_f16(BM, BN, true), idesc2 = umma::idesc_f16(BM, 2 * BN, true);
       int it = 0, ch = 0;
       for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
         const int c0 = max(kb0, cc * EX_CHUNK), c1 = min(kb1, (cc + 1) * EX_CHUNK);
@@ -663,18 +663,21 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
-// Exact kernel with coupled pairs.  The 28 pairs (p, q) are walked as 16
-// groups: for each B slice q, the A slices p = 0, 2, 4, 6 each with its
-// successor p + 1 while p + 1 <= 6 - q.  A group's stage holds A_p, A_p+1
-// (one 256-row box: the staging puts the slices of a tile next to each
-// other) and B_q, 48 KiB in all, and feeds two accumulators, so a pair costs
-// 24 KiB of tile loads instead of 32: the TMA feed, not the tensor core,
-// bounds these kernels (about 100-120 GB/s per SM).
-// Each group's two accumulators (weights p + q and p + 1 + q) take half of a
-// 256-column TMEM buffer; two buffers fill the 512 columns.  Updates with
-// K <= 256 use a second table (below) in which the pairs of one weight share
-// an accumulator.  Plain updates store the tile's fixed-point sums for
-// exact_finish_kernel; residuals apply them here (exact_store).
+// Exact kernel with coupled pairs.  The 28 slice pairs (A_a, B_b), a + b <= 6,
+// are walked as 16 groups: for each A slice a, the B slices b = 0, 2, 4, 6
+// each with its successor b + 1 while b + 1 <= 6 - a.  A group's stage holds
+// A_a and B_b, B_b+1 (one 256-row box: the staging puts the slices of a tile
+// next to each other), 48 KiB in all, and feeds two adjacent accumulators
+// (weights a + b and a + b + 1) with one MMA of N = 256.  A pair costs 24 KiB
+// of tile loads instead of 32 (the TMA feed bounds these kernels, about
+// 100-120 GB/s per SM), and 12 KiB of shared-memory operand reads per 16-wide
+// K step instead of 16 (two N = 128 MMAs that shared one B tile, the earlier
+// form, read at the 128 B per clock that shared memory delivers).
+// Each group's two accumulators take half of a 256-column TMEM buffer; two
+// buffers fill the 512 columns.  Updates with K <= 256 use a second table
+// (below) in which the pairs of one weight share an accumulator.  Plain
+// updates store the tile's fixed-point sums for exact_finish_kernel;
+// residuals apply them here (exact_store).
 // Warps: 0 loads A, 1 issues the MMAs, 2 loads B, 3-10 drain.
 // ---------------------------------------------------------------------------
 constexpr int CP_STAGES = 4;
@@ -685,9 +688,11 @@ static_assert(CP_DYN_SMEM + 16 <= 232448, "coupled exact kernel shared memory ab
 
 // Group tables.  A group is drained as one or two accumulators (d0, d1) of
 // weights w0, w1; it is filled by segments, each one K loop of one slice
-// pair (p, q) into d0 or d1, or of the coupled pairs (p, q) -> d0 and
-// (p + 1, q) -> d1 that share the B_q tile.  A segment's init bits mark the
-// first write into each accumulator (its MMAs start with enable_input_d 0).
+// pair (A_q, B_p) into d0 or d1, or of the coupled pairs (A_q, B_p) -> d0
+// and (A_q, B_p+1) -> d1 that share the A_q tile (the entries name B's slice
+// first: the pair set is symmetric, so p and q range as in (A_p, B_q)).  A
+// segment's init bits mark the first write into each accumulator (its MMAs
+// start with enable_input_d 0); a coupled segment's two bits are equal.
 //   segment: p | q << 4 | coupled << 8 | dst << 9 | init0 << 10 | init1 << 11
 //   group:   first segment | segment count << 8 | w0 << 12 | w1 << 16 (15: no d1)
 constexpr uint16_t cp_seg(int p, int q, int two, int dst, int i0, int i1) {
@@ -741,8 +746,8 @@ __device__ __forceinline__ CpSeg cp_seg_at(int i) {
 }
 
 __global__ void __launch_bounds__(EX_THREADS, 1)
-    umma_exact_coupled_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmA2,
-                              const __grid_constant__ CUtensorMap tmB, const ExactParams p) {
+    umma_exact_coupled_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                              const __grid_constant__ CUtensorMap tmB2, const ExactParams p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* fullA = reinterpret_cast<uint64_t*>(smem + CP_STAGES * CP_STAGE_BYTES);  // A producer's loads
@@ -814,13 +819,15 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
               const uint32_t fb = umma::smem_u32(&own[s]);
               uint8_t* st = smem + s * CP_STAGE_BYTES;
               // Staged rows: slice sl of the tile at row r0 starts at r0 * 7 + sl * 128,
-              // so A_p and A_p+1 are one 256-row box.
+              // so B_p and B_p+1 are one 256-row box.  A segment (p, q) takes
+              // A's slice q against B's slice p (and p + 1).
               if (is_a) {
-                umma::mbar_arrive_expect_tx(fb, (uint32_t)((sg.two ? 2 : 1) * TILE_BYTES));
-                umma::tma_load_2d(umma::smem_u32(st), sg.two ? &tmA2 : &tmA, fb, kb * BK, m0 * EX_SLICES + sg.p * BM);
-              } else {
                 umma::mbar_arrive_expect_tx(fb, (uint32_t)TILE_BYTES);
-                umma::tma_load_2d(umma::smem_u32(st + 2 * TILE_BYTES), &tmB, fb, kb * BK, n0 * EX_SLICES + sg.q * BN);
+                umma::tma_load_2d(umma::smem_u32(st), &tmA, fb, kb * BK, m0 * EX_SLICES + sg.q * BM);
+              } else {
+                umma::mbar_arrive_expect_tx(fb, (uint32_t)((sg.two ? 2 : 1) * TILE_BYTES));
+                umma::tma_load_2d(umma::smem_u32(st + TILE_BYTES), sg.two ? &tmB2 : &tmB, fb, kb * BK,
+                                  n0 * EX_SLICES + sg.p * BN);
               }
             }
           }
@@ -830,7 +837,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t idesc = umma::idesc_f16(BM, BN, true);
+      const uint32_t idesc = umma::idesc_f16(BM, BN, true), idesc2 = umma::idesc_f16(BM, 2 * BN, true);
       int it = 0, ch = 0;
       for (int cc = kb0 / EX_CHUNK; cc * EX_CHUNK < kb1 && ok; ++cc) {
         const int c0 = max(kb0, cc * EX_CHUNK), c1 = min(kb1, (cc + 1) * EX_CHUNK);
@@ -849,10 +856,14 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
           for (int si = s0; si < s0 + ns && ok; ++si) {
             const CpSeg sg = cp_seg_at(si);
             // The first MMA of a segment starts an accumulator the segment
-            // initialises and adds to one an earlier segment started.
+            // initialises and adds to one an earlier segment started.  A
+            // coupled segment is one MMA of N = 256 into both accumulators
+            // (adjacent in TMEM), against B's two slices (adjacent in shared
+            // memory); its two accumulators start together (init0 == init1
+            // for every coupled segment of the tables).
             const uint32_t first0 = sg.two ? (sg.init0 ? 0u : 1u) : (sg.dst ? (sg.init1 ? 0u : 1u) : (sg.init0 ? 0u : 1u));
-            const uint32_t first1 = sg.init1 ? 0u : 1u;
             const uint32_t dA = sg.two ? d0 : (sg.dst ? d1 : d0);
+            const uint32_t id = sg.two ? idesc2 : idesc;
             for (int kb = c0; kb < c1; ++kb, ++it) {
               const int s = it % CP_STAGES;
               if (!umma::mbar_wait(umma::smem_u32(&fullA[s]), (uint32_t)(it / CP_STAGES) & 1u, &s_abort,
@@ -863,18 +874,11 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
                 break;
               }
               umma::fence_after_sync();
-              const uint32_t a0 = umma::smem_u32(smem + s * CP_STAGE_BYTES);
-              const uint32_t a1 = a0 + TILE_BYTES, b0 = a0 + 2 * TILE_BYTES;
+              const uint32_t a0 = umma::smem_u32(smem + s * CP_STAGE_BYTES), b0 = a0 + TILE_BYTES;
 #pragma unroll
               for (int kk = 0; kk < BK / 16; ++kk)
-                umma::mma_f16(dA, umma::desc_kmajor_sw128(a0 + kk * 32), umma::desc_kmajor_sw128(b0 + kk * 32), idesc,
+                umma::mma_f16(dA, umma::desc_kmajor_sw128(a0 + kk * 32), umma::desc_kmajor_sw128(b0 + kk * 32), id,
                               (kb > c0 || kk > 0) ? 1u : first0);
-              if (sg.two) {
-#pragma unroll
-                for (int kk = 0; kk < BK / 16; ++kk)
-                  umma::mma_f16(d1, umma::desc_kmajor_sw128(a1 + kk * 32), umma::desc_kmajor_sw128(b0 + kk * 32),
-                                idesc, (kb > c0 || kk > 0) ? 1u : first1);
-              }
               umma::mma_commit(umma::smem_u32(&empty[s]));
             }
           }
@@ -1368,10 +1372,10 @@ bool exact_merged_enabled() {
 int launch_exact_coupled(const ExactParams& params, const Staged& A, const Staged& B, cudaStream_t s) {
   ExactParams p = params;
   p.merged = A.K_pad <= CP_MERGED_MAX_K && exact_merged_enabled() ? 1 : 0;
-  CUtensorMap mA, mA2, mB;
+  CUtensorMap mA, mB, mB2;
   NLA_TRY(make_map(&mA, A.slices, true, (uint64_t)A.K_pad, (uint64_t)(EX_SLICES * A.rows_pad)));
-  NLA_TRY(make_map(&mA2, A.slices, true, (uint64_t)A.K_pad, (uint64_t)(EX_SLICES * A.rows_pad), 2 * BM));
   NLA_TRY(make_map(&mB, B.slices, true, (uint64_t)B.K_pad, (uint64_t)(EX_SLICES * B.rows_pad)));
+  NLA_TRY(make_map(&mB2, B.slices, true, (uint64_t)B.K_pad, (uint64_t)(EX_SLICES * B.rows_pad), 2 * BN));
   static std::once_flag once;
   static cudaError_t st = cudaSuccess;
   std::call_once(once, [] {
@@ -1380,7 +1384,7 @@ int launch_exact_coupled(const ExactParams& params, const Staged& A, const Stage
   if (st != cudaSuccess) return cuda_status(st, "cudaFuncSetAttribute(umma_exact_coupled_kernel)");
   const int64_t grid = (int64_t)p.tiles_m * p.tiles_n;
   if (grid > 2147483647LL) return fail(NLA_ERR_UNSUPPORTED, "too many output tiles");
-  umma_exact_coupled_kernel<<<(unsigned)grid, EX_THREADS, CP_DYN_SMEM, s>>>(mA, mA2, mB, p);
+  umma_exact_coupled_kernel<<<(unsigned)grid, EX_THREADS, CP_DYN_SMEM, s>>>(mA, mB, mB2, p);
   NLA_CHECK_LAUNCH("umma_exact_coupled_kernel");
   return NLA_OK;
 }
