@@ -39,6 +39,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -86,7 +87,7 @@ def parse():
     ap.add_argument("--sweep-plain", action="store_true",
                     help="plain F32/F64 TRSM and TRMM over the 8 side/uplo/trans forms, alpha 0.5 (config 1)")
     ap.add_argument("--sizes", default="4096,8192,16384")
-    ap.add_argument("--kernel-case", choices=["exact", "fast", "leaf", "dfma"], default=None,
+    ap.add_argument("--kernel-case", choices=["exact", "fast", "leaf", "pair", "dfma"], default=None,
                     help="run single launches of one kernel on a moderate case (for ncu captures)")
     ap.add_argument("--case-size", type=int, default=4096)
     ap.add_argument("--case-reps", type=int, default=2)
@@ -756,6 +757,9 @@ def run_kernel_case(args):
       fast   the same with 3 BF16 slices (FP32 accumulation);
       leaf   one FP64 diagonal-block solve of order 128 with 8 s right-hand
              sides (--case-shape n,m for order n with m right-hand sides);
+      pair   one exact mixed solve (L/L/N, 7 BF16 slices, 0 sweeps) of order
+             s with 4 s right-hand sides, whose 128-row nodes each run one
+             leaf_pair_kernel launch (s / 128 per solve);
       dfma   one FP64 update on CUDA cores, s x s x s."""
     import torch
 
@@ -786,6 +790,13 @@ def run_kernel_case(args):
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
             pkg.LeftLowerTRSM_(A, B)
+        elif args.kernel_case == "pair":
+            A = (cm(s, s) / math.sqrt(s)).tril_(-1)
+            A.diagonal().copy_(2.0 + torch.randn(s, generator=g, device=dev, dtype=torch.float64).abs())
+            B = torch.rand(4 * s, s, generator=g, device=dev, dtype=torch.float64).T * 2.0 - 1.0
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            pkg.unified_rectrxm_mixed_("L", "L", "N", 1.0, "S", A, B, split_terms=7, sweeps=0)
         else:
             A, B, C = cm(s, s), cm(s, s), cm(s, s)
             torch.cuda.synchronize(dev)
