@@ -135,11 +135,8 @@ int launch_scale_complex(int dtype, int64_t rows, int64_t cols, double alpha_re,
 // Tensor-core update on staged slices (nla_umma.cu).  C (M x N) += alpha *
 // op(A) (M x K) * op(B) (K x N); in_dtype NLA_F64 (split into S BF16/FP16
 // slices) or NLA_F16 (one unscaled slice); out_dtype NLA_F64 or NLA_F16.
-// With overwrite (exact 7-slice products only) C := alpha * op(A) op(B); C may
-// then be the same matrix as B (both operands are staged before C is written).
 int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat& A, const Mat& B, const Mat& C,
-                       int in_dtype, int out_dtype, int S, bool bf16, void* ws, size_t ws_bytes, cudaStream_t s,
-                       bool overwrite = false);
+                       int in_dtype, int out_dtype, int S, bool bf16, void* ws, size_t ws_bytes, cudaStream_t s);
 size_t sliced_workspace_bytes(int64_t M, int64_t N, int64_t K, int S);
 
 // An operand staged for the tensor cores: S K-major 16-bit slices of a
@@ -176,8 +173,7 @@ struct ResidualTerm {
 // fixed_buf (A.rows_pad x N int64, or null) lets a plain update leave its
 // fixed-point sums there for a separate finishing pass over C.
 int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat& C, bool trans_out,
-                      cudaStream_t s, const ResidualTerm* res = nullptr, long long* fixed_buf = nullptr,
-                      bool overwrite = false);
+                      cudaStream_t s, const ResidualTerm* res = nullptr, long long* fixed_buf = nullptr);
 constexpr int EXACT_SLICES = 7;
 int workspace_get(cudaStream_t s, size_t bytes, void** out);
 int device_status(cudaStream_t s);

@@ -174,9 +174,11 @@ int default_mixed_cutoff() {
 // is a large share of a solve whose updates run on the tensor cores.  Here
 // each leaf block T (at most 64 rows) is inverted once in FP64, and the leaf
 // becomes X := inv(T) X, an exact 7-slice product on the tensor cores
-// rounded once per element.  (X + (inv(T) - I) X, which needs no overwrite,
-// loses digits to cancellation when T's diagonal is large: x ~ b / d from
-// b - (1 - 1/d) b.)
+// rounded once per element.  (X + (inv(T) - I) X, the form a general
+// accumulating update would give, loses digits to cancellation when T's
+// diagonal is large: x ~ b / d from b - (1 - 1/d) b.)  Where both halves of
+// a recursion node are leaves, leaf_pair_kernel runs the two leaves and the
+// update between them in one launch.
 // ---------------------------------------------------------------------------
 namespace {
 

@@ -304,7 +304,6 @@ struct ExactParams {
   // P[i + j * ldp]) and exact_finish_kernel applies them to C.
   long long* P;
   int64_t ldp;
-  int overwrite;  // exact_finish_kernel: C := alpha * P instead of C += alpha * P
 };
 
 // K range of the staged triangle that meets rows [r0, r0 + span).
@@ -440,7 +439,7 @@ __global__ void __launch_bounds__(256) exact_finish_kernel(const ExactParams p) 
       const int64_t col = cbase + c0 + c;
       const bool in = col < p.N;
       v[c] = in ? p.P[(int64_t)i + col * p.ldp] : 0;
-      cv[c] = in && !p.overwrite ? static_cast<const double*>(p.C)[(int64_t)i + col * p.ldc] : 0.0;
+      cv[c] = in ? static_cast<const double*>(p.C)[(int64_t)i + col * p.ldc] : 0.0;
       ej[c] = in ? p.eb[col] : 0;
     }
 #pragma unroll
@@ -1569,12 +1568,9 @@ size_t sliced_workspace_bytes(int64_t M, int64_t N, int64_t K, int S) {
 // One tensor-core update.  in_dtype is NLA_F64 (split into S slices of BF16
 // or FP16) or NLA_F16 (S = 1, staged as is).  out_dtype is NLA_F64 or NLA_F16.
 int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat& A, const Mat& B, const Mat& C,
-                       int in_dtype, int out_dtype, int S, bool bf16, void* ws, size_t ws_bytes, cudaStream_t s,
-                       bool overwrite) {
+                       int in_dtype, int out_dtype, int S, bool bf16, void* ws, size_t ws_bytes, cudaStream_t s) {
   if (M <= 0 || N <= 0 || K <= 0) return NLA_OK;
   if (C.t) return fail(NLA_ERR_UNSUPPORTED, "tensor-core update: transposed output view");
-  if (overwrite && (S != EXACT_SLICES || in_dtype != NLA_F64))
-    return fail(NLA_ERR_UNSUPPORTED, "tensor-core update: overwrite needs the exact 7-slice products");
   const bool copy = in_dtype == NLA_F16;
   if (copy) S = 1;
   if (S == EXACT_SLICES && !copy) {
@@ -1602,7 +1598,7 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
       NLA_TRY(stage_operand(transposed(B), N, K, NLA_F64, S, true, 0, static_cast<uint8_t*>(base) + sa, &Bs, s,
                             false));
     }
-    return launch_exact_gemm(As, Bs, alpha, C, false, s, nullptr, fixed, overwrite);
+    return launch_exact_gemm(As, Bs, alpha, C, false, s, nullptr, fixed);
   }
   if (S < 1 || S > 3) return fail(NLA_ERR_ARG, "split terms must be 1, 2, 3 or 7");
   const int beta = bf16 ? 8 : 11;
@@ -1693,7 +1689,7 @@ int launch_sliced_gemm(int64_t M, int64_t N, int64_t K, double alpha, const Mat&
 // C (M x N, FP64) += alpha * A * B^T from two operands staged with
 // EX_SLICES BF16 slices (A: M rows, B: N rows, same K).
 int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat& C, bool trans_out,
-                      cudaStream_t s, const ResidualTerm* res, long long* fixed_buf, bool overwrite) {
+                      cudaStream_t s, const ResidualTerm* res, long long* fixed_buf) {
   const int64_t M = A.rows, N = B.rows, K = A.K;
   if (M <= 0 || N <= 0 || K <= 0) return NLA_OK;
   if (B.K != K || A.S != EX_SLICES || B.S != EX_SLICES || !A.bf16 || !B.bf16 || !A.scaled || !B.scaled)
@@ -1741,10 +1737,6 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
   if (fixed_buf && !res && !trans_out && exact_finish_enabled() && (N + FINISH_COLS - 1) / FINISH_COLS <= 65535) {
     p.P = fixed_buf;
     p.ldp = A.rows_pad;
-    p.overwrite = overwrite ? 1 : 0;
-  } else if (overwrite) {
-    // Only the finishing pass writes C without reading it.
-    return fail(NLA_ERR_UNSUPPORTED, "exact update: overwrite needs the finishing pass and its workspace");
   }
   const int rc = exact_coupled() ? launch_exact_coupled(p, A, B, s) : launch_exact_pairs(p, A, B, s);
   if (rc != NLA_OK || !p.P) return rc;
