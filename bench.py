@@ -170,13 +170,15 @@ PLAIN_STEPS = 3  # timed solves of the plain FP64 comparison
 E2E_STEPS = 15   # synchronised end-to-end steps (host buffers to host result)
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
-# exact tensor-core kernel, averaged over the 255 updates of one default
-# solve at n = m = 16384.  ncu cannot run inside the timed bench, so this is
+# exact tensor-core kernel, averaged over the 127 updates of one default
+# solve at n = m = 16384 (the 128 updates between sibling leaves run inside
+# the leaf pair kernel).  ncu cannot run inside the timed bench, so this is
 # the figure of one ncu capture of the same workload, with the commit and
 # command it was taken on (TRAFFIC_SOURCE).
-TRAFFIC_BYTES_PER_LAUNCH = 214.7e6
-TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:umma_exact -s 510 -c 510 "
-                  "python bench.py --steps 1 --warmup 1 --no-plain --no-cpu-baseline, at commit cd51b7e")
+TRAFFIC_BYTES_PER_LAUNCH = 421.6e6
+TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:umma_exact "
+                  "-s 127 -c 127 python bench.py --steps 1 --warmup 1 --no-plain --no-cpu-baseline (the timed "
+                  "solve's 127 updates), at commit 125abf4")
 
 
 def make_inputs(n, m, seed=0):
