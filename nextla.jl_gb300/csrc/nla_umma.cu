@@ -671,7 +671,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
 // of tile loads instead of 32 (the TMA feed bounds these kernels, about
 // 100-120 GB/s per SM), and 12 KiB of shared-memory operand reads per 16-wide
 // K step instead of 16 (two N = 128 MMAs that shared one B tile, the earlier
-// form, read at the 128 B per clock that shared memory delivers).
+// form, read close to the 128 B per clock that shared memory delivers).
 // Each group's two accumulators take half of a 256-column TMEM buffer; two
 // buffers fill the 512 columns.  Updates with K <= 256 use a second table
 // (below) in which the pairs of one weight share an accumulator.  Plain
