@@ -1194,7 +1194,7 @@ struct StageJob {
 // nrm[] itself, so no memsets, no atomics and one launch replace the eight
 // stream operations of two separately staged operands.
 template <typename Sl, int NS>
-__global__ void __launch_bounds__(256, 3) stage_pair_kernel(const StageJob a, const StageJob b) {
+__global__ void __launch_bounds__(256, 4) stage_pair_kernel(const StageJob a, const StageJob b) {
   __shared__ double tile[2][32][65];
   __shared__ int sred[8][32];
   __shared__ int sexp[32];
