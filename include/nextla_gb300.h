@@ -387,12 +387,14 @@ NLA_API int nla_measure_pipes(double* dfma_tflops, double* dmma_tflops, double* 
 /*
  * Kernel tracing (no counterpart in the reference, which has no tracing).
  * nla_trace_enable(1) clears earlier records and starts recording; every
- * library kernel launched afterwards is bracketed by CUDA events on its
- * stream together with its algorithmic flops and bytes.  nla_trace_enable(0)
- * stops recording.  nla_trace_summary() waits for the recorded events and
- * returns, for one kernel class, the number of launches, their summed device
- * time in milliseconds and their summed algorithmic flops and bytes.  Do not
- * trace work that is being captured into a CUDA graph.
+ * library operation launched afterwards (one kernel, or a few that belong
+ * together, such as an update and its finishing pass) is bracketed by CUDA
+ * events on its stream together with its algorithmic flops and bytes.
+ * nla_trace_enable(0) stops recording.  nla_trace_summary() waits for the
+ * recorded events and returns, for one kernel class, the number of kernel
+ * launches (copies count one each), their summed device time in milliseconds
+ * and their summed algorithmic flops and bytes.  Do not trace work that is
+ * being captured into a CUDA graph.
  */
 #define NLA_K_LEAF_SOLVE 0 /* diagonal-block solve */
 #define NLA_K_LEAF_MULT 1  /* diagonal-block multiply */

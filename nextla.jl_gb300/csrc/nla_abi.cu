@@ -39,6 +39,8 @@ struct TraceRec {
   int kclass;
   cudaEvent_t e0, e1;
   double flops, bytes;
+  int kernels;       // kernel launches inside the scope
+  TraceRec* parent;  // the scope open around this one on the same thread
 };
 std::mutex g_trace_mu;
 std::atomic<bool> g_trace_on{false};
@@ -68,6 +70,7 @@ void clear_trace_locked() {
 
 namespace {
 thread_local int t_trace_class = -1;  // TraceClassScope's override, or -1
+thread_local TraceRec* t_trace_open = nullptr;  // innermost recording scope of this thread
 }
 
 TraceClassScope::TraceClassScope(int kclass) : prev(t_trace_class) { t_trace_class = kclass; }
@@ -78,15 +81,23 @@ void trace_begin(int kclass, cudaStream_t s, double flops, double bytes, void** 
   if (!g_trace_on.load(std::memory_order_relaxed)) return;
   if (t_trace_class >= 0) kclass = t_trace_class;
   std::lock_guard<std::mutex> lk(g_trace_mu);
-  TraceRec* r = new TraceRec{kclass, pooled_event(), pooled_event(), flops, bytes};
+  TraceRec* r = new TraceRec{kclass, pooled_event(), pooled_event(), flops, bytes, 1, t_trace_open};
   cudaEventRecord(r->e0, s);
   g_trace.push_back(r);
+  t_trace_open = r;
   *handle = r;
 }
 
 void trace_end(void* handle, cudaStream_t s) {
   TraceRec* r = static_cast<TraceRec*>(handle);
   cudaEventRecord(r->e1, s);
+  if (t_trace_open == r) t_trace_open = r->parent;
+}
+
+void trace_kernels(int extra) {
+  if (!t_trace_open) return;
+  std::lock_guard<std::mutex> lk(g_trace_mu);
+  t_trace_open->kernels += extra;
 }
 
 int num_sms() {
@@ -364,7 +375,7 @@ int nla_trace_summary(int kernel_class, int64_t* launches, double* ms, double* f
     float x = 0;
     e = cudaEventElapsedTime(&x, r->e0, r->e1);
     if (e != cudaSuccess) return cuda_status(e, "nla_trace_summary");
-    ++n;
+    n += r->kernels;
     t += x;
     f += r->flops;
     b += r->bytes;

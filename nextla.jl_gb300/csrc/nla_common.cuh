@@ -95,6 +95,9 @@ template <> struct Elem<__half> {
 // ---------------------------------------------------------------------------
 void trace_begin(int kclass, cudaStream_t s, double flops, double bytes, void** handle);
 void trace_end(void* handle, cudaStream_t s);
+// Counts `extra` more kernel launches in the innermost recording scope of
+// this thread (a scope counts one launch unless told otherwise).
+void trace_kernels(int extra);
 
 struct TraceScope {
   void* h = nullptr;

@@ -735,6 +735,7 @@ int launch_inverses(const RecPlan& c, const double* A, int64_t lda, int tA, cons
     }
     leaf_inverse_kernel<<<(unsigned)g.count, 256, INV_SMEM, c.s>>>(g);
     NLA_CHECK_LAUNCH("leaf_inverse_kernel");
+    if (j0 > 0) trace_kernels(1);
   }
   return NLA_OK;
 }

@@ -1496,6 +1496,7 @@ int stage_operand(const Mat& X, int64_t rows, int64_t K, int in_dtype, int S, bo
     }
   }
   NLA_CHECK_LAUNCH("split_kernel");
+  trace_kernels(1);  // row_exp_kernel and split_kernel
   return NLA_OK;
 }
 
@@ -1743,6 +1744,7 @@ int launch_exact_gemm(const Staged& A, const Staged& B, double alpha, const Mat&
   const int64_t gy = (N + FINISH_COLS - 1) / FINISH_COLS;
   exact_finish_kernel<<<dim3((unsigned)((M + 255) / 256), (unsigned)gy), 256, 0, s>>>(p);
   NLA_CHECK_LAUNCH("exact_finish_kernel");
+  trace_kernels(1);  // the exact kernel and its finishing pass
   return NLA_OK;
 }
 
